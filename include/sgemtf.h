@@ -1,0 +1,233 @@
+/*
+ * sgemtf.h -- C ABI of the GB300 evolutionary-multitasking engine.
+ *
+ * One handle owns a set of optimisation tasks.  Each task is one island of
+ * NP individuals in D dimensions that evolves on one benchmark function of a
+ * shifted, rotated argument z = Q (x - o).  All populations stay resident on
+ * one GPU; one emt_run() call advances every task by a number of generations
+ * (DE/rand/1/bin, DE/current/1/bin or SBX + polynomial-mutation GA), with
+ * periodic elite transfer between tasks.
+ *
+ * The reference program has no library interface: its replaceable unit is the
+ * per-task host function
+ *     void iter(int task_idx, int cthread_idx, cudaStream_t* streams)
+ *         (proposed model/SG-EMTF.cu:1646, SG-EMTF_DE.cu:1576)
+ * with the kernels it launches.  Each entry point below names the reference
+ * code it replaces.
+ *
+ * Conventions
+ *   - Every call returns EMT_OK (0) or an emt_status error code; the message
+ *     of the last failure on a handle is in emt_last_error().
+ *   - The handle owns all device memory.  Caller buffers are HOST memory and
+ *     are copied in or out; no device pointer crosses this interface except
+ *     the optional CUDA stream (a cudaStream_t passed as void*; NULL = the
+ *     legacy default stream).
+ *   - A handle is used by one host thread at a time.  Calls on different
+ *     handles are independent: the library keeps no global mutable state.
+ *   - Random numbers come from a counter-based Philox4x32-10 stream keyed by
+ *     emt_config.seed, so a run is reproducible bit for bit: the same seed and
+ *     call sequence give the same populations on every run.
+ *
+ * Function ids follow the order sphere, rastrigin, ackley, griewank,
+ * rosenbrock, schwefel, weierstrass.  The reference numbers the same functions
+ * 0 Sphere, 1 Rosenbrock, 2 Ackley, 3 Rastrigin, 4 Griewank, 5 Weierstrass,
+ * 6 Schwefel (proposed model/SG-EMTF.cu:917-1101); emt_function_from_reference
+ * converts.
+ */
+#ifndef SGEMTF_H
+#define SGEMTF_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EMT_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define EMT_API __attribute__((visibility("default")))
+#else
+#define EMT_API
+#endif
+
+/* Opaque engine handle; owns the device state of its tasks. */
+typedef struct emt_handle emt_handle_t;
+
+typedef enum emt_status {
+  EMT_OK = 0,
+  EMT_ERR_INVALID_ARG = 1,   /* bad pointer, size or enum value           */
+  EMT_ERR_OUT_OF_MEMORY = 2, /* a device or host allocation failed         */
+  EMT_ERR_CUDA = 3,          /* a CUDA runtime call or kernel failed       */
+  EMT_ERR_DEVICE_TIMEOUT = 4,/* a bounded device-side wait gave up         */
+  EMT_ERR_STATE = 5,         /* call out of order (e.g. no tasks yet)      */
+  EMT_ERR_UNSUPPORTED = 6,   /* valid request this build cannot serve      */
+  EMT_ERR_DEVICE_CHECK = 7   /* a kernel's own bounds/descriptor check fired */
+} emt_status;
+
+typedef enum emt_algorithm {
+  EMT_DE_RAND1_BIN = 0,    /* v = x_r1 + F (x_r2 - x_r3), binomial crossover  */
+  EMT_DE_CURRENT1_BIN = 1, /* v = x_i  + F (x_r2 - x_r3): the reference's DE,
+                              proposed model/SG-EMTF_DE.cu:547-600,474-495    */
+  EMT_GA_SBX_PM = 2        /* SBX crossover + polynomial mutation: the
+                              reference's GA, SG-EMTF.cu:548-750,772-831      */
+} emt_algorithm;
+
+/* Arithmetic of the rotation z = Q (x - o) behind every evaluation. */
+typedef enum emt_precision {
+  EMT_ROT_FP32 = 0,   /* FP32 FMA on CUDA cores                          */
+  EMT_ROT_TF32X3 = 1, /* tcgen05 tensor cores, hi/lo TF32 split, 3 products,
+                         FP32 accumulation in tensor memory               */
+  EMT_ROT_AUTO = 2    /* the fastest form the device supports            */
+} emt_precision;
+
+typedef enum emt_function {
+  EMT_SPHERE = 0,
+  EMT_RASTRIGIN = 1,
+  EMT_ACKLEY = 2,
+  EMT_GRIEWANK = 3,
+  EMT_ROSENBROCK = 4,
+  EMT_SCHWEFEL = 5,
+  EMT_WEIERSTRASS = 6,
+  EMT_NUM_FUNCTIONS = 7
+} emt_function;
+
+typedef enum emt_rotation {
+  EMT_ROTATION_IDENTITY = 0,  /* z = x - o                                  */
+  EMT_ROTATION_SEEDED_QR = 1, /* Q = orthogonal factor of the FP64 QR of a
+                                 seeded N(0,1) D x D matrix, stored FP32     */
+  EMT_ROTATION_DENSE = 2,     /* Q given by the caller (FP64, row-major)    */
+  EMT_ROTATION_DIAG = 3       /* z = m .* (x - o): the reference's
+                                 z = M[d] * (x + b[d]) with o = -b
+                                 (SG-EMTF.cu:181-195, use at :922)          */
+} emt_rotation;
+
+/* Reference-compatibility switches (emt_config.flags). */
+#define EMT_FLAG_REF_GRIEWANK_NO_PRODUCT 0x1u /* GA file drops the product
+                                                 term (SG-EMTF.cu:1029)      */
+#define EMT_FLAG_REF_WEIERSTRASS_CONST 0x2u   /* offset computed as the host
+                                                 code does, PI = 3.1415926,
+                                                 float cosf (SG-EMTF.cu:354-361) */
+#define EMT_FLAG_REF_ACKLEY_E 0x4u            /* E = 2.718282 (SG-EMTF.cu:54) */
+#define EMT_FLAG_REF_BOXES 0x8u               /* box table of SG-EMTF.cu:197-214 */
+#define EMT_FLAG_NO_RECHECK 0x10u             /* select on FP32 fitness only */
+
+typedef struct emt_config {
+  int32_t algorithm;         /* emt_algorithm                                */
+  int32_t precision;         /* emt_precision                                */
+  float F;                   /* DE scale factor (reference 0.5, SG-EMTF_DE.cu:43) */
+  float CR;                  /* DE crossover rate (reference 0.6, :39)       */
+  float eta_c;               /* SBX distribution index (reference 2, SG-EMTF.cu:46) */
+  float p_c;                 /* per-gene SBX probability (reference 1, :718)  */
+  float eta_m;               /* PM distribution index (reference 5, :49)      */
+  float p_m;                 /* per-gene PM probability; < 0 means 1/D (reference 1, :555) */
+  int32_t transfer_interval; /* generations between elite transfers; 0 = off */
+  float transfer_rate;       /* fraction of the island sent (reference 50/512) */
+  float transfer_mix;        /* probability that a candidate gene comes from
+                                the partner (reference 1 - 0.6, SG-EMTF.cu:1551) */
+  uint32_t flags;            /* EMT_FLAG_*                                    */
+  uint64_t seed;             /* Philox key                                    */
+  double recheck_rel;        /* FP64 re-check window, relative to the fitness
+                                scale; 0 = library default                   */
+  int32_t device;            /* CUDA device ordinal                           */
+  int32_t reserved[7];
+} emt_config;
+
+typedef struct emt_task_desc {
+  int32_t function;              /* emt_function                             */
+  int32_t dim;                   /* D, 1..EMT_MAX_DIM                        */
+  int32_t pop;                   /* NP, 4..EMT_MAX_POP                       */
+  float lo, hi;                  /* box; lo >= hi selects the function's box */
+  int32_t rotation;              /* emt_rotation                             */
+  const double* rotation_matrix; /* DENSE: D*D row-major, else ignored      */
+  const float* diag;             /* DIAG: D scale factors, else ignored     */
+  const float* shift;            /* D floats; NULL draws o ~ U(0.8 * box)   */
+} emt_task_desc;
+
+#define EMT_MAX_DIM 128
+#define EMT_MAX_POP 256
+
+typedef struct emt_stats {
+  uint64_t evaluations;       /* fitness evaluations on the device         */
+  uint64_t generations;       /* sum over tasks of generations completed    */
+  uint64_t rechecks;          /* selections re-decided in FP64              */
+  uint64_t recheck_flips;     /* of those, how many FP32 would have got wrong */
+  uint64_t transfers_accepted;/* elite-transfer candidates that replaced a member */
+  double device_ms;           /* device time of the last emt_run            */
+  int32_t n_tasks;
+  int32_t precision_used;     /* emt_precision actually run                 */
+} emt_stats;
+
+/* Fills *cfg with DE/rand/1/bin, F = 0.5, CR = 0.9, SBX eta 15 / p_c 0.9,
+ * PM eta 15 / p_m = 1/D, no transfer, FP32 rotation, seed 1. */
+EMT_API void emt_config_default(emt_config* cfg);
+
+/* Reference function number (SG-EMTF.cu:917-1101) -> emt_function, or -1. */
+EMT_API int32_t emt_function_from_reference(int32_t reference_type);
+
+/* The function's box [lo, hi]; reference_boxes != 0 gives SG-EMTF.cu:197-214. */
+EMT_API int emt_function_box(int32_t function, int32_t reference_boxes, float* lo, float* hi);
+
+/* Replaces the reference's initialization() (SG-EMTF.cu:293-380): validates
+ * the configuration and binds the device.  No task exists yet. */
+EMT_API int emt_create(const emt_config* cfg, emt_handle_t** out);
+
+/* Adds n tasks (para_init + pop_init, SG-EMTF.cu:146-195): copies the
+ * rotation and shift, generates what the descriptors leave to the seed. */
+EMT_API int emt_add_tasks(emt_handle_t* h, int32_t n, const emt_task_desc* tasks);
+
+/* Draws every task's initial population from the seed and evaluates it
+ * (pop_init + evaluate, SG-EMTF.cu:146-159,1428-1479).  emt_run calls it
+ * on first use; calling it again restarts every task from generation 0. */
+EMT_API int emt_reset(emt_handle_t* h, void* stream);
+
+/* Advances every task by `generations` generations: the per-task loop of
+ * iter() (SG-EMTF.cu:1669-1723) over GeneticOpera (:1289-1426), popSort
+ * (:462-486) and knowledgeTransfer (:1514-1591), for all tasks at once.
+ * Asynchronous on `stream`; emt_sync waits and reports device errors. */
+EMT_API int emt_run(emt_handle_t* h, int32_t generations, void* stream);
+
+/* Waits for the handle's work and reports a kernel's error word. */
+EMT_API int emt_sync(emt_handle_t* h);
+
+/* Best member of one task (messageTransfer, SG-EMTF.cu:1601-1615).  The
+ * fitness is re-evaluated in FP64 on the host from the stored vector. */
+EMT_API int emt_get_best(emt_handle_t* h, int32_t task, double* fitness, float* x);
+
+/* FP32 fitness of every task's best member, n_tasks floats. */
+EMT_API int emt_get_best_all(emt_handle_t* h, float* fitness);
+
+/* One task's population (NP * D floats, row-major) and FP32 fitness (NP). */
+EMT_API int emt_get_population(emt_handle_t* h, int32_t task, float* x, float* fitness);
+
+/* Replaces one task's population and evaluates it on the device. */
+EMT_API int emt_set_population(emt_handle_t* h, int32_t task, const float* x);
+
+/* The rotation (D*D FP32, row-major) and shift (D) the device uses. */
+EMT_API int emt_get_task_params(emt_handle_t* h, int32_t task, float* rotation, float* shift);
+
+/* Evaluates n arbitrary points of one task on the device (the reference's
+ * evaluate kernel, SG-EMTF.cu:1428-1479).  x: n*D floats; fitness: n floats;
+ * z: optional n*D floats receiving the rotated argument. */
+EMT_API int emt_evaluate(emt_handle_t* h, int32_t task, int32_t n, const float* x,
+                 float* fitness, float* z);
+
+EMT_API int emt_get_stats(emt_handle_t* h, emt_stats* out);
+
+/* Size in bytes of a checkpoint, then the checkpoint itself: populations,
+ * fitness and per-task generation counters.  Philox counters are derived
+ * from those, so a restored run continues bit for bit. */
+EMT_API int emt_snapshot_size(emt_handle_t* h, size_t* bytes);
+EMT_API int emt_snapshot(emt_handle_t* h, void* buf, size_t bytes);
+EMT_API int emt_restore(emt_handle_t* h, const void* buf, size_t bytes);
+
+EMT_API const char* emt_last_error(const emt_handle_t* h);
+EMT_API const char* emt_status_string(int status);
+EMT_API void emt_destroy(emt_handle_t* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SGEMTF_H */

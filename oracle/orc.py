@@ -1,0 +1,229 @@
+"""ctypes binding of the CPU oracle (test infrastructure only).
+
+Used by tests/, __graft_entry__.smoke() and the CPU-baseline leg of bench.py
+as the checker; the product never imports it.  `build()` compiles
+oracle/emt_oracle.c with the committed Makefile.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libemt_oracle.so")
+
+SPHERE, RASTRIGIN, ACKLEY, GRIEWANK, ROSENBROCK, SCHWEFEL, WEIERSTRASS = range(7)
+FUNCTION_NAMES = ["sphere", "rastrigin", "ackley", "griewank", "rosenbrock", "schwefel",
+                  "weierstrass"]
+DE_RAND1, DE_CURRENT1, GA = 0, 1, 2
+FLAG_REF_GRIEWANK_NO_PRODUCT = 0x1
+FLAG_REF_WEIERSTRASS_CONST = 0x2
+FLAG_REF_ACKLEY_E = 0x4
+FLAG_REF_BOXES = 0x8
+FLAG_NO_RECHECK = 0x10
+
+P_POP_INIT, P_SHIFT, P_QR_NORMAL, P_DE_INDEX, P_DE_CR = 1, 2, 3, 4, 5
+P_GA_PARENT, P_GA_SBX, P_GA_PM, P_TRANSFER_PARTNER, P_TRANSFER_MIX = 6, 7, 8, 9, 10
+
+_F32P = ctypes.POINTER(ctypes.c_float)
+_F64P = ctypes.POINTER(ctypes.c_double)
+_U8P = ctypes.POINTER(ctypes.c_uint8)
+
+
+class Task(ctypes.Structure):
+    _fields_ = [("fid", ctypes.c_int), ("D", ctypes.c_int), ("NP", ctypes.c_int),
+                ("lo", ctypes.c_float), ("hi", ctypes.c_float), ("Q", _F32P),
+                ("o", _F32P), ("flags", ctypes.c_uint32), ("id", ctypes.c_uint32)]
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("algorithm", ctypes.c_int), ("F", ctypes.c_float), ("CR", ctypes.c_float),
+                ("eta_c", ctypes.c_float), ("p_c", ctypes.c_float), ("eta_m", ctypes.c_float),
+                ("p_m", ctypes.c_float), ("transfer_mix", ctypes.c_float),
+                ("seed", ctypes.c_uint64), ("recheck_rel", ctypes.c_double),
+                ("flags", ctypes.c_uint32)]
+
+
+def build(quiet=True):
+    out = subprocess.run(["make", "-C", HERE], capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
+    if not quiet:
+        print(out.stdout)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        L.orc_u01.restype = ctypes.c_float
+        L.orc_u01.argtypes = [ctypes.c_uint32]
+        L.orc_eval64.restype = ctypes.c_double
+        L.orc_eval64.argtypes = [ctypes.POINTER(Task), _F32P, _F64P, _F64P]
+        L.orc_eval32.restype = ctypes.c_float
+        L.orc_eval32.argtypes = [ctypes.POINTER(Task), _F32P, _F32P]
+        L.orc_weierstrass_rotation_bound.restype = ctypes.c_double
+        L.orc_weierstrass_rotation_bound.argtypes = [ctypes.POINTER(Task), _F32P]
+        L.orc_weierstrass_reference_offset.restype = ctypes.c_double
+        L.orc_powf.restype = ctypes.c_float
+        L.orc_powf.argtypes = [ctypes.c_float, ctypes.c_float]
+        L.orc_gen_shift.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int,
+                                    ctypes.c_float, ctypes.c_float, _F32P]
+        L.orc_gen_population.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int,
+                                         ctypes.c_int, ctypes.c_float, ctypes.c_float, _F32P]
+        L.orc_gen_rotation.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int, _F64P]
+        L.orc_draw.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32,
+                               ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                               ctypes.POINTER(ctypes.c_uint32)]
+        L.orc_generation.restype = ctypes.c_int
+        L.orc_generation.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(Task), _F32P, _F32P,
+                                     _F64P, ctypes.c_uint32, ctypes.c_int, _U8P]
+        L.orc_trial.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(Task), _F32P,
+                                ctypes.c_uint32, ctypes.c_int, _F32P]
+        L.orc_rank.argtypes = [_F32P, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+        L.orc_transfer_partner.restype = ctypes.c_int
+        L.orc_transfer_partner.argtypes = [ctypes.POINTER(Params), ctypes.c_uint32,
+                                           ctypes.c_uint32, ctypes.c_uint32]
+        L.orc_transfer_in.restype = ctypes.c_int
+        L.orc_transfer_in.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(Task),
+                                      ctypes.POINTER(Task), _F32P, ctypes.c_int, _F32P, _F32P,
+                                      _F64P, ctypes.c_uint32, ctypes.c_int]
+        L.orc_run_threads.restype = ctypes.c_double
+        L.orc_run_threads.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(Task), ctypes.c_int,
+                                      ctypes.POINTER(_F32P), ctypes.POINTER(_F32P),
+                                      ctypes.POINTER(_F64P), ctypes.c_uint32, ctypes.c_int,
+                                      ctypes.c_int, ctypes.c_int]
+        L.orc_box.argtypes = [ctypes.c_int, ctypes.c_int, _F32P, _F32P]
+        _lib = L
+    return _lib
+
+
+def _p32(a):
+    return a.ctypes.data_as(_F32P)
+
+
+def _p64(a):
+    return a.ctypes.data_as(_F64P)
+
+
+def box(fid, reference_boxes=False):
+    lo, hi = ctypes.c_float(), ctypes.c_float()
+    lib().orc_box(fid, int(reference_boxes), ctypes.byref(lo), ctypes.byref(hi))
+    return lo.value, hi.value
+
+
+def draw(seed, task, gen, member, purpose, block):
+    out = (ctypes.c_uint32 * 4)()
+    lib().orc_draw(seed, task, gen, member, purpose, block, out)
+    return list(out)
+
+
+def philox(ctr, key):
+    out = (ctypes.c_uint32 * 4)()
+    lib().orc_philox4x32_10((ctypes.c_uint32 * 4)(*ctr), (ctypes.c_uint32 * 2)(*key), out)
+    return list(out)
+
+
+def gen_shift(seed, task, D, lo, hi):
+    o = np.zeros(D, np.float32)
+    lib().orc_gen_shift(seed, task, D, lo, hi, _p32(o))
+    return o
+
+
+def gen_population(seed, task, NP, D, lo, hi):
+    X = np.zeros((NP, D), np.float32)
+    lib().orc_gen_population(seed, task, NP, D, lo, hi, _p32(X))
+    return X
+
+
+def gen_rotation(seed, task, D):
+    Q = np.zeros((D, D), np.float64)
+    lib().orc_gen_rotation(seed, task, D, _p64(Q))
+    return Q
+
+
+class OTask:
+    """An oracle task: keeps the numpy buffers alive behind the C struct."""
+
+    def __init__(self, fid, D, NP, lo, hi, Q=None, o=None, flags=0, tid=0):
+        self.Q = None if Q is None else np.ascontiguousarray(Q, np.float32)
+        self.o = np.zeros(D, np.float32) if o is None else np.ascontiguousarray(o, np.float32)
+        self.c = Task(fid, D, NP, lo, hi, _p32(self.Q) if self.Q is not None else None,
+                      _p32(self.o), flags, tid)
+
+    @property
+    def D(self):
+        return self.c.D
+
+    @property
+    def NP(self):
+        return self.c.NP
+
+    def eval64(self, x):
+        x = np.ascontiguousarray(x, np.float32)
+        s = ctypes.c_double()
+        z = np.zeros(max(self.D, 1), np.float64)
+        f = lib().orc_eval64(ctypes.byref(self.c), _p32(x), ctypes.byref(s), _p64(z))
+        return f, s.value, z
+
+    def eval32(self, x):
+        x = np.ascontiguousarray(x, np.float32)
+        s = ctypes.c_float()
+        f = lib().orc_eval32(ctypes.byref(self.c), _p32(x), ctypes.byref(s))
+        return f, s.value
+
+    def weier_bound(self, x):
+        x = np.ascontiguousarray(x, np.float32)
+        return lib().orc_weierstrass_rotation_bound(ctypes.byref(self.c), _p32(x))
+
+
+def params(algorithm=DE_RAND1, F=0.5, CR=0.9, eta_c=15.0, p_c=0.9, eta_m=15.0, p_m=-1.0,
+           transfer_mix=0.4, seed=1, recheck_rel=0.0, flags=0):
+    return Params(algorithm, F, CR, eta_c, p_c, eta_m, p_m, transfer_mix, seed, recheck_rel,
+                  flags)
+
+
+def generation(p, t, X, fit32, fit64, gen, mode):
+    acc = np.zeros(t.NP, np.uint8)
+    n = lib().orc_generation(ctypes.byref(p), ctypes.byref(t.c), _p32(X), _p32(fit32),
+                             _p64(fit64), gen, mode, acc.ctypes.data_as(_U8P))
+    return acc, n
+
+
+def trial(p, t, X, gen, i):
+    u = np.zeros(t.D, np.float32)
+    lib().orc_trial(ctypes.byref(p), ctypes.byref(t.c), _p32(X), gen, i, _p32(u))
+    return u
+
+
+def rank(fit32):
+    fit32 = np.ascontiguousarray(fit32, np.float32)
+    r = np.zeros(len(fit32), np.int32)
+    lib().orc_rank(_p32(fit32), len(fit32), r.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    return r
+
+
+def transfer_partner(p, t, n_tasks, gen):
+    return lib().orc_transfer_partner(ctypes.byref(p), t, n_tasks, gen)
+
+
+def transfer_in(p, t, pt, elites, X, fit32, fit64, gen, mode):
+    elites = np.ascontiguousarray(elites, np.float32)
+    return lib().orc_transfer_in(ctypes.byref(p), ctypes.byref(t.c), ctypes.byref(pt.c),
+                                 _p32(elites), elites.shape[0], _p32(X), _p32(fit32),
+                                 _p64(fit64), gen, mode)
+
+
+def run_threads(p, tasks, X, fit32, fit64, gen0, gens, mode, threads):
+    n = len(tasks)
+    arr = (Task * n)(*[t.c for t in tasks])
+    xp = (_F32P * n)(*[_p32(a) for a in X])
+    fp = (_F32P * n)(*[_p32(a) for a in fit32])
+    dp = (_F64P * n)(*[_p64(a) for a in fit64])
+    return lib().orc_run_threads(ctypes.byref(p), arr, n, xp, fp, dp, gen0, gens, mode, threads)

@@ -1,0 +1,809 @@
+// emt_api.cu -- the C ABI (include/sgemtf.h): handle, task packing and the
+// host orchestration of the device kernels.
+//
+// Replaces the reference's host layer: initialization() (proposed model/
+// SG-EMTF.cu:293-380), one std::thread per task running iter() (:1646-1745)
+// over 8 shared streams, and the pthread/cudaEvent hand-shake for transfers
+// (:1678-1722).  Here every task advances in the same launch; transfers are
+// epoch boundaries between launches, so no host thread waits on another.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/sgemtf.h"
+#include "emt_internal.h"
+
+namespace {
+
+using emt::TaskDev;
+
+struct HostTask {
+  int fid = 0, D = 0, NP = 0;
+  float lo = 0.f, hi = 0.f;
+  std::vector<float> Q;  // D*D row-major, the operator the device applies
+  std::vector<float> o;  // D
+  float woff = 0.f, qnorm = 1.f;
+  double woff64 = 0.0;
+};
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaError_t ensure(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    if (count == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc((void**)&p, count * sizeof(T));
+    if (e == cudaSuccess) n = count;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+}  // namespace
+
+struct emt_handle {
+  emt_config cfg{};
+  int device = 0;
+  std::vector<HostTask> tasks;
+  std::vector<TaskDev> table;
+  std::vector<int32_t> order;
+  bool uploaded = false, initialized = false;
+  uint32_t gdone = 0;  // generations completed by every task
+  int elite_parity = 0;
+  size_t smem_bytes = 0;
+  std::string err;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  bool timing_pending = false;
+  double device_ms = 0.0;
+  unsigned long long stats_base[4] = {0, 0, 0, 0};
+
+  DevBuf<TaskDev> d_tasks;
+  DevBuf<int32_t> d_order;
+  DevBuf<float> d_pop, d_fit32, d_tol32, d_qt, d_shift, d_elites[2], d_best_f32;
+  DevBuf<double> d_fit64, d_best_f64;
+  DevBuf<uint32_t> d_gen;
+  DevBuf<unsigned long long> d_stats;
+  DevBuf<int32_t> d_err, d_best_idx;
+
+  int fail(int code, const std::string& msg) {
+    err = msg;
+    return code;
+  }
+  int cuda_fail(cudaError_t e, const char* what) {
+    err = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? EMT_ERR_OUT_OF_MEMORY : EMT_ERR_CUDA;
+  }
+};
+
+namespace {
+
+const float kBoxStd[7][2] = {{-100.f, 100.f}, {-5.12f, 5.12f},   {-32.768f, 32.768f},
+                             {-600.f, 600.f}, {-2.048f, 2.048f}, {-500.f, 500.f},
+                             {-0.5f, 0.5f}};
+// SG-EMTF.cu:197-214 by reference type; kRefToFid maps the type to our id.
+const float kBoxRef[7][2] = {{-100.f, 100.f}, {-50.f, 50.f},   {-50.f, 50.f}, {-50.f, 50.f},
+                             {-100.f, 100.f}, {-0.5f, 0.5f}, {-500.f, 500.f}};
+const int kRefToFid[7] = {EMT_SPHERE,   EMT_ROSENBROCK,  EMT_ACKLEY,  EMT_RASTRIGIN,
+                          EMT_GRIEWANK, EMT_WEIERSTRASS, EMT_SCHWEFEL};
+
+// Relative cost of one gene's function term, for the longest-first order.
+const float kFnCost[7] = {1.f, 16.f, 18.f, 30.f, 6.f, 28.f, 200.f};
+
+// The Weierstrass offset as the reference's host code computes it
+// (SG-EMTF.cu:354-361): PI = 3.1415926 (double), b_ *= 3 in float, cosf.
+float weierstrass_reference_offset() {
+  float a = 1.f, b = 1.f, res = 0.f;
+  for (int i = 0; i <= 20; ++i) {
+    double arg = 2 * 3.1415926 * (double)b * 0.5;
+    res += a * cosf((float)arg);
+    a *= 0.5f;
+    b *= 3.f;
+  }
+  return res;
+}
+
+// Orthogonal factor of the FP64 Householder QR of a seeded N(0,1) D x D
+// matrix (Box-Muller on Philox words, purpose P_QR_NORMAL), column signs
+// fixed so that R has a positive diagonal.
+void seeded_rotation(uint64_t seed, uint32_t task, int D, std::vector<double>& Q) {
+  std::vector<double> A((size_t)D * D), v(D);
+  for (int r = 0; r < D; ++r)
+    for (int c = 0; c < D; c += 4) {
+      emt::U4 w = emt::draw(seed, task, 0, (uint32_t)r, emt::P_QR_NORMAL, (uint32_t)(c >> 2));
+      uint32_t ww[4] = {w.x, w.y, w.z, w.w};
+      for (int h = 0; h < 2; ++h) {
+        double u1 = ((double)ww[2 * h] + 1.0) * 0x1p-32;
+        double u2 = (double)ww[2 * h + 1] * 0x1p-32;
+        double rad = std::sqrt(-2.0 * std::log(u1));
+        double th = 6.283185307179586 * u2;
+        if (c + 2 * h < D) A[(size_t)r * D + c + 2 * h] = rad * std::cos(th);
+        if (c + 2 * h + 1 < D) A[(size_t)r * D + c + 2 * h + 1] = rad * std::sin(th);
+      }
+    }
+  Q.assign((size_t)D * D, 0.0);
+  for (int i = 0; i < D; ++i) Q[(size_t)i * D + i] = 1.0;
+  for (int k = 0; k < D - 1; ++k) {
+    double nrm = 0.0;
+    for (int i = k; i < D; ++i) nrm += A[(size_t)i * D + k] * A[(size_t)i * D + k];
+    nrm = std::sqrt(nrm);
+    if (nrm == 0.0) continue;
+    double alpha = A[(size_t)k * D + k] > 0 ? -nrm : nrm;
+    std::fill(v.begin(), v.end(), 0.0);
+    for (int i = k; i < D; ++i) v[i] = A[(size_t)i * D + k];
+    v[k] -= alpha;
+    double vn = 0.0;
+    for (int i = k; i < D; ++i) vn += v[i] * v[i];
+    if (vn == 0.0) continue;
+    for (int c = k; c < D; ++c) {
+      double s = 0.0;
+      for (int i = k; i < D; ++i) s += v[i] * A[(size_t)i * D + c];
+      s = 2.0 * s / vn;
+      for (int i = k; i < D; ++i) A[(size_t)i * D + c] -= s * v[i];
+    }
+    for (int r = 0; r < D; ++r) {
+      double s = 0.0;
+      for (int i = k; i < D; ++i) s += Q[(size_t)r * D + i] * v[i];
+      s = 2.0 * s / vn;
+      for (int i = k; i < D; ++i) Q[(size_t)r * D + i] -= s * v[i];
+    }
+  }
+  for (int c = 0; c < D; ++c)
+    if (A[(size_t)c * D + c] < 0)
+      for (int r = 0; r < D; ++r) Q[(size_t)r * D + c] = -Q[(size_t)r * D + c];
+}
+
+int max_smem_optin(int device) {
+  int v = 0;
+  if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess)
+    return 0;
+  return v;
+}
+
+int upload(emt_handle* h) {
+  if (h->uploaded) return EMT_OK;
+  const int n = (int)h->tasks.size();
+  if (n == 0) return h->fail(EMT_ERR_STATE, "no tasks");
+  h->table.resize(n);
+  int64_t pop = 0, q = 0, o = 0, el = 0;
+  int32_t fit = 0;
+  size_t smem = 0;
+  for (int t = 0; t < n; ++t) {
+    const HostTask& ht = h->tasks[t];
+    TaskDev& d = h->table[t];
+    d.fid = ht.fid;
+    d.D = ht.D;
+    d.NP = ht.NP;
+    d.DP = emt::round4(ht.D);
+    d.lo = ht.lo;
+    d.hi = ht.hi;
+    d.woff = ht.woff;
+    d.woff64 = ht.woff64;
+    d.qnorm = ht.qnorm;
+    d.pop_off = pop;
+    pop += (int64_t)ht.NP * d.DP;
+    d.q_off = q;
+    q += (int64_t)ht.D * d.DP;
+    d.o_off = o;
+    o += d.DP;
+    d.elite_off = el;
+    el += (int64_t)ht.NP * d.DP;
+    d.fit_off = fit;
+    fit += ht.NP;
+    d.flags = h->cfg.flags;
+    d.qt_in_smem = emt::smem_layout(ht.D, ht.NP, true).total <= emt::kSmemLimit ? 1 : 0;
+    d.pad_ = 0;
+    smem = std::max(smem, emt::smem_layout(ht.D, ht.NP, d.qt_in_smem != 0).total);
+  }
+  h->smem_bytes = smem;
+  // longest-first order: the hardware hands CTAs to free SM slots in block
+  // order, so costly islands start first and the tail is made of cheap ones.
+  h->order.resize(n);
+  std::iota(h->order.begin(), h->order.end(), 0);
+  std::vector<double> cost(n);
+  for (int t = 0; t < n; ++t) {
+    const HostTask& ht = h->tasks[t];
+    cost[t] = (double)ht.NP * ht.D * (ht.D + 40.0 + kFnCost[ht.fid]);
+  }
+  std::stable_sort(h->order.begin(), h->order.end(),
+                   [&](int a, int b) { return cost[a] > cost[b]; });
+
+  std::vector<float> hq((size_t)q, 0.f), ho((size_t)o, 0.f);
+  for (int t = 0; t < n; ++t) {
+    const HostTask& ht = h->tasks[t];
+    const TaskDev& d = h->table[t];
+    for (int k = 0; k < ht.D; ++k)
+      for (int c = 0; c < ht.D; ++c) hq[(size_t)d.q_off + (size_t)k * d.DP + c] = ht.Q[(size_t)c * ht.D + k];
+    for (int j = 0; j < ht.D; ++j) ho[(size_t)d.o_off + j] = ht.o[j];
+  }
+  cudaError_t e;
+  if ((e = cudaSetDevice(h->device)) != cudaSuccess) return h->cuda_fail(e, "cudaSetDevice");
+  if ((e = h->d_tasks.ensure(n)) != cudaSuccess ||
+      (e = h->d_order.ensure(n)) != cudaSuccess ||
+      (e = h->d_pop.ensure((size_t)pop)) != cudaSuccess ||
+      (e = h->d_fit32.ensure((size_t)fit)) != cudaSuccess ||
+      (e = h->d_tol32.ensure((size_t)fit)) != cudaSuccess ||
+      (e = h->d_fit64.ensure((size_t)fit)) != cudaSuccess ||
+      (e = h->d_qt.ensure((size_t)q)) != cudaSuccess ||
+      (e = h->d_shift.ensure((size_t)o)) != cudaSuccess ||
+      (e = h->d_gen.ensure(n)) != cudaSuccess ||
+      (e = h->d_stats.ensure(4)) != cudaSuccess || (e = h->d_err.ensure(1)) != cudaSuccess ||
+      (e = h->d_best_idx.ensure(n)) != cudaSuccess ||
+      (e = h->d_best_f32.ensure(n)) != cudaSuccess ||
+      (e = h->d_best_f64.ensure(n)) != cudaSuccess)
+    return h->cuda_fail(e, "cudaMalloc");
+  if (h->cfg.transfer_interval > 0 && n > 1)
+    for (int b = 0; b < 2; ++b)
+      if ((e = h->d_elites[b].ensure((size_t)el)) != cudaSuccess) return h->cuda_fail(e, "cudaMalloc");
+  if ((e = cudaMemcpy(h->d_tasks.p, h->table.data(), sizeof(TaskDev) * n, cudaMemcpyHostToDevice)) ||
+      (e = cudaMemcpy(h->d_order.p, h->order.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice)) ||
+      (e = cudaMemcpy(h->d_qt.p, hq.data(), sizeof(float) * hq.size(), cudaMemcpyHostToDevice)) ||
+      (e = cudaMemcpy(h->d_shift.p, ho.data(), sizeof(float) * ho.size(), cudaMemcpyHostToDevice)) ||
+      (e = cudaMemset(h->d_gen.p, 0, sizeof(uint32_t) * n)) ||
+      (e = cudaMemset(h->d_pop.p, 0, sizeof(float) * (size_t)pop)) ||
+      (e = cudaMemset(h->d_stats.p, 0, sizeof(unsigned long long) * 4)) ||
+      (e = cudaMemset(h->d_err.p, 0, sizeof(int32_t))))
+    return h->cuda_fail(e, "upload");
+  h->uploaded = true;
+  h->initialized = false;
+  return EMT_OK;
+}
+
+emt::EpochArgs base_args(emt_handle* h, int mode) {
+  emt::EpochArgs a{};
+  a.tasks = h->d_tasks.p;
+  a.order = h->d_order.p;
+  a.single_task = -1;
+  a.n_tasks = (int32_t)h->tasks.size();
+  a.mode = mode;
+  a.pop = h->d_pop.p;
+  a.fit32 = h->d_fit32.p;
+  a.tol32 = h->d_tol32.p;
+  a.fit64 = h->d_fit64.p;
+  a.qt = h->d_qt.p;
+  a.shift = h->d_shift.p;
+  a.gen = h->d_gen.p;
+  a.gens = 0;
+  a.algorithm = h->cfg.algorithm;
+  a.F = h->cfg.F;
+  a.CR = h->cfg.CR;
+  a.eta_c = h->cfg.eta_c;
+  a.p_c = h->cfg.p_c;
+  a.eta_m = h->cfg.eta_m;
+  a.p_m = h->cfg.p_m;
+  a.seed = h->cfg.seed;
+  a.recheck_rel = (float)(h->cfg.recheck_rel > 0 ? h->cfg.recheck_rel : 1e-5);
+  a.flags = h->cfg.flags;
+  a.transfer_import = 0;
+  a.transfer_export = 0;
+  a.transfer_rate = h->cfg.transfer_rate;
+  a.transfer_mix = h->cfg.transfer_mix;
+  a.stats = h->d_stats.p;
+  a.err = h->d_err.p;
+  a.smem_bytes = h->smem_bytes;
+  return a;
+}
+
+int check_task(const emt_handle* h, int32_t task) {
+  return (task >= 0 && task < (int32_t)h->tasks.size()) ? EMT_OK : EMT_ERR_INVALID_ARG;
+}
+
+}  // namespace
+
+extern "C" {
+
+void emt_config_default(emt_config* cfg) {
+  if (!cfg) return;
+  std::memset(cfg, 0, sizeof(*cfg));
+  cfg->algorithm = EMT_DE_RAND1_BIN;
+  cfg->precision = EMT_ROT_FP32;
+  cfg->F = 0.5f;
+  cfg->CR = 0.9f;
+  cfg->eta_c = 15.f;
+  cfg->p_c = 0.9f;
+  cfg->eta_m = 15.f;
+  cfg->p_m = -1.f;
+  cfg->transfer_interval = 0;
+  cfg->transfer_rate = 0.1f;
+  cfg->transfer_mix = 0.4f;
+  cfg->flags = 0;
+  cfg->seed = 1;
+  cfg->recheck_rel = 0.0;
+  cfg->device = 0;
+}
+
+int32_t emt_function_from_reference(int32_t t) { return (t >= 0 && t < 7) ? kRefToFid[t] : -1; }
+
+int emt_function_box(int32_t fid, int32_t reference_boxes, float* lo, float* hi) {
+  if (fid < 0 || fid >= EMT_NUM_FUNCTIONS || !lo || !hi) return EMT_ERR_INVALID_ARG;
+  if (reference_boxes) {
+    for (int t = 0; t < 7; ++t)
+      if (kRefToFid[t] == fid) {
+        *lo = kBoxRef[t][0];
+        *hi = kBoxRef[t][1];
+        return EMT_OK;
+      }
+  }
+  *lo = kBoxStd[fid][0];
+  *hi = kBoxStd[fid][1];
+  return EMT_OK;
+}
+
+const char* emt_status_string(int s) {
+  switch (s) {
+    case EMT_OK: return "ok";
+    case EMT_ERR_INVALID_ARG: return "invalid argument";
+    case EMT_ERR_OUT_OF_MEMORY: return "out of memory";
+    case EMT_ERR_CUDA: return "CUDA error";
+    case EMT_ERR_DEVICE_TIMEOUT: return "device-side wait timed out";
+    case EMT_ERR_STATE: return "call out of order";
+    case EMT_ERR_UNSUPPORTED: return "unsupported";
+    case EMT_ERR_DEVICE_CHECK: return "device-side check failed";
+    default: return "unknown status";
+  }
+}
+
+int emt_create(const emt_config* cfg, emt_handle_t** out) {
+  if (!cfg || !out) return EMT_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (cfg->algorithm < EMT_DE_RAND1_BIN || cfg->algorithm > EMT_GA_SBX_PM) return EMT_ERR_INVALID_ARG;
+  if (cfg->precision < EMT_ROT_FP32 || cfg->precision > EMT_ROT_AUTO) return EMT_ERR_INVALID_ARG;
+  if (!(cfg->CR >= 0.f && cfg->CR <= 1.f) || !(cfg->p_c >= 0.f && cfg->p_c <= 1.f) ||
+      !(cfg->eta_c >= 0.f) || !(cfg->eta_m >= 0.f) || !(cfg->p_m <= 1.f) ||
+      !std::isfinite(cfg->F) || cfg->transfer_interval < 0 ||
+      !(cfg->transfer_rate > 0.f && cfg->transfer_rate <= 1.f) ||
+      !(cfg->transfer_mix >= 0.f && cfg->transfer_mix <= 1.f) || !(cfg->recheck_rel >= 0.0))
+    return EMT_ERR_INVALID_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return EMT_ERR_CUDA;
+  if (cfg->device < 0 || cfg->device >= ndev) return EMT_ERR_INVALID_ARG;
+  if (cfg->precision == EMT_ROT_TF32X3) return EMT_ERR_UNSUPPORTED;
+  emt_handle* h = new (std::nothrow) emt_handle();
+  if (!h) return EMT_ERR_OUT_OF_MEMORY;
+  h->cfg = *cfg;
+  if (h->cfg.precision == EMT_ROT_AUTO) h->cfg.precision = EMT_ROT_FP32;
+  h->device = cfg->device;
+  if (cudaSetDevice(h->device) != cudaSuccess || cudaEventCreate(&h->ev0) != cudaSuccess ||
+      cudaEventCreate(&h->ev1) != cudaSuccess) {
+    delete h;
+    return EMT_ERR_CUDA;
+  }
+  *out = h;
+  return EMT_OK;
+}
+
+int emt_add_tasks(emt_handle_t* h, int32_t n, const emt_task_desc* td) {
+  if (!h) return EMT_ERR_INVALID_ARG;
+  if (n < 0 || (n > 0 && !td)) return h->fail(EMT_ERR_INVALID_ARG, "bad task array");
+  const int smem_cap = max_smem_optin(h->device);
+  std::vector<HostTask> add;
+  add.reserve(n);
+  for (int i = 0; i < n; ++i) {
+    const emt_task_desc& d = td[i];
+    const uint32_t id = (uint32_t)(h->tasks.size() + add.size());
+    if (d.function < 0 || d.function >= EMT_NUM_FUNCTIONS)
+      return h->fail(EMT_ERR_INVALID_ARG, "task " + std::to_string(i) + ": bad function id");
+    if (d.dim < 1 || d.dim > EMT_MAX_DIM)
+      return h->fail(EMT_ERR_INVALID_ARG, "task " + std::to_string(i) + ": dim out of range");
+    if (d.pop < 4 || d.pop > EMT_MAX_POP)
+      return h->fail(EMT_ERR_INVALID_ARG, "task " + std::to_string(i) + ": pop out of range");
+    if ((size_t)smem_cap < emt::smem_layout(d.dim, d.pop, false).total)
+      return h->fail(EMT_ERR_UNSUPPORTED, "task " + std::to_string(i) +
+                                              ": island does not fit in shared memory");
+    HostTask ht;
+    ht.fid = d.function;
+    ht.D = d.dim;
+    ht.NP = d.pop;
+    if (d.lo < d.hi && std::isfinite(d.lo) && std::isfinite(d.hi)) {
+      ht.lo = d.lo;
+      ht.hi = d.hi;
+    } else {
+      emt_function_box(d.function, (h->cfg.flags & EMT_FLAG_REF_BOXES) ? 1 : 0, &ht.lo, &ht.hi);
+    }
+    const int D = d.dim;
+    ht.Q.assign((size_t)D * D, 0.f);
+    switch (d.rotation) {
+      case EMT_ROTATION_IDENTITY:
+        for (int k = 0; k < D; ++k) ht.Q[(size_t)k * D + k] = 1.f;
+        break;
+      case EMT_ROTATION_SEEDED_QR: {
+        std::vector<double> Q;
+        seeded_rotation(h->cfg.seed, id, D, Q);
+        for (size_t k = 0; k < Q.size(); ++k) ht.Q[k] = (float)Q[k];
+        break;
+      }
+      case EMT_ROTATION_DENSE:
+        if (!d.rotation_matrix) return h->fail(EMT_ERR_INVALID_ARG, "dense rotation without matrix");
+        for (size_t k = 0; k < (size_t)D * D; ++k) {
+          if (!std::isfinite(d.rotation_matrix[k])) return h->fail(EMT_ERR_INVALID_ARG, "non-finite rotation");
+          ht.Q[k] = (float)d.rotation_matrix[k];
+        }
+        break;
+      case EMT_ROTATION_DIAG:
+        if (!d.diag) return h->fail(EMT_ERR_INVALID_ARG, "diagonal rotation without factors");
+        for (int k = 0; k < D; ++k) ht.Q[(size_t)k * D + k] = d.diag[k];
+        break;
+      default:
+        return h->fail(EMT_ERR_INVALID_ARG, "bad rotation kind");
+    }
+    ht.o.assign(D, 0.f);
+    if (d.shift) {
+      for (int k = 0; k < D; ++k) ht.o[k] = d.shift[k];
+    } else {
+      const float a = emt::fmul(0.8f, ht.lo), r = emt::fmul(0.8f, emt::fsub(ht.hi, ht.lo));
+      for (int k = 0; k < D; k += 4) {
+        emt::U4 w = emt::draw(h->cfg.seed, id, 0, 0, emt::P_SHIFT, (uint32_t)(k >> 2));
+        for (int qd = 0; qd < 4 && k + qd < D; ++qd) ht.o[k + qd] = emt::ffma(emt::u01(emt::word(w, qd)), r, a);
+      }
+    }
+    double qn = 0.0;
+    for (int r = 0; r < D; ++r) {
+      double s = 0.0;
+      for (int c = 0; c < D; ++c) s += (double)ht.Q[(size_t)r * D + c] * ht.Q[(size_t)r * D + c];
+      qn = std::max(qn, std::sqrt(s));
+    }
+    ht.qnorm = (float)qn;
+    if (h->cfg.flags & EMT_FLAG_REF_WEIERSTRASS_CONST)
+      ht.woff64 = -(double)D * (double)weierstrass_reference_offset();
+    else
+      ht.woff64 = (double)D * (2.0 - 0x1p-20);
+    ht.woff = (float)ht.woff64;
+    add.push_back(std::move(ht));
+  }
+  for (auto& t : add) h->tasks.push_back(std::move(t));
+  h->uploaded = false;
+  h->initialized = false;
+  return EMT_OK;
+}
+
+int emt_reset(emt_handle_t* h, void* stream) {
+  if (!h) return EMT_ERR_INVALID_ARG;
+  int rc = upload(h);
+  if (rc) return rc;
+  h->stream = (cudaStream_t)stream;
+  emt::EpochArgs a = base_args(h, emt::MODE_INIT);
+  int e = emt_launch_epoch(a, (int)h->tasks.size(), stream);
+  if (e) return h->cuda_fail((cudaError_t)e, "init launch");
+  h->initialized = true;
+  h->gdone = 0;
+  h->elite_parity = 0;
+  return EMT_OK;
+}
+
+int emt_run(emt_handle_t* h, int32_t generations, void* stream) {
+  if (!h) return EMT_ERR_INVALID_ARG;
+  if (generations < 0) return h->fail(EMT_ERR_INVALID_ARG, "negative generation count");
+  if (!h->initialized) {
+    int rc = emt_reset(h, stream);
+    if (rc) return rc;
+  }
+  h->stream = (cudaStream_t)stream;
+  const int n = (int)h->tasks.size();
+  const int interval = (h->cfg.transfer_interval > 0 && n > 1) ? h->cfg.transfer_interval : 0;
+  cudaEventRecord(h->ev0, h->stream);
+  int left = generations;
+  while (left > 0) {
+    int g = left;
+    bool do_import = false, do_export = false;
+    if (interval) {
+      do_import = h->gdone > 0 && (h->gdone % (uint32_t)interval) == 0;
+      int to_boundary = interval - (int)(h->gdone % (uint32_t)interval);
+      g = std::min(left, to_boundary);
+      do_export = ((h->gdone + (uint32_t)g) % (uint32_t)interval) == 0;
+    }
+    emt::EpochArgs a = base_args(h, emt::MODE_EPOCH);
+    a.gens = g;
+    if (interval) {
+      a.transfer_import = do_import ? 1 : 0;
+      a.transfer_export = do_export ? 1 : 0;
+      a.elites_in = h->d_elites[h->elite_parity ^ 1].p;
+      a.elites_out = h->d_elites[h->elite_parity].p;
+    }
+    int e = emt_launch_epoch(a, n, stream);
+    if (e) return h->cuda_fail((cudaError_t)e, "epoch launch");
+    if (interval && do_export) h->elite_parity ^= 1;
+    h->gdone += (uint32_t)g;
+    left -= g;
+  }
+  cudaEventRecord(h->ev1, h->stream);
+  h->timing_pending = true;
+  return EMT_OK;
+}
+
+int emt_sync(emt_handle_t* h) {
+  if (!h) return EMT_ERR_INVALID_ARG;
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return h->cuda_fail(e, "stream synchronize");
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return h->cuda_fail(e, "kernel");
+  if (h->timing_pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, h->ev0, h->ev1) == cudaSuccess) h->device_ms = ms;
+    h->timing_pending = false;
+  }
+  if (h->d_err.p) {
+    int32_t code = 0;
+    e = cudaMemcpy(&code, h->d_err.p, sizeof(code), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return h->cuda_fail(e, "error word");
+    if (code) {
+      cudaMemset(h->d_err.p, 0, sizeof(int32_t));
+      return h->fail(EMT_ERR_DEVICE_CHECK, "device check " + std::to_string(code) +
+                                               (code == emt::CHECK_BAD_DESCRIPTOR ? " (bad task descriptor)"
+                                                : code == emt::CHECK_SMEM_TOO_SMALL ? " (shared memory too small)"
+                                                : code == emt::CHECK_BAD_PARTNER ? " (bad transfer partner)"
+                                                                                 : ""));
+    }
+  }
+  return EMT_OK;
+}
+
+static int ensure_ready(emt_handle* h) {
+  if (h->tasks.empty()) return h->fail(EMT_ERR_STATE, "no tasks");
+  if (!h->initialized) {
+    int rc = emt_reset(h, h->stream);
+    if (rc) return rc;
+  }
+  return emt_sync(h);
+}
+
+int emt_get_best(emt_handle_t* h, int32_t task, double* fitness, float* x) {
+  if (!h) return EMT_ERR_INVALID_ARG;
+  if (check_task(h, task)) return h->fail(EMT_ERR_INVALID_ARG, "task index out of range");
+  int rc = ensure_ready(h);
+  if (rc) return rc;
+  emt::BestArgs b{h->d_tasks.p, (int32_t)h->tasks.size(), h->d_pop.p, h->d_fit32.p, h->d_fit64.p,
+                  h->d_qt.p, h->d_shift.p, h->d_best_idx.p, h->d_best_f32.p, h->d_best_f64.p};
+  int e = emt_launch_best(b, h->stream);
+  if (e) return h->cuda_fail((cudaError_t)e, "best launch");
+  if ((rc = emt_sync(h))) return rc;
+  int32_t idx = 0;
+  double f = 0.0;
+  cudaMemcpy(&idx, h->d_best_idx.p + task, sizeof(idx), cudaMemcpyDeviceToHost);
+  cudaMemcpy(&f, h->d_best_f64.p + task, sizeof(f), cudaMemcpyDeviceToHost);
+  if (fitness) *fitness = f;
+  if (x) {
+    const TaskDev& d = h->table[task];
+    cudaError_t ce = cudaMemcpy(x, h->d_pop.p + d.pop_off + (size_t)idx * d.DP, sizeof(float) * d.D,
+                                cudaMemcpyDeviceToHost);
+    if (ce != cudaSuccess) return h->cuda_fail(ce, "copy best");
+  }
+  return EMT_OK;
+}
+
+int emt_get_best_all(emt_handle_t* h, float* fitness) {
+  if (!h || !fitness) return EMT_ERR_INVALID_ARG;
+  int rc = ensure_ready(h);
+  if (rc) return rc;
+  emt::BestArgs b{h->d_tasks.p, (int32_t)h->tasks.size(), h->d_pop.p, h->d_fit32.p, h->d_fit64.p,
+                  h->d_qt.p, h->d_shift.p, h->d_best_idx.p, h->d_best_f32.p, h->d_best_f64.p};
+  int e = emt_launch_best(b, h->stream);
+  if (e) return h->cuda_fail((cudaError_t)e, "best launch");
+  cudaError_t ce = cudaMemcpyAsync(fitness, h->d_best_f32.p, sizeof(float) * h->tasks.size(),
+                                   cudaMemcpyDeviceToHost, h->stream);
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "copy best");
+  return emt_sync(h);
+}
+
+int emt_get_population(emt_handle_t* h, int32_t task, float* x, float* fitness) {
+  if (!h) return EMT_ERR_INVALID_ARG;
+  if (check_task(h, task)) return h->fail(EMT_ERR_INVALID_ARG, "task index out of range");
+  int rc = ensure_ready(h);
+  if (rc) return rc;
+  const TaskDev& d = h->table[task];
+  cudaError_t e = cudaSuccess;
+  if (x)
+    e = cudaMemcpy2D(x, sizeof(float) * d.D, h->d_pop.p + d.pop_off, sizeof(float) * d.DP,
+                     sizeof(float) * d.D, d.NP, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && fitness)
+    e = cudaMemcpy(fitness, h->d_fit32.p + d.fit_off, sizeof(float) * d.NP, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return h->cuda_fail(e, "copy population");
+  return EMT_OK;
+}
+
+int emt_set_population(emt_handle_t* h, int32_t task, const float* x) {
+  if (!h || !x) return EMT_ERR_INVALID_ARG;
+  if (check_task(h, task)) return h->fail(EMT_ERR_INVALID_ARG, "task index out of range");
+  int rc = ensure_ready(h);
+  if (rc) return rc;
+  const TaskDev& d = h->table[task];
+  for (size_t k = 0; k < (size_t)d.NP * d.D; ++k)
+    if (!(x[k] >= d.lo && x[k] <= d.hi)) return h->fail(EMT_ERR_INVALID_ARG, "member outside the box");
+  cudaError_t e = cudaMemcpy2D(h->d_pop.p + d.pop_off, sizeof(float) * d.DP, x, sizeof(float) * d.D,
+                               sizeof(float) * d.D, d.NP, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return h->cuda_fail(e, "copy population");
+  emt::EpochArgs a = base_args(h, emt::MODE_EVAL);
+  a.single_task = task;
+  int le = emt_launch_epoch(a, 1, h->stream);
+  if (le) return h->cuda_fail((cudaError_t)le, "evaluate launch");
+  return emt_sync(h);
+}
+
+int emt_get_task_params(emt_handle_t* h, int32_t task, float* rotation, float* shift) {
+  if (!h) return EMT_ERR_INVALID_ARG;
+  if (check_task(h, task)) return h->fail(EMT_ERR_INVALID_ARG, "task index out of range");
+  const HostTask& t = h->tasks[task];
+  if (rotation) std::memcpy(rotation, t.Q.data(), sizeof(float) * t.Q.size());
+  if (shift) std::memcpy(shift, t.o.data(), sizeof(float) * t.o.size());
+  return EMT_OK;
+}
+
+int emt_evaluate(emt_handle_t* h, int32_t task, int32_t n, const float* x, float* fitness,
+                 float* z) {
+  if (!h || (n > 0 && (!x || !fitness)) || n < 0) return EMT_ERR_INVALID_ARG;
+  if (check_task(h, task)) return h->fail(EMT_ERR_INVALID_ARG, "task index out of range");
+  int rc = upload(h);
+  if (rc) return rc;
+  if (n == 0) return EMT_OK;
+  const HostTask& t = h->tasks[task];
+  float *dx = nullptr, *df = nullptr, *dz = nullptr;
+  cudaError_t e;
+  if ((e = cudaMalloc(&dx, sizeof(float) * (size_t)n * t.D)) != cudaSuccess) return h->cuda_fail(e, "cudaMalloc");
+  if ((e = cudaMalloc(&df, sizeof(float) * (size_t)n)) != cudaSuccess) {
+    cudaFree(dx);
+    return h->cuda_fail(e, "cudaMalloc");
+  }
+  if (z && (e = cudaMalloc(&dz, sizeof(float) * (size_t)n * t.D)) != cudaSuccess) {
+    cudaFree(dx);
+    cudaFree(df);
+    return h->cuda_fail(e, "cudaMalloc");
+  }
+  e = cudaMemcpy(dx, x, sizeof(float) * (size_t)n * t.D, cudaMemcpyHostToDevice);
+  int out = EMT_OK;
+  if (e == cudaSuccess) {
+    emt::EvalArgs a{h->d_tasks.p, task, n, dx, df, dz, h->d_qt.p, h->d_shift.p, h->d_err.p,
+                    emt::smem_layout(t.D, 64).total};
+    int le = emt_launch_eval(a, h->stream);
+    if (le) out = h->cuda_fail((cudaError_t)le, "evaluate launch");
+    else if ((out = emt_sync(h)) == EMT_OK) {
+      e = cudaMemcpy(fitness, df, sizeof(float) * n, cudaMemcpyDeviceToHost);
+      if (e == cudaSuccess && z) e = cudaMemcpy(z, dz, sizeof(float) * (size_t)n * t.D, cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) out = h->cuda_fail(e, "copy results");
+    }
+  } else {
+    out = h->cuda_fail(e, "copy points");
+  }
+  cudaFree(dx);
+  cudaFree(df);
+  if (dz) cudaFree(dz);
+  return out;
+}
+
+int emt_get_stats(emt_handle_t* h, emt_stats* out) {
+  if (!h || !out) return EMT_ERR_INVALID_ARG;
+  std::memset(out, 0, sizeof(*out));
+  out->n_tasks = (int32_t)h->tasks.size();
+  out->precision_used = EMT_ROT_FP32;
+  if (h->d_stats.p) {
+    int rc = emt_sync(h);
+    if (rc) return rc;
+    unsigned long long s[4];
+    cudaError_t e = cudaMemcpy(s, h->d_stats.p, sizeof(s), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return h->cuda_fail(e, "copy stats");
+    out->rechecks = s[0];
+    out->recheck_flips = s[1];
+    out->transfers_accepted = s[2];
+    out->evaluations = s[3];
+    out->generations = h->initialized ? (uint64_t)h->gdone * h->tasks.size() : 0;
+  }
+  out->device_ms = h->device_ms;
+  return EMT_OK;
+}
+
+// Checkpoint layout: magic, task count, generation counter, then per task
+// pop (NP*D floats), fit32, tol32 (NP floats), fit64 (NP doubles), gen.
+static const uint64_t kSnapMagic = 0x31504E5354464D45ull;  // "EMFTSNP1"
+
+int emt_snapshot_size(emt_handle_t* h, size_t* bytes) {
+  if (!h || !bytes) return EMT_ERR_INVALID_ARG;
+  size_t s = 3 * sizeof(uint64_t);
+  for (const auto& t : h->tasks) s += (size_t)t.NP * t.D * 4 + (size_t)t.NP * (4 + 4 + 8) + 4;
+  *bytes = s;
+  return EMT_OK;
+}
+
+int emt_snapshot(emt_handle_t* h, void* buf, size_t bytes) {
+  if (!h || !buf) return EMT_ERR_INVALID_ARG;
+  size_t need = 0;
+  emt_snapshot_size(h, &need);
+  if (bytes < need) return h->fail(EMT_ERR_INVALID_ARG, "snapshot buffer too small");
+  int rc = ensure_ready(h);
+  if (rc) return rc;
+  unsigned char* p = (unsigned char*)buf;
+  uint64_t hdr[3] = {kSnapMagic, (uint64_t)h->tasks.size(), (uint64_t)h->gdone};
+  std::memcpy(p, hdr, sizeof(hdr));
+  p += sizeof(hdr);
+  for (size_t t = 0; t < h->tasks.size(); ++t) {
+    const TaskDev& d = h->table[t];
+    cudaError_t e = cudaMemcpy2D(p, sizeof(float) * d.D, h->d_pop.p + d.pop_off, sizeof(float) * d.DP,
+                                 sizeof(float) * d.D, d.NP, cudaMemcpyDeviceToHost);
+    p += (size_t)d.NP * d.D * 4;
+    if (e == cudaSuccess) e = cudaMemcpy(p, h->d_fit32.p + d.fit_off, 4 * (size_t)d.NP, cudaMemcpyDeviceToHost);
+    p += 4 * (size_t)d.NP;
+    if (e == cudaSuccess) e = cudaMemcpy(p, h->d_tol32.p + d.fit_off, 4 * (size_t)d.NP, cudaMemcpyDeviceToHost);
+    p += 4 * (size_t)d.NP;
+    if (e == cudaSuccess) e = cudaMemcpy(p, h->d_fit64.p + d.fit_off, 8 * (size_t)d.NP, cudaMemcpyDeviceToHost);
+    p += 8 * (size_t)d.NP;
+    if (e == cudaSuccess) e = cudaMemcpy(p, h->d_gen.p + t, 4, cudaMemcpyDeviceToHost);
+    p += 4;
+    if (e != cudaSuccess) return h->cuda_fail(e, "snapshot");
+  }
+  return EMT_OK;
+}
+
+int emt_restore(emt_handle_t* h, const void* buf, size_t bytes) {
+  if (!h || !buf) return EMT_ERR_INVALID_ARG;
+  size_t need = 0;
+  emt_snapshot_size(h, &need);
+  if (bytes < need) return h->fail(EMT_ERR_INVALID_ARG, "snapshot too small");
+  const unsigned char* p = (const unsigned char*)buf;
+  uint64_t hdr[3];
+  std::memcpy(hdr, p, sizeof(hdr));
+  p += sizeof(hdr);
+  if (hdr[0] != kSnapMagic || hdr[1] != h->tasks.size())
+    return h->fail(EMT_ERR_INVALID_ARG, "snapshot does not match this handle");
+  int rc = upload(h);
+  if (rc) return rc;
+  for (size_t t = 0; t < h->tasks.size(); ++t) {
+    const TaskDev& d = h->table[t];
+    cudaError_t e = cudaMemcpy2D(h->d_pop.p + d.pop_off, sizeof(float) * d.DP, p, sizeof(float) * d.D,
+                                 sizeof(float) * d.D, d.NP, cudaMemcpyHostToDevice);
+    p += (size_t)d.NP * d.D * 4;
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_fit32.p + d.fit_off, p, 4 * (size_t)d.NP, cudaMemcpyHostToDevice);
+    p += 4 * (size_t)d.NP;
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_tol32.p + d.fit_off, p, 4 * (size_t)d.NP, cudaMemcpyHostToDevice);
+    p += 4 * (size_t)d.NP;
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_fit64.p + d.fit_off, p, 8 * (size_t)d.NP, cudaMemcpyHostToDevice);
+    p += 8 * (size_t)d.NP;
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_gen.p + t, p, 4, cudaMemcpyHostToDevice);
+    p += 4;
+    if (e != cudaSuccess) return h->cuda_fail(e, "restore");
+  }
+  h->gdone = (uint32_t)hdr[2];
+  h->initialized = true;
+  h->elite_parity = 0;
+  return EMT_OK;
+}
+
+const char* emt_last_error(const emt_handle_t* h) { return h ? h->err.c_str() : "null handle"; }
+
+void emt_destroy(emt_handle_t* h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  h->d_tasks.release();
+  h->d_order.release();
+  h->d_pop.release();
+  h->d_fit32.release();
+  h->d_tol32.release();
+  h->d_qt.release();
+  h->d_shift.release();
+  h->d_elites[0].release();
+  h->d_elites[1].release();
+  h->d_best_f32.release();
+  h->d_fit64.release();
+  h->d_best_f64.release();
+  h->d_gen.release();
+  h->d_stats.release();
+  h->d_err.release();
+  h->d_best_idx.release();
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  delete h;
+}
+
+}  // extern "C"

@@ -1,0 +1,451 @@
+// emt_functions.cuh -- the seven benchmark functions on the device.
+//
+// FP32 form (every evaluation): one warp per individual, lanes over genes,
+// butterfly reductions (a fixed order, so results repeat run to run).  Besides
+// f it returns the "scale", the sum of absolute sub-terms, which bounds the
+// rounding error of f and sets the FP64 re-check window.
+//
+// FP64-class form (re-check of near-tie selections): the rotation by a
+// compensated double-FP32 dot product (dot2_rotation) and the terms in double
+// precision; Weierstrass reduces each argument exactly (eval_row_weier_precise).
+//
+// Definitions follow the reference's evaluation() (proposed model/
+// SG-EMTF.cu:898-1111): Sphere :918, Rosenbrock :939, Ackley :963 (E =
+// 2.718282 in reference mode), Rastrigin :991, Griewank :1014 (product as in
+// SG-EMTF_DE.cu:989; EMT_FLAG_REF_GRIEWANK_NO_PRODUCT drops it as the GA file
+// does), Weierstrass :1049 (a = 0.5, b = 3, k = 0..20), Schwefel :1079.
+#pragma once
+
+#include "emt_internal.h"
+
+namespace emt {
+
+enum Fid : int {
+  F_SPHERE = 0,
+  F_RASTRIGIN = 1,
+  F_ACKLEY = 2,
+  F_GRIEWANK = 3,
+  F_ROSENBROCK = 4,
+  F_SCHWEFEL = 5,
+  F_WEIERSTRASS = 6
+};
+
+constexpr uint32_t FLAG_REF_GRIEWANK_NO_PRODUCT = 0x1u;
+constexpr uint32_t FLAG_REF_WEIERSTRASS_CONST = 0x2u;
+constexpr uint32_t FLAG_REF_ACKLEY_E = 0x4u;
+constexpr uint32_t FLAG_REF_BOXES = 0x8u;
+constexpr uint32_t FLAG_NO_RECHECK = 0x10u;
+
+// Weierstrass terms k = 0..20 of one gene: sum of 0.5^k cos(2 pi 3^k (z + 1/2))
+// and of their absolute values.  cos(2 pi 3^k (z + 1/2)) = -cos(pi y_k) with
+// y_k = 2 * 3^k * |z| (3^k is odd).  y_k mod 2 is computed exactly from the
+// FP32 significand of z for k <= 6; terms k >= 7 follow the angle-tripling
+// identity cos(3t) = cos t (4 cos^2 t - 3), whose error grows 3x per step but
+// is weighted 0.5^k (total below 1.5e-6 per gene).
+__device__ __forceinline__ void weier_gene_f32(float z, float& sum, float& sabs) {
+  const float az = fabsf(z);
+  const uint32_t bits = __float_as_uint(az);
+  const uint32_t E = bits >> 23;
+  const uint32_t M = (bits & 0x7FFFFFu) | 0x800000u;
+  const int sh = 149 - (int)E;  // y_0 = M / 2^sh for normal az
+  float s = 0.f, sa = 0.f, ak = 1.f, c = 1.f;
+  if (E == 0u || sh > 61) {
+    float p3 = 2.f;
+#pragma unroll
+    for (int k = 0; k <= 6; ++k) {
+      c = cospif(p3 * az);
+      s = fmaf(ak, -c, s);
+      sa = fmaf(ak, fabsf(c), sa);
+      ak *= 0.5f;
+      p3 *= 3.f;
+    }
+  } else if (sh <= 0) {
+    c = (sh == 0 && (M & 1u)) ? -1.f : 1.f;  // y_k integer, parity of M 3^k
+#pragma unroll
+    for (int k = 0; k <= 6; ++k) {
+      s = fmaf(ak, -c, s);
+      sa += ak;
+      ak *= 0.5f;
+    }
+  } else if (sh <= 31) {
+    const uint32_t mask = (2u << sh) - 1u;
+    const float scale = __uint_as_float((uint32_t)(127 - sh) << 23);
+    uint32_t r = M & mask;
+#pragma unroll
+    for (int k = 0; k <= 6; ++k) {
+      c = cospif((float)r * scale);
+      s = fmaf(ak, -c, s);
+      sa = fmaf(ak, fabsf(c), sa);
+      ak *= 0.5f;
+      r = (r * 3u) & mask;
+    }
+  } else {
+    const unsigned long long mask = (2ull << sh) - 1ull;
+    const float scale = __uint_as_float((uint32_t)(127 - sh) << 23);
+    unsigned long long r = M;
+#pragma unroll
+    for (int k = 0; k <= 6; ++k) {
+      c = cospif((float)r * scale);
+      s = fmaf(ak, -c, s);
+      sa = fmaf(ak, fabsf(c), sa);
+      ak *= 0.5f;
+      r = (r * 3ull) & mask;
+    }
+  }
+#pragma unroll
+  for (int k = 7; k <= 20; ++k) {
+    c = c * fmaf(4.f * c, c, -3.f);
+    s = fmaf(ak, -c, s);
+    sa = fmaf(ak, fabsf(c), sa);
+    ak *= 0.5f;
+  }
+  sum = s;
+  sabs = sa;
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int m = 16; m > 0; m >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, m);
+  return v;
+}
+__device__ __forceinline__ float warp_prod(float v) {
+#pragma unroll
+  for (int m = 16; m > 0; m >>= 1) v *= __shfl_xor_sync(0xFFFFFFFFu, v, m);
+  return v;
+}
+__device__ __forceinline__ double warp_sum64(double v) {
+#pragma unroll
+  for (int m = 16; m > 0; m >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, m);
+  return v;
+}
+__device__ __forceinline__ double warp_prod64(double v) {
+#pragma unroll
+  for (int m = 16; m > 0; m >>= 1) v *= __shfl_xor_sync(0xFFFFFFFFu, v, m);
+  return v;
+}
+
+// Bound on the Weierstrass error caused by rounding of the rotation, per
+// member: |dz_j| <= (gamma_{D+1} + 2^-20) * |q_j|_2 * |x - o|_2 (Cauchy-Schwarz
+// on the worst-case FP32 dot-product bound, plus the TF32 split error), pushed
+// through every term and capped by the term's range.
+__device__ __forceinline__ float weier_rotation_bound(int D, float qnorm, float snorm) {
+  const float u = 0x1p-24f;
+  const float g = (float)(D + 1) * u / (1.f - (float)(D + 1) * u) + 0x1p-20f;
+  const float dz = g * qnorm * snorm + u * snorm;
+  float b = 0.f, ak = 1.f, e = 6.2831855f * dz;
+#pragma unroll
+  for (int k = 0; k <= 20; ++k) {
+    b = fmaf(ak, fminf(e, 2.f), b);
+    ak *= 0.5f;
+    e *= 3.f;
+  }
+  return (float)D * (b + 4e-6f);
+}
+
+struct FnConst {
+  int fid, D;
+  uint32_t flags;
+  float woff, qnorm, rel;
+  double woff64;
+};
+
+// FP32 fitness of one rotated row z[0..D) (shared memory), evaluated by the
+// calling warp; x is the unrotated row and o the shift.  Returns f; *tol
+// gets the half-width of the near-tie window, rel * scale, where scale is the
+// sum of absolute sub-terms of f and rel the stated accuracy of the FP32 form
+// (1e-5; the parity tests check |f - f64| <= 1e-5 scale).  Weierstrass adds
+// the conditioning bound of its 3^k-amplified terms (weier_rotation_bound).
+// Near an optimum the forms below avoid cancellation: Ackley uses expm1 of
+// sum z^2 and of sum sin^2(pi z), Griewank 1 - prod cos = -expm1(sum
+// log1p(-2 sin^2(theta/2))), Rastrigin z^2 + 20 sin^2(pi z).
+__device__ float eval_row_f32(const FnConst& fc, const float* __restrict__ z,
+                              const float* __restrict__ x, const float* __restrict__ o,
+                              float* tol) {
+  const int lane = threadIdx.x & 31;
+  const int D = fc.D;
+  float a = 0.f, b = 0.f, c = 1.f, sa = 0.f, ss = 0.f;
+  int neg = 0;
+  switch (fc.fid) {
+    case F_SPHERE:
+      for (int j = lane; j < D; j += 32) {
+        const float v = z[j];
+        a = fmaf(v, v, a);
+      }
+      sa = a;
+      break;
+    case F_RASTRIGIN:
+      for (int j = lane; j < D; j += 32) {
+        const float v = z[j], sp = sinpif(v), z2 = v * v;
+        const float t = fmaf(20.f * sp, sp, z2);
+        a += t;
+        sa += t;
+      }
+      break;
+    case F_ACKLEY:
+      for (int j = lane; j < D; j += 32) {
+        const float v = z[j], sp = sinpif(v);
+        a = fmaf(v, v, a);
+        b = fmaf(sp, sp, b);           // sum sin^2(pi z)
+      }
+      break;
+    case F_GRIEWANK:
+      for (int j = lane; j < D; j += 32) {
+        const float v = z[j];
+        a = fmaf(v, v, a);
+        if (!(fc.flags & FLAG_REF_GRIEWANK_NO_PRODUCT)) {
+          const float th = __fdiv_rn(v, sqrtf((float)(j + 1)));
+          const float ct = cosf(th);
+          c *= ct;
+          if (ct > 0.f) {
+            const float sh = sinf(0.5f * th);
+            b += log1pf(-2.f * sh * sh);
+          } else {
+            neg = 1;
+          }
+        }
+      }
+      break;
+    case F_ROSENBROCK:
+      for (int j = lane; j + 1 < D; j += 32) {
+        const float v = z[j], n = z[j + 1];
+        const float t1 = fmaf(v, v, -n), t2 = v - 1.f;
+        const float t = fmaf(100.f * t1, t1, t2 * t2);
+        a += t;
+        sa += t + 200.f * fabsf(t1) * fmaf(v, v, fabsf(n)) + 2.f * fabsf(t2) * (fabsf(v) + 1.f);
+      }
+      break;
+    case F_SCHWEFEL:
+      for (int j = lane; j < D; j += 32) {
+        const float v = z[j], r = sqrtf(fabsf(v)), sr = sinf(r), t = v * sr;
+        a += t;
+        sa += fabsf(t);
+      }
+      break;
+    case F_WEIERSTRASS:
+      for (int j = lane; j < D; j += 32) {
+        float t, ta;
+        weier_gene_f32(z[j], t, ta);
+        a += t;
+        sa += ta;
+        const float d = x[j] - o[j];
+        ss = fmaf(d, d, ss);
+      }
+      break;
+    default:
+      break;
+  }
+  a = warp_sum(a);
+  sa = warp_sum(sa);
+  float f, scale;
+  switch (fc.fid) {
+    case F_ACKLEY: {
+      b = warp_sum(b);
+      const float e = 2.71828183f;
+      const float eref = (fc.flags & FLAG_REF_ACKLEY_E) ? 2.718282f - e : 0.f;
+      const float r = sqrtf(a / (float)D);
+      const float t1 = -20.f * expm1f(-0.2f * r);       // 20 - 20 exp(-0.2 sqrt(A/D))
+      const float t2 = -e * expm1f(-2.f * b / (float)D); // e - exp(sum cos(2 pi z) / D)
+      f = t1 + t2 + eref;
+      scale = t1 + t2 + fabsf(eref);
+      break;
+    }
+    case F_GRIEWANK: {
+      float om;  // 1 - prod cos
+      if (fc.flags & FLAG_REF_GRIEWANK_NO_PRODUCT) {
+        om = 0.f;
+        scale = a / 4000.f;
+      } else {
+        b = warp_sum(b);
+        c = warp_prod(c);
+        neg = __any_sync(0xFFFFFFFFu, neg);
+        om = neg ? 1.f - c : -expm1f(b);
+        scale = a / 4000.f + fabsf(om) + (neg ? fabsf(c) + 1.f : 0.f);
+      }
+      f = om + a / 4000.f;
+      break;
+    }
+    case F_SCHWEFEL:
+      f = 418.9829f * (float)D - a;
+      scale = 418.9829f * (float)D + sa;
+      break;
+    case F_WEIERSTRASS:
+      f = a + fc.woff;
+      scale = sa + fabsf(fc.woff);
+      break;
+    default:  // sphere, rastrigin, rosenbrock: non-negative sums
+      f = a;
+      scale = sa;
+      break;
+  }
+  float t = fc.rel * scale;
+  if (fc.fid == F_WEIERSTRASS) t += weier_rotation_bound(D, fc.qnorm, sqrtf(warp_sum(ss)));
+  *tol = t;
+  return f;
+}
+
+// s + e = a + b exactly (Knuth's TwoSum).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// One Weierstrass gene from a high-precision argument z (double holding a
+// double-FP32 value): y_k = 2 * 3^k * |z| mod 2 is reduced exactly on the
+// 53-bit significand (r <- 3 r mod 2^(sh+1)), then cos(pi y_k) in FP32;
+// the 21 terms are summed with Kahan compensation.
+__device__ __forceinline__ float weier_gene_precise(double z) {
+  const double az = fabs(z);
+  const unsigned long long b = (unsigned long long)__double_as_longlong(az);
+  const int E = (int)(b >> 52);
+  const unsigned long long M = (b & ((1ull << 52) - 1ull)) | (1ull << 52);
+  const int sh = 1074 - E;  // y_0 = M / 2^sh for normal az
+  float s = 0.f, comp = 0.f, ak = 1.f;
+  auto add = [&](float c) {
+    const float v = __fsub_rn(__fmul_rn(-ak, c), comp);
+    const float t = __fadd_rn(s, v);
+    comp = __fsub_rn(__fsub_rn(t, s), v);
+    s = t;
+    ak *= 0.5f;
+  };
+  if (az == 0.0) {
+    for (int k = 0; k <= 20; ++k) add(1.f);
+  } else if (E == 0 || sh > 61) {
+    double p3 = 2.0;
+    for (int k = 0; k <= 20; ++k) {
+      double y = p3 * az;
+      y -= 2.0 * floor(0.5 * y);
+      add(cospif((float)y));
+      p3 *= 3.0;
+    }
+  } else if (sh <= 0) {
+    const float c = (sh == 0 && (M & 1ull)) ? -1.f : 1.f;
+    for (int k = 0; k <= 20; ++k) add(c);
+  } else {
+    const unsigned long long mask = (2ull << sh) - 1ull;
+    unsigned long long r = M & mask;
+    const int drop = sh > 24 ? sh - 24 : 0;
+    const float scale = __uint_as_float((uint32_t)(127 - (sh - drop)) << 23);
+    for (int k = 0; k <= 20; ++k) {
+      add(cospif((float)(r >> drop) * scale));
+      r = (r * 3ull) & mask;
+    }
+  }
+  return s;
+}
+
+// z_n = sum_k q_nk (x_k - o_k) to FP64-class accuracy on the FP32 pipe: the
+// compensated dot product of Ogita, Rump and Oishi ("Dot2", SIAM J. Sci.
+// Comput. 26, 2005) over the exact split x_k - o_k = sh_k + sl_k, so that
+// |z - z_exact| <~ u |z| + gamma_D^2 sum_k |q_nk||x_k - o_k|.  This GPU's
+// FP64 pipe runs at a small fraction of its FP32 rate, so ~12 FP32
+// operations per product beat one FP64 FMA.
+__device__ __forceinline__ double dot2_rotation(const float* __restrict__ x,
+                                                const float* __restrict__ o,
+                                                const float* __restrict__ qt, int DP, int D,
+                                                int n) {
+  float S = 0.f, C = 0.f;
+  for (int k = 0; k < D; ++k) {
+    const float q = qt[k * DP + n];
+    float sh, sl;
+    two_sum(x[k], -o[k], sh, sl);
+    const float p = __fmul_rn(q, sh);
+    const float pe = __fmaf_rn(q, sh, -p);
+    float t, te;
+    two_sum(S, p, t, te);
+    S = t;
+    C = __fmaf_rn(q, sl, __fadd_rn(C, __fadd_rn(te, pe)));
+  }
+  return (double)S + (double)C;
+}
+
+// Weierstrass re-check: z_n by dot2_rotation, then the exactly reduced terms
+// above (FP32/INT pipes only).
+__device__ double eval_row_weier_precise(const FnConst& fc, const float* __restrict__ x,
+                                         const float* __restrict__ o,
+                                         const float* __restrict__ qt, int DP, double woff64) {
+  const int lane = threadIdx.x & 31;
+  double acc = 0.0;
+  for (int n = lane; n < fc.D; n += 32)
+    acc += (double)weier_gene_precise(dot2_rotation(x, o, qt, DP, fc.D, n));
+  acc = warp_sum64(acc);
+  return acc + woff64;
+}
+
+// FP64-class fitness of x (shared memory row), evaluated by the calling warp:
+// z_n = sum_k Q[n][k] (x_k - o_k) by dot2_rotation (qt[k*DP + n] = Q[n][k]),
+// terms in double.  zbuf: DP doubles of per-warp scratch.
+__device__ double eval_row_f64(const FnConst& fc, const float* __restrict__ x,
+                               const float* __restrict__ o, const float* __restrict__ qt,
+                               int DP, double* zbuf) {
+  if (fc.fid == F_WEIERSTRASS) return eval_row_weier_precise(fc, x, o, qt, DP, fc.woff64);
+  const int lane = threadIdx.x & 31;
+  const int D = fc.D;
+  for (int n = lane; n < D; n += 32) zbuf[n] = dot2_rotation(x, o, qt, DP, D, n);
+  __syncwarp();
+  double a = 0.0, b = (fc.fid == F_GRIEWANK) ? 1.0 : 0.0;
+  switch (fc.fid) {
+    case F_SPHERE:
+      for (int j = lane; j < D; j += 32) a = fma(zbuf[j], zbuf[j], a);
+      break;
+    case F_RASTRIGIN:
+      for (int j = lane; j < D; j += 32) {
+        double v = zbuf[j];
+        a += v * v - 10.0 * cospi(2.0 * v) + 10.0;
+      }
+      break;
+    case F_ACKLEY:
+      for (int j = lane; j < D; j += 32) {
+        double v = zbuf[j];
+        a = fma(v, v, a);
+        b += cospi(2.0 * v);
+      }
+      break;
+    case F_GRIEWANK:
+      for (int j = lane; j < D; j += 32) {
+        double v = zbuf[j];
+        a = fma(v, v, a);
+        if (!(fc.flags & FLAG_REF_GRIEWANK_NO_PRODUCT)) b *= cos(v / sqrt((double)(j + 1)));
+      }
+      break;
+    case F_ROSENBROCK:
+      for (int j = lane; j + 1 < D; j += 32) {
+        double v = zbuf[j], n = zbuf[j + 1];
+        double t1 = v * v - n, t2 = v - 1.0;
+        a += 100.0 * t1 * t1 + t2 * t2;
+      }
+      break;
+    case F_SCHWEFEL:
+      for (int j = lane; j < D; j += 32) {
+        double v = zbuf[j];
+        a += v * sin(sqrt(fabs(v)));
+      }
+      break;
+    default:
+      break;
+  }
+  a = warp_sum64(a);
+  double f;
+  switch (fc.fid) {
+    case F_ACKLEY: {
+      b = warp_sum64(b);
+      const double e = (fc.flags & FLAG_REF_ACKLEY_E) ? 2.718282 : 2.718281828459045;
+      f = -20.0 * exp(-0.2 * sqrt(a / D)) - exp(b / D) + 20.0 + e;
+      break;
+    }
+    case F_GRIEWANK:
+      b = warp_prod64(b);
+      f = 1.0 + a / 4000.0 - b;
+      break;
+    case F_SCHWEFEL:
+      f = 418.9829 * D - a;
+      break;
+    default:
+      f = a;
+      break;
+  }
+  __syncwarp();
+  return f;
+}
+
+}  // namespace emt

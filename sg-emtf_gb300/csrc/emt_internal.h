@@ -1,0 +1,150 @@
+// emt_internal.h -- device-side task table, launch arguments and the shared
+// memory layout of the fused epoch kernel.  Shared by emt_kernels.cu (device
+// code) and emt_api.cu (host orchestration); not part of the public ABI.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include "emt_common.cuh"
+
+namespace emt {
+
+constexpr int kThreads = 256;  // one CTA per task, 8 warps
+constexpr int kWarps = kThreads / 32;
+constexpr int kMaxDim = 128;
+constexpr int kMaxPop = 256;
+
+// Per-task descriptor resident in HBM.  Row strides are padded to DP (a
+// multiple of 4 floats) so every population row starts 16-byte aligned and
+// moves as float4.
+struct TaskDev {
+  int32_t fid, D, NP, DP;
+  float lo, hi;
+  float woff;   // Weierstrass offset added to the term sum
+  float qnorm;  // max row 2-norm of Q (rounding bound of the rotation)
+  double woff64;  // the same offset in double precision
+  int64_t pop_off;    // floats, into pop[]: NP rows of DP
+  int64_t q_off;      // floats, into qt[]: D rows of DP, qt[k][n] = Q[n][k]
+  int64_t o_off;      // floats, into shift[]: DP
+  int64_t elite_off;  // floats, into elites[]: kmax rows of DP
+  int32_t fit_off;    // into fit32[], tol32[], fit64[]: NP
+  uint32_t flags;
+  int32_t qt_in_smem;  // 1: Q staged in shared memory; 0: read through L1
+  int32_t pad_;
+};
+
+// Largest dynamic shared memory a CTA may use (GB300: 227 KB).
+constexpr size_t kSmemLimit = 227 * 1024;
+
+enum Mode : int { MODE_EPOCH = 0, MODE_INIT = 1, MODE_EVAL = 2 };
+
+struct EpochArgs {
+  const TaskDev* tasks;
+  const int32_t* order;  // CTA -> task (longest-first)
+  int32_t single_task;   // >= 0: the grid's one CTA works on this task
+  int32_t n_tasks;
+  int32_t mode;
+  float* pop;
+  float* fit32;
+  float* tol32;
+  double* fit64;
+  const float* qt;
+  const float* shift;
+  uint32_t* gen;  // generations completed per task
+  int32_t gens;   // generations in this launch
+  int32_t algorithm;
+  float F, CR, eta_c, p_c, eta_m, p_m;
+  uint64_t seed;
+  float recheck_rel;
+  uint32_t flags;
+  // elite transfer
+  int32_t transfer_import, transfer_export;
+  float transfer_rate, transfer_mix;
+  const float* elites_in;
+  float* elites_out;
+  unsigned long long* stats;  // [0] rechecks [1] flips [2] transfers [3] evaluations
+  int32_t* err;               // first kernel-side check that fired (0 = none)
+  size_t smem_bytes;          // dynamic shared memory the launch provides
+};
+
+// Arguments of the standalone evaluation kernel (emt_evaluate).
+struct EvalArgs {
+  const TaskDev* tasks;
+  int32_t task;
+  int32_t n;
+  const float* x;  // n * D, unpadded
+  float* f;        // n
+  float* z;        // n * D or null
+  const float* qt;
+  const float* shift;
+  int32_t* err;
+  size_t smem_bytes;
+};
+
+EMT_HD int round4(int v) { return (v + 3) & ~3; }
+EMT_HD size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
+
+struct Layout {
+  int DP, NPP;
+  size_t fit64, z64, X, U, ST, Z, QT, o, fit, tol, ftr, ttr, idx, flag, list, misc, total;
+};
+
+// Shared-memory carve-up for one task; identical on host and device.  With
+// qt_in_smem false the rotation is read from global memory (L1/L2) instead,
+// for islands too large to hold Q next to the population.
+EMT_HD Layout smem_layout(int D, int NP, bool qt_in_smem = true) {
+  Layout L;
+  L.DP = round4(D);
+  L.NPP = round4(NP);
+  size_t off = 0;
+  L.fit64 = off; off = align16(off + sizeof(double) * NP);
+  L.z64 = off;   off = align16(off + sizeof(double) * kWarps * L.DP);
+  L.X = off;     off = align16(off + sizeof(float) * NP * L.DP);
+  L.U = off;     off = align16(off + sizeof(float) * NP * L.DP);
+  L.ST = off;    off = align16(off + sizeof(float) * L.DP * L.NPP);
+  L.Z = off;     off = align16(off + sizeof(float) * NP * L.DP);
+  L.QT = off;    off = align16(off + (qt_in_smem ? sizeof(float) * D * L.DP : 0));
+  L.o = off;     off = align16(off + sizeof(float) * L.DP);
+  L.fit = off;   off = align16(off + sizeof(float) * NP);
+  L.tol = off;   off = align16(off + sizeof(float) * NP);
+  L.ftr = off;   off = align16(off + sizeof(float) * NP);
+  L.ttr = off;   off = align16(off + sizeof(float) * NP);
+  L.idx = off;   off = align16(off + sizeof(int) * 4 * NP);
+  L.flag = off;  off = align16(off + sizeof(int) * NP);
+  L.list = off;  off = align16(off + sizeof(int) * NP);
+  L.misc = off;  off = align16(off + sizeof(int) * 8);
+  L.total = off;
+  return L;
+}
+
+// Error codes written to EpochArgs::err by the kernels' own checks.
+enum DeviceCheck : int32_t {
+  CHECK_OK = 0,
+  CHECK_BAD_DESCRIPTOR = 1,
+  CHECK_SMEM_TOO_SMALL = 2,
+  CHECK_BAD_PARTNER = 3
+};
+
+// Arguments of the best-member kernel (popSort + messageTransfer,
+// SG-EMTF.cu:462-486,1601-1615): per task, warp-shuffle argmin of the FP32
+// fitness, then the winner's fitness in FP64.
+struct BestArgs {
+  const TaskDev* tasks;
+  int32_t n_tasks;
+  const float* pop;
+  const float* fit32;
+  const double* fit64;
+  const float* qt;
+  const float* shift;
+  int32_t* best_idx;
+  float* best_f32;
+  double* best_f64;
+};
+
+}  // namespace emt
+
+// Kernel launchers (emt_kernels.cu).
+int emt_launch_epoch(const emt::EpochArgs& a, int grid, void* stream);
+int emt_launch_eval(const emt::EvalArgs& a, void* stream);
+int emt_launch_best(const emt::BestArgs& a, void* stream);

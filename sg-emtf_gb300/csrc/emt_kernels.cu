@@ -1,0 +1,584 @@
+// emt_kernels.cu -- the fused generation kernel (FP32 CUDA-core rotation form)
+// and the standalone evaluation kernel.
+//
+// One CTA owns one task for a whole epoch (all generations between two elite
+// transfers).  Its island lives in shared memory across generations, as the
+// reference's GeneticOpera keeps its sub-population in shared memory
+// (proposed model/SG-EMTF.cu:1289-1426), but without the reference's
+// cross-block shuffle and its unbounded grid spin (:1384-1392): an island is
+// owned by exactly one CTA, so no CTA ever waits on another.
+//
+// Per generation (all in shared memory):
+//   1. trial vectors: DE/rand/1/bin, DE/current/1/bin or SBX + polynomial
+//      mutation, from the counter-based Philox stream (bit-exact with the
+//      host replay);
+//   2. rotation Z = (U - o) Q^T: 4x4 register tiles, float4 operand loads;
+//   3. function epilogue: one warp per trial, FP32 value + error scale;
+//   4. selection (ties go to the trial, SG-EMTF_DE.cu:679-706): a trial whose
+//      FP32 fitness lies within the rounding window of its parent's is
+//      re-decided in FP64 so that selections do not depend on FP32 rounding.
+#include <cuda_runtime.h>
+
+#include "emt_functions.cuh"
+
+namespace emt {
+
+struct Smem {
+  double *fit64, *z64;
+  float *X, *U, *ST, *Z, *QT, *o, *fit, *tol, *ftr, *ttr;
+  int *idx, *flag, *list, *misc;
+};
+
+__device__ __forceinline__ Smem carve(unsigned char* base, const Layout& L) {
+  Smem s;
+  s.fit64 = (double*)(base + L.fit64);
+  s.z64 = (double*)(base + L.z64);
+  s.X = (float*)(base + L.X);
+  s.U = (float*)(base + L.U);
+  s.ST = (float*)(base + L.ST);
+  s.Z = (float*)(base + L.Z);
+  s.QT = (float*)(base + L.QT);
+  s.o = (float*)(base + L.o);
+  s.fit = (float*)(base + L.fit);
+  s.tol = (float*)(base + L.tol);
+  s.ftr = (float*)(base + L.ftr);
+  s.ttr = (float*)(base + L.ttr);
+  s.idx = (int*)(base + L.idx);
+  s.flag = (int*)(base + L.flag);
+  s.list = (int*)(base + L.list);
+  s.misc = (int*)(base + L.misc);
+  return s;
+}
+
+__device__ __forceinline__ void report(int32_t* err, int32_t code) {
+  if (err) atomicCAS(err, 0, code);
+}
+
+__device__ __forceinline__ bool descriptor_ok(const TaskDev& t) {
+  return t.D >= 1 && t.D <= kMaxDim && t.NP >= 4 && t.NP <= kMaxPop && t.DP == round4(t.D) &&
+         t.fid >= 0 && t.fid <= F_WEIERSTRASS && t.lo < t.hi;
+}
+
+// Z[0..nrows) = ST^T Q^T over k < D; ST is [DP][NPP] (column i = row i of
+// U - o), QT is [D][DP] with zero padding beyond D.
+__device__ void rotate_f32(const Smem& s, int D, int DP, int NPP, int nrows) {
+  const int ncg = DP >> 2;
+  const int nrg = (nrows + 3) >> 2;
+  const int ntile = nrg * ncg;
+  for (int tt = threadIdx.x; tt < ntile; tt += kThreads) {
+    const int rg = tt / ncg, cg = tt - rg * ncg;
+    const float* a = s.ST + 4 * rg;
+    const float* b = s.QT + 4 * cg;
+    float c[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) c[r][q] = 0.f;
+#pragma unroll 2
+    for (int k = 0; k < D; ++k) {
+      const float4 av = *reinterpret_cast<const float4*>(a + k * NPP);
+      const float4 bv = *reinterpret_cast<const float4*>(b + k * DP);
+      const float ar[4] = {av.x, av.y, av.z, av.w};
+      const float br[4] = {bv.x, bv.y, bv.z, bv.w};
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) c[r][q] = fmaf(ar[r], br[q], c[r][q]);
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int row = 4 * rg + r;
+      if (row < nrows)
+        *reinterpret_cast<float4*>(s.Z + row * DP + 4 * cg) =
+            make_float4(c[r][0], c[r][1], c[r][2], c[r][3]);
+    }
+  }
+}
+
+// Evaluates rows [0, nrows) of `rows` (shared memory, stride DP) whose
+// differences rows - o are already in ST: rotation, then one warp per row.
+__device__ void evaluate_rows(const Smem& s, const FnConst& fc, const float* rows, int nrows,
+                              int DP, int NPP, float* fout, float* tout) {
+  rotate_f32(s, fc.D, DP, NPP, nrows);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int i = warp; i < nrows; i += kWarps) {
+    float t;
+    const float f = eval_row_f32(fc, s.Z + i * DP, rows + i * DP, s.o, &t);
+    if (lane == 0) {
+      fout[i] = f;
+      tout[i] = t;
+    }
+  }
+  __syncthreads();
+}
+
+// ST[j][i] = rows[i][j] - o[j] for i < nrows, j < D.
+__device__ void stage_differences(const Smem& s, const float* rows, int nrows, int D, int DP,
+                                  int NPP) {
+  for (int it = threadIdx.x; it < nrows * D; it += kThreads) {
+    const int j = it / nrows, i = it - j * nrows;
+    s.ST[j * NPP + i] = fsub(rows[i * DP + j], s.o[j]);
+  }
+}
+
+// Trial vectors of generation G into U (and U - o into ST).
+__device__ void build_trials(const Smem& s, const EpochArgs& a, const TaskDev& td, int task,
+                             uint32_t G, int DP, int NPP) {
+  const int D = td.D, NP = td.NP;
+  const float lo = td.lo, hi = td.hi;
+  if (a.algorithm == 0 || a.algorithm == 1) {
+    for (int i = threadIdx.x; i < NP; i += kThreads) {
+      const U4 w = draw(a.seed, (uint32_t)task, G, (uint32_t)i, P_DE_INDEX, 0);
+      int r1, r2, r3, jr;
+      de_indices(w, i, NP, D, r1, r2, r3, jr);
+      s.idx[4 * i + 0] = a.algorithm == 0 ? r1 : i;
+      s.idx[4 * i + 1] = r2;
+      s.idx[4 * i + 2] = r3;
+      s.idx[4 * i + 3] = jr;
+    }
+    __syncthreads();
+    const int nb = (D + 3) >> 2;
+    for (int it = threadIdx.x; it < NP * nb; it += kThreads) {
+      const int b = it / NP, i = it - b * NP;
+      const U4 w = draw(a.seed, (uint32_t)task, G, (uint32_t)i, P_DE_CR, (uint32_t)b);
+      const int base = s.idx[4 * i], r2 = s.idx[4 * i + 1], r3 = s.idx[4 * i + 2],
+                jr = s.idx[4 * i + 3];
+      const float* xb = s.X + base * DP;
+      const float* x2 = s.X + r2 * DP;
+      const float* x3 = s.X + r3 * DP;
+      const float* xi = s.X + i * DP;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int j = 4 * b + q;
+        if (j < D) {
+          const float m = clamp_box(ffma(a.F, fsub(x2[j], x3[j]), xb[j]), lo, hi);
+          const float tr = (u01(word(w, q)) < a.CR || j == jr) ? m : xi[j];
+          s.U[i * DP + j] = tr;
+          s.ST[j * NPP + i] = fsub(tr, s.o[j]);
+        }
+      }
+    }
+    return;
+  }
+  // GA: parent index per member (CrossPrep, SG-EMTF.cu:803-812), SBX on the
+  // pair (i, i^1) (:711-749) and polynomial mutation (:565-605).
+  for (int i = threadIdx.x; i < NP; i += kThreads)
+    s.idx[i] = (int)(draw(a.seed, (uint32_t)task, G, (uint32_t)i, P_GA_PARENT, 0).x % (uint32_t)NP);
+  __syncthreads();
+  const float ec = fdiv(1.f, fadd(a.eta_c, 1.f));
+  const float em1 = fadd(a.eta_m, 1.f), em = fdiv(1.f, em1);
+  const float pm = a.p_m < 0.f ? fdiv(1.f, (float)D) : a.p_m;
+  const float range = fsub(hi, lo);
+  const int nb = (D + 1) >> 1;
+  for (int it = threadIdx.x; it < NP * nb; it += kThreads) {
+    const int b = it / NP, i = it - b * NP;
+    const int r0 = s.idx[i];
+    const int pi = i ^ 1;
+    const int partner = pi < NP ? s.idx[pi] : r0;
+    const U4 ws = draw(a.seed, (uint32_t)task, G, (uint32_t)i, P_GA_SBX, (uint32_t)b);
+    const U4 wm = draw(a.seed, (uint32_t)task, G, (uint32_t)i, P_GA_PM, (uint32_t)b);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int j = 2 * b + h;
+      if (j >= D) break;
+      const float x0 = s.X[r0 * DP + j], x1 = s.X[partner * DP + j];
+      float c;
+      if (u01(word(ws, 2 * h)) < a.p_c) {
+        const float pu = u01(word(ws, 2 * h + 1));
+        const float tv = pu <= 0.5f ? fmul(2.f, pu) : fdiv(0.5f, fsub(1.f, pu));
+        float beta = det_powf(tv, ec);
+        if (i & 1) beta = -beta;
+        c = fmul(0.5f, ffma(fadd(1.f, beta), x0, fmul(fsub(1.f, beta), x1)));
+        c = clamp_box(c, lo, hi);
+      } else {
+        c = x0;
+      }
+      if (u01(word(wm, 2 * h)) < pm) {
+        const float um = u01(word(wm, 2 * h + 1));
+        float dq;
+        if (um <= 0.5f) {
+          const float d1 = fdiv(fsub(c, lo), range);
+          const float v = ffma(fsub(1.f, fmul(2.f, um)), det_powf(fsub(1.f, d1), em1), fmul(2.f, um));
+          dq = fsub(det_powf(v, em), 1.f);
+        } else {
+          const float d2 = fdiv(fsub(hi, c), range);
+          const float v = ffma(fmul(2.f, fsub(um, 0.5f)), det_powf(fsub(1.f, d2), em1),
+                               fmul(2.f, fsub(1.f, um)));
+          dq = fsub(1.f, det_powf(v, em));
+        }
+        c = clamp_box(ffma(dq, range, c), lo, hi);
+      }
+      s.U[i * DP + j] = c;
+      s.ST[j * NPP + i] = fsub(c, s.o[j]);
+    }
+  }
+}
+
+// Selection of nrows candidates (rows of U, fitness ftr/ttr) against members
+// target[c] (X rows).  strict: candidate must be strictly better (transfer);
+// otherwise ties go to the candidate (generation step).  Returns the number
+// of replacements (valid in thread 0).
+__device__ int select_and_replace(const Smem& s, const EpochArgs& a, const FnConst& fc,
+                                  int nrows, const int* target, bool strict, int DP,
+                                  unsigned long long* rechecks, unsigned long long* flips) {
+  const bool recheck = !(a.flags & FLAG_NO_RECHECK);
+  if (threadIdx.x == 0) s.misc[0] = 0;
+  __syncthreads();
+  for (int c = threadIdx.x; c < nrows; c += kThreads) {
+    const int m = target ? target[c] : c;
+    const float ft = s.ftr[c], fp = s.fit[m];
+    const bool d32 = strict ? (ft < fp) : (ft <= fp);
+    if (recheck && fabsf(ft - fp) <= s.ttr[c] + s.tol[m]) {
+      s.flag[c] = 2;
+      s.list[atomicAdd(&s.misc[0], 1)] = c;
+    } else {
+      s.flag[c] = d32 ? 1 : 0;
+    }
+  }
+  __syncthreads();
+  const int nre = s.misc[0];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int r = warp; r < nre; r += kWarps) {
+    const int c = s.list[r];
+    const int m = target ? target[c] : c;
+    double* zb = s.z64 + warp * DP;
+    // a candidate bit-identical to the member it would replace is a tie in
+    // any precision: no re-evaluation needed
+    bool same = true;
+    for (int j = lane; j < fc.D; j += 32)
+      same &= __float_as_uint(s.U[c * DP + j]) == __float_as_uint(s.X[m * DP + j]);
+    same = __all_sync(0xFFFFFFFFu, same);
+    double fp = s.fit64[m], ft;
+    if (same) {
+      ft = fp;
+    } else {
+      ft = eval_row_f64(fc, s.U + c * DP, s.o, s.QT, DP, zb);
+      if (isnan(fp)) fp = eval_row_f64(fc, s.X + m * DP, s.o, s.QT, DP, zb);
+    }
+    const bool d64 = same ? !strict : (strict ? (ft < fp) : (ft <= fp));
+    const bool d32 = strict ? (s.ftr[c] < s.fit[m]) : (s.ftr[c] <= s.fit[m]);
+    if (lane == 0) {
+      s.flag[c] = d64 ? 3 : 0;
+      // FP64 value of whichever vector member m holds after this selection,
+      // cached for its next re-check.  Targets are distinct, so no race.
+      s.fit64[m] = d64 ? ft : fp;
+      if (rechecks) atomicAdd(rechecks, 1ull);
+      if (flips && d64 != d32) atomicAdd(flips, 1ull);
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  // copy accepted candidates into the population
+  const int nq = DP >> 2;
+  for (int it = threadIdx.x; it < nrows * nq; it += kThreads) {
+    const int c = it / nq, q = it - c * nq;
+    if (s.flag[c] & 1) {
+      const int m = target ? target[c] : c;
+      reinterpret_cast<float4*>(s.X + m * DP)[q] = reinterpret_cast<const float4*>(s.U + c * DP)[q];
+    }
+  }
+  int acc = 0;
+  for (int c = threadIdx.x; c < nrows; c += kThreads) {
+    if (s.flag[c] & 1) {
+      const int m = target ? target[c] : c;
+      s.fit[m] = s.ftr[c];
+      s.tol[m] = s.ttr[c];
+      if (s.flag[c] == 1) s.fit64[m] = __longlong_as_double(0x7FF8000000000000ll);
+      ++acc;
+    }
+  }
+  __syncthreads();
+  (void)fc;
+  return acc;
+}
+
+// rank[i] = #{j : fit[j] < fit[i] or (fit[j] == fit[i] and j < i)}; writes
+// byrank[rank[i]] = i.
+__device__ void rank_members(const Smem& s, int NP, int* byrank) {
+  for (int i = threadIdx.x; i < NP; i += kThreads) {
+    const float fi = s.fit[i];
+    int r = 0;
+    for (int j = 0; j < NP; ++j) {
+      const float fj = s.fit[j];
+      r += (fj < fi || (fj == fi && j < i)) ? 1 : 0;
+    }
+    byrank[r] = i;
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ int transfer_k(float rate, int NP) {
+  int k = (int)(rate * (float)NP + 0.5f);
+  return k < 1 ? 1 : (k > NP ? NP : k);
+}
+
+__global__ void __launch_bounds__(kThreads) epoch_kernel(const EpochArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int task = a.single_task >= 0 ? a.single_task
+                                      : (a.order ? a.order[blockIdx.x] : (int)blockIdx.x);
+  if (task < 0 || task >= a.n_tasks) {
+    if (threadIdx.x == 0) report(a.err, CHECK_BAD_DESCRIPTOR);
+    return;
+  }
+  const TaskDev td = a.tasks[task];
+  if (!descriptor_ok(td)) {
+    if (threadIdx.x == 0) report(a.err, CHECK_BAD_DESCRIPTOR);
+    return;
+  }
+  const int D = td.D, NP = td.NP;
+  const Layout L = smem_layout(D, NP, td.qt_in_smem != 0);
+  if (L.total > a.smem_bytes) {
+    if (threadIdx.x == 0) report(a.err, CHECK_SMEM_TOO_SMALL);
+    return;
+  }
+  const int DP = L.DP, NPP = L.NPP;
+  Smem s = carve(smem_raw, L);
+  if (!td.qt_in_smem) s.QT = const_cast<float*>(a.qt + td.q_off);
+  FnConst fc;
+  fc.fid = td.fid;
+  fc.D = D;
+  fc.flags = td.flags;
+  fc.woff = td.woff;
+  fc.qnorm = td.qnorm;
+  fc.rel = a.recheck_rel;
+  fc.woff64 = td.woff64;
+
+  // ---- load the task into shared memory ----
+  const float* gq = a.qt + td.q_off;
+  if (td.qt_in_smem)
+    for (int it = threadIdx.x; it < D * (DP >> 2); it += kThreads)
+      reinterpret_cast<float4*>(s.QT)[it] = reinterpret_cast<const float4*>(gq)[it];
+  for (int j = threadIdx.x; j < DP; j += kThreads) s.o[j] = j < D ? a.shift[td.o_off + j] : 0.f;
+  for (int it = threadIdx.x; it < DP * NPP; it += kThreads) s.ST[it] = 0.f;
+  float* gpop = a.pop + td.pop_off;
+  if (a.mode == MODE_INIT) {
+    const float r = fsub(td.hi, td.lo);
+    const int nb = (D + 3) >> 2;
+    for (int it = threadIdx.x; it < NP * nb; it += kThreads) {
+      const int i = it / nb, b = it - i * nb;
+      const U4 w = draw(a.seed, (uint32_t)task, 0u, (uint32_t)i, P_POP_INIT, (uint32_t)b);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int j = 4 * b + q;
+        if (j < D) s.X[i * DP + j] = fminf(ffma(u01(word(w, q)), r, td.lo), td.hi);
+      }
+      if (4 * b + 4 >= DP)
+        for (int j = D; j < DP; ++j) s.X[i * DP + j] = 0.f;
+    }
+  } else {
+    for (int it = threadIdx.x; it < NP * (DP >> 2); it += kThreads)
+      reinterpret_cast<float4*>(s.X)[it] = reinterpret_cast<const float4*>(gpop)[it];
+    for (int i = threadIdx.x; i < NP; i += kThreads) {
+      s.fit[i] = a.fit32[td.fit_off + i];
+      s.tol[i] = a.tol32[td.fit_off + i];
+      s.fit64[i] = a.fit64[td.fit_off + i];
+    }
+  }
+  for (int it = threadIdx.x; it < NP * DP; it += kThreads) s.U[it] = 0.f;
+  __syncthreads();
+
+  unsigned long long* st_re = a.stats ? a.stats + 0 : nullptr;
+  unsigned long long* st_fl = a.stats ? a.stats + 1 : nullptr;
+
+  if (a.mode == MODE_INIT || a.mode == MODE_EVAL) {
+    stage_differences(s, s.X, NP, D, DP, NPP);
+    __syncthreads();
+    evaluate_rows(s, fc, s.X, NP, DP, NPP, s.fit, s.tol);
+    for (int i = threadIdx.x; i < NP; i += kThreads)
+      s.fit64[i] = __longlong_as_double(0x7FF8000000000000ll);
+    if (threadIdx.x == 0) {
+      a.gen[task] = a.mode == MODE_INIT ? 0u : a.gen[task];
+      if (a.stats) atomicAdd(a.stats + 3, (unsigned long long)NP);
+    }
+  } else {
+    const uint32_t gen0 = a.gen[task];
+    // ---- elite transfer in (knowledgeTransfer, SG-EMTF.cu:1514-1591) ----
+    if (a.transfer_import && a.elites_in && a.n_tasks > 1) {
+      const U4 w = draw(a.seed, (uint32_t)task, gen0, 0u, P_TRANSFER_PARTNER, 0);
+      uint32_t p = w.x % (uint32_t)(a.n_tasks - 1);
+      if (p >= (uint32_t)task) ++p;
+      const TaskDev pd = a.tasks[p];
+      if (!descriptor_ok(pd)) {
+        if (threadIdx.x == 0) report(a.err, CHECK_BAD_PARTNER);
+      } else {
+        int* byrank = s.idx;  // NP ints (idx has 4*NP)
+        rank_members(s, NP, byrank);
+        const int kt = transfer_k(a.transfer_rate, NP), kp = transfer_k(a.transfer_rate, pd.NP);
+        const int k = kt < kp ? kt : kp;
+        const float* el = a.elites_in + pd.elite_off;
+        const float rp = fsub(pd.hi, pd.lo), rt = fsub(td.hi, td.lo);
+        for (int it = threadIdx.x; it < k * D; it += kThreads) {
+          const int c = it / D, j = it - c * D;
+          const U4 wm = draw(a.seed, (uint32_t)task, gen0, (uint32_t)c, P_TRANSFER_MIX, (uint32_t)(j >> 2));
+          float v = s.X[byrank[c] * DP + j];
+          if (j < pd.D && u01(word(wm, j & 3)) < a.transfer_mix) {
+            const float r = fdiv(fsub(el[c * pd.DP + j], pd.lo), rp);
+            v = clamp_box(ffma(r, rt, td.lo), td.lo, td.hi);
+          }
+          s.U[c * DP + j] = v;
+        }
+        __syncthreads();
+        stage_differences(s, s.U, k, D, DP, NPP);
+        __syncthreads();
+        evaluate_rows(s, fc, s.U, k, DP, NPP, s.ftr, s.ttr);
+        int* target = s.idx + NP;  // member of rank NP - k + c
+        for (int c = threadIdx.x; c < k; c += kThreads) target[c] = byrank[NP - k + c];
+        __syncthreads();
+        const int acc = select_and_replace(s, a, fc, k, target, true, DP, st_re, st_fl);
+        if (acc && a.stats) atomicAdd(a.stats + 2, (unsigned long long)acc);
+        if (threadIdx.x == 0 && a.stats) atomicAdd(a.stats + 3, (unsigned long long)k);
+      }
+      __syncthreads();
+    }
+    // ---- generations ----
+    for (int g = 0; g < a.gens; ++g) {
+      const uint32_t G = gen0 + (uint32_t)g + 1u;
+      build_trials(s, a, td, task, G, DP, NPP);
+      __syncthreads();
+      evaluate_rows(s, fc, s.U, NP, DP, NPP, s.ftr, s.ttr);
+      select_and_replace(s, a, fc, NP, nullptr, false, DP, st_re, st_fl);
+    }
+    if (threadIdx.x == 0) {
+      a.gen[task] = gen0 + (uint32_t)a.gens;
+      if (a.stats) atomicAdd(a.stats + 3, (unsigned long long)NP * (unsigned long long)a.gens);
+    }
+    // ---- elite export: top-k rows for the next epoch's receivers ----
+    if (a.transfer_export && a.elites_out) {
+      __syncthreads();
+      int* byrank = s.idx;
+      rank_members(s, NP, byrank);
+      const int k = transfer_k(a.transfer_rate, NP);
+      float* el = a.elites_out + td.elite_off;
+      for (int it = threadIdx.x; it < k * DP; it += kThreads) {
+        const int c = it / DP, j = it - c * DP;
+        el[c * DP + j] = s.X[byrank[c] * DP + j];
+      }
+    }
+  }
+  __syncthreads();
+  // ---- write the island back ----
+  for (int it = threadIdx.x; it < NP * (DP >> 2); it += kThreads)
+    reinterpret_cast<float4*>(gpop)[it] = reinterpret_cast<const float4*>(s.X)[it];
+  for (int i = threadIdx.x; i < NP; i += kThreads) {
+    a.fit32[td.fit_off + i] = s.fit[i];
+    a.tol32[td.fit_off + i] = s.tol[i];
+    a.fit64[td.fit_off + i] = s.fit64[i];
+  }
+}
+
+// Evaluates n caller points of one task in chunks of up to 64 rows per CTA
+// (the reference's evaluate kernel, SG-EMTF.cu:1428-1479).
+__global__ void __launch_bounds__(kThreads) eval_kernel(const EvalArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const TaskDev td = a.tasks[a.task];
+  if (!descriptor_ok(td)) {
+    if (threadIdx.x == 0) report(a.err, CHECK_BAD_DESCRIPTOR);
+    return;
+  }
+  const int D = td.D;
+  const int rows = 64;
+  const Layout L = smem_layout(D, rows);
+  if (L.total > a.smem_bytes) {
+    if (threadIdx.x == 0) report(a.err, CHECK_SMEM_TOO_SMALL);
+    return;
+  }
+  const int DP = L.DP, NPP = L.NPP;
+  const Smem s = carve(smem_raw, L);
+  FnConst fc;
+  fc.fid = td.fid;
+  fc.D = D;
+  fc.flags = td.flags;
+  fc.woff = td.woff;
+  fc.qnorm = td.qnorm;
+  fc.rel = 0.f;
+  fc.woff64 = td.woff64;
+  const float* gq = a.qt + td.q_off;
+  for (int it = threadIdx.x; it < D * DP; it += kThreads) s.QT[it] = gq[it];
+  for (int j = threadIdx.x; j < DP; j += kThreads) s.o[j] = j < D ? a.shift[td.o_off + j] : 0.f;
+  for (int it = threadIdx.x; it < DP * NPP; it += kThreads) s.ST[it] = 0.f;
+  const int r0 = blockIdx.x * rows;
+  const int nr = min(rows, a.n - r0);
+  for (int it = threadIdx.x; it < rows * DP; it += kThreads) {
+    const int i = it / DP, j = it - i * DP;
+    s.U[it] = (i < nr && j < D) ? a.x[(size_t)(r0 + i) * D + j] : 0.f;
+  }
+  __syncthreads();
+  stage_differences(s, s.U, nr, D, DP, NPP);
+  __syncthreads();
+  evaluate_rows(s, fc, s.U, nr, DP, NPP, s.ftr, s.ttr);
+  for (int i = threadIdx.x; i < nr; i += kThreads) a.f[r0 + i] = s.ftr[i];
+  if (a.z)
+    for (int it = threadIdx.x; it < nr * D; it += kThreads) {
+      const int i = it / D, j = it - i * D;
+      a.z[(size_t)(r0 + i) * D + j] = s.Z[i * DP + j];
+    }
+}
+
+__global__ void __launch_bounds__(32) best_kernel(const BestArgs a) {
+  __shared__ double zbuf[kMaxDim];
+  const int task = blockIdx.x;
+  if (task >= a.n_tasks) return;
+  const TaskDev td = a.tasks[task];
+  if (!descriptor_ok(td)) return;
+  const int lane = threadIdx.x;
+  float bf = __int_as_float(0x7F800000);
+  int bi = 0x7FFFFFFF;
+  for (int i = lane; i < td.NP; i += 32) {
+    const float f = a.fit32[td.fit_off + i];
+    if (f < bf || (f == bf && i < bi)) { bf = f; bi = i; }
+  }
+#pragma unroll
+  for (int m = 16; m > 0; m >>= 1) {
+    const float of = __shfl_xor_sync(0xFFFFFFFFu, bf, m);
+    const int oi = __shfl_xor_sync(0xFFFFFFFFu, bi, m);
+    if (of < bf || (of == bf && oi < bi)) { bf = of; bi = oi; }
+  }
+  if (bi < 0 || bi >= td.NP) bi = 0;
+  double f64 = a.fit64[td.fit_off + bi];
+  if (isnan(f64)) {
+    FnConst fc;
+    fc.fid = td.fid;
+    fc.D = td.D;
+    fc.flags = td.flags;
+    fc.woff = td.woff;
+    fc.qnorm = td.qnorm;
+    fc.rel = 0.f;
+    fc.woff64 = td.woff64;
+    f64 = eval_row_f64(fc, a.pop + td.pop_off + (size_t)bi * td.DP, a.shift + td.o_off,
+                       a.qt + td.q_off, td.DP, zbuf);
+  }
+  if (lane == 0) {
+    a.best_idx[task] = bi;
+    a.best_f32[task] = bf;
+    a.best_f64[task] = f64;
+  }
+}
+
+}  // namespace emt
+
+int emt_launch_best(const emt::BestArgs& a, void* stream) {
+  if (a.n_tasks <= 0) return 0;
+  emt::best_kernel<<<a.n_tasks, 32, 0, (cudaStream_t)stream>>>(a);
+  return (int)cudaGetLastError();
+}
+
+int emt_launch_epoch(const emt::EpochArgs& a, int grid, void* stream) {
+  if (grid <= 0) return 0;
+  static_assert(sizeof(emt::EpochArgs) < 4096, "kernel parameter block");
+  cudaError_t e = cudaFuncSetAttribute(emt::epoch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)a.smem_bytes);
+  if (e != cudaSuccess) return (int)e;
+  emt::epoch_kernel<<<grid, emt::kThreads, a.smem_bytes, (cudaStream_t)stream>>>(a);
+  return (int)cudaGetLastError();
+}
+
+int emt_launch_eval(const emt::EvalArgs& a, void* stream) {
+  const int grid = (a.n + 63) / 64;
+  if (grid <= 0) return 0;
+  cudaError_t e = cudaFuncSetAttribute(emt::eval_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)a.smem_bytes);
+  if (e != cudaSuccess) return (int)e;
+  emt::eval_kernel<<<grid, emt::kThreads, a.smem_bytes, (cudaStream_t)stream>>>(a);
+  return (int)cudaGetLastError();
+}

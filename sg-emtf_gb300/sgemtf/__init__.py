@@ -1,0 +1,273 @@
+"""Python binding of the engine's C ABI (include/sgemtf.h).
+
+A thin ctypes layer over sg-emtf_gb300/_build/libsgemtf.so: every call goes
+straight to the CUDA library.  There is no Python or CPU implementation of
+the engine behind it; if the library is missing, importing `lib()` raises.
+
+    eng = Engine(Config(seed=1))
+    eng.add_tasks([TaskDesc(function=SPHERE, dim=50, pop=64, rotation=ROTATION_SEEDED_QR)])
+    eng.run(2000)
+    f, x = eng.best(0)
+"""
+import ctypes
+import os
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG_DIR, "_build", "libsgemtf.so")
+
+# ---- enums (include/sgemtf.h) ----
+OK, ERR_INVALID_ARG, ERR_OUT_OF_MEMORY, ERR_CUDA, ERR_DEVICE_TIMEOUT, ERR_STATE, \
+    ERR_UNSUPPORTED, ERR_DEVICE_CHECK = range(8)
+DE_RAND1_BIN, DE_CURRENT1_BIN, GA_SBX_PM = range(3)
+ROT_FP32, ROT_TF32X3, ROT_AUTO = range(3)
+SPHERE, RASTRIGIN, ACKLEY, GRIEWANK, ROSENBROCK, SCHWEFEL, WEIERSTRASS = range(7)
+FUNCTION_NAMES = ["sphere", "rastrigin", "ackley", "griewank", "rosenbrock", "schwefel",
+                  "weierstrass"]
+ROTATION_IDENTITY, ROTATION_SEEDED_QR, ROTATION_DENSE, ROTATION_DIAG = range(4)
+FLAG_REF_GRIEWANK_NO_PRODUCT = 0x1
+FLAG_REF_WEIERSTRASS_CONST = 0x2
+FLAG_REF_ACKLEY_E = 0x4
+FLAG_REF_BOXES = 0x8
+FLAG_NO_RECHECK = 0x10
+MAX_DIM, MAX_POP = 128, 256
+
+EXPORTED = [
+    "emt_config_default", "emt_function_from_reference", "emt_function_box", "emt_create",
+    "emt_add_tasks", "emt_reset", "emt_run", "emt_sync", "emt_get_best", "emt_get_best_all",
+    "emt_get_population", "emt_set_population", "emt_get_task_params", "emt_evaluate",
+    "emt_get_stats", "emt_snapshot_size", "emt_snapshot", "emt_restore", "emt_last_error",
+    "emt_status_string", "emt_destroy",
+]
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("algorithm", ctypes.c_int32), ("precision", ctypes.c_int32),
+                ("F", ctypes.c_float), ("CR", ctypes.c_float), ("eta_c", ctypes.c_float),
+                ("p_c", ctypes.c_float), ("eta_m", ctypes.c_float), ("p_m", ctypes.c_float),
+                ("transfer_interval", ctypes.c_int32), ("transfer_rate", ctypes.c_float),
+                ("transfer_mix", ctypes.c_float), ("flags", ctypes.c_uint32),
+                ("seed", ctypes.c_uint64), ("recheck_rel", ctypes.c_double),
+                ("device", ctypes.c_int32), ("reserved", ctypes.c_int32 * 7)]
+
+    def __init__(self, **kw):
+        super().__init__()
+        lib().emt_config_default(ctypes.byref(self))
+        for k, v in kw.items():
+            if not hasattr(self, k):
+                raise AttributeError(k)
+            setattr(self, k, v)
+
+
+class TaskDescC(ctypes.Structure):
+    _fields_ = [("function", ctypes.c_int32), ("dim", ctypes.c_int32), ("pop", ctypes.c_int32),
+                ("lo", ctypes.c_float), ("hi", ctypes.c_float), ("rotation", ctypes.c_int32),
+                ("rotation_matrix", ctypes.POINTER(ctypes.c_double)),
+                ("diag", ctypes.POINTER(ctypes.c_float)),
+                ("shift", ctypes.POINTER(ctypes.c_float))]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("evaluations", ctypes.c_uint64), ("generations", ctypes.c_uint64),
+                ("rechecks", ctypes.c_uint64), ("recheck_flips", ctypes.c_uint64),
+                ("transfers_accepted", ctypes.c_uint64), ("device_ms", ctypes.c_double),
+                ("n_tasks", ctypes.c_int32), ("precision_used", ctypes.c_int32)]
+
+
+class TaskDesc:
+    """One task; arrays are kept alive here until add_tasks copies them."""
+
+    def __init__(self, function, dim, pop, lo=0.0, hi=0.0, rotation=ROTATION_SEEDED_QR,
+                 rotation_matrix=None, diag=None, shift=None):
+        self.function, self.dim, self.pop = int(function), int(dim), int(pop)
+        self.lo, self.hi, self.rotation = float(lo), float(hi), int(rotation)
+        self.rotation_matrix = None if rotation_matrix is None else np.ascontiguousarray(
+            rotation_matrix, np.float64)
+        self.diag = None if diag is None else np.ascontiguousarray(diag, np.float32)
+        self.shift = None if shift is None else np.ascontiguousarray(shift, np.float32)
+
+    def c(self):
+        def ptr(a, t):
+            return None if a is None else a.ctypes.data_as(ctypes.POINTER(t))
+        return TaskDescC(self.function, self.dim, self.pop, self.lo, self.hi, self.rotation,
+                         ptr(self.rotation_matrix, ctypes.c_double), ptr(self.diag, ctypes.c_float),
+                         ptr(self.shift, ctypes.c_float))
+
+
+class EngineError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("%s (%d): %s" % (status_string(status), status, message))
+        self.status = status
+
+
+_lib = None
+
+
+def lib():
+    """The loaded CUDA library.  Raises if it was not built: there is no
+    fallback implementation."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libsgemtf.so not built: run `python sg-emtf_gb300/build.py` "
+                               "(or __graft_entry__.build())")
+        L = ctypes.CDLL(LIB_PATH)
+        vp = ctypes.c_void_p
+        i32 = ctypes.c_int32
+        f32p = ctypes.POINTER(ctypes.c_float)
+        L.emt_config_default.argtypes = [ctypes.POINTER(Config)]
+        L.emt_config_default.restype = None
+        L.emt_function_from_reference.argtypes = [i32]
+        L.emt_function_from_reference.restype = i32
+        L.emt_function_box.argtypes = [i32, i32, f32p, f32p]
+        L.emt_create.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(vp)]
+        L.emt_add_tasks.argtypes = [vp, i32, ctypes.POINTER(TaskDescC)]
+        L.emt_reset.argtypes = [vp, vp]
+        L.emt_run.argtypes = [vp, i32, vp]
+        L.emt_sync.argtypes = [vp]
+        L.emt_get_best.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_double), f32p]
+        L.emt_get_best_all.argtypes = [vp, f32p]
+        L.emt_get_population.argtypes = [vp, i32, f32p, f32p]
+        L.emt_set_population.argtypes = [vp, i32, f32p]
+        L.emt_get_task_params.argtypes = [vp, i32, f32p, f32p]
+        L.emt_evaluate.argtypes = [vp, i32, i32, f32p, f32p, f32p]
+        L.emt_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
+        L.emt_snapshot_size.argtypes = [vp, ctypes.POINTER(ctypes.c_size_t)]
+        L.emt_snapshot.argtypes = [vp, vp, ctypes.c_size_t]
+        L.emt_restore.argtypes = [vp, vp, ctypes.c_size_t]
+        L.emt_last_error.argtypes = [vp]
+        L.emt_last_error.restype = ctypes.c_char_p
+        L.emt_status_string.argtypes = [ctypes.c_int]
+        L.emt_status_string.restype = ctypes.c_char_p
+        L.emt_destroy.argtypes = [vp]
+        L.emt_destroy.restype = None
+        _lib = L
+    return _lib
+
+
+def status_string(s):
+    return lib().emt_status_string(s).decode()
+
+
+def function_box(fid, reference_boxes=False):
+    lo, hi = ctypes.c_float(), ctypes.c_float()
+    rc = lib().emt_function_box(fid, int(reference_boxes), ctypes.byref(lo), ctypes.byref(hi))
+    if rc:
+        raise EngineError(rc, "function_box")
+    return lo.value, hi.value
+
+
+def _f32(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+class Engine:
+    """One emt_handle: a set of tasks resident on one GPU."""
+
+    def __init__(self, config=None, **kw):
+        self.config = config if config is not None else Config(**kw)
+        self._h = ctypes.c_void_p()
+        rc = lib().emt_create(ctypes.byref(self.config), ctypes.byref(self._h))
+        if rc:
+            raise EngineError(rc, "emt_create")
+        self.tasks = []
+
+    def _check(self, rc, what):
+        if rc:
+            raise EngineError(rc, "%s: %s" % (what, lib().emt_last_error(self._h).decode()))
+
+    def add_tasks(self, descs):
+        descs = list(descs)
+        arr = (TaskDescC * len(descs))(*[d.c() for d in descs])
+        self._check(lib().emt_add_tasks(self._h, len(descs), arr), "emt_add_tasks")
+        self.tasks.extend(descs)
+
+    def reset(self, stream=None):
+        self._check(lib().emt_reset(self._h, stream), "emt_reset")
+
+    def run(self, generations, stream=None, sync=True):
+        self._check(lib().emt_run(self._h, int(generations), stream), "emt_run")
+        if sync:
+            self.sync()
+
+    def sync(self):
+        self._check(lib().emt_sync(self._h), "emt_sync")
+
+    def _dim(self, task):
+        if 0 <= task < len(self.tasks):
+            return self.tasks[task].dim, self.tasks[task].pop
+        return 1, 1  # the library reports the bad index
+
+    def best(self, task):
+        x = np.zeros(self._dim(task)[0], np.float32)
+        f = ctypes.c_double()
+        self._check(lib().emt_get_best(self._h, task, ctypes.byref(f), _f32(x)), "emt_get_best")
+        return f.value, x
+
+    def best_all(self):
+        out = np.zeros(len(self.tasks), np.float32)
+        self._check(lib().emt_get_best_all(self._h, _f32(out)), "emt_get_best_all")
+        return out
+
+    def population(self, task):
+        D, NP = self._dim(task)
+        x = np.zeros((NP, D), np.float32)
+        f = np.zeros(NP, np.float32)
+        self._check(lib().emt_get_population(self._h, task, _f32(x), _f32(f)),
+                    "emt_get_population")
+        return x, f
+
+    def set_population(self, task, x):
+        x = np.ascontiguousarray(x, np.float32)
+        self._check(lib().emt_set_population(self._h, task, _f32(x)), "emt_set_population")
+
+    def task_params(self, task):
+        D, _ = self._dim(task)
+        Q = np.zeros((D, D), np.float32)
+        o = np.zeros(D, np.float32)
+        self._check(lib().emt_get_task_params(self._h, task, _f32(Q), _f32(o)),
+                    "emt_get_task_params")
+        return Q, o
+
+    def evaluate(self, task, x, want_z=False):
+        x = np.ascontiguousarray(np.atleast_2d(x), np.float32)
+        n = x.shape[0]
+        f = np.zeros(n, np.float32)
+        z = np.zeros_like(x) if want_z else None
+        self._check(lib().emt_evaluate(self._h, task, n, _f32(x), _f32(f),
+                                       _f32(z) if want_z else None), "emt_evaluate")
+        return (f, z) if want_z else f
+
+    def stats(self):
+        s = Stats()
+        self._check(lib().emt_get_stats(self._h, ctypes.byref(s)), "emt_get_stats")
+        return {k: getattr(s, k) for k, _ in Stats._fields_}
+
+    def snapshot(self):
+        n = ctypes.c_size_t()
+        self._check(lib().emt_snapshot_size(self._h, ctypes.byref(n)), "emt_snapshot_size")
+        buf = ctypes.create_string_buffer(n.value)
+        self._check(lib().emt_snapshot(self._h, buf, n.value), "emt_snapshot")
+        return buf.raw
+
+    def restore(self, blob):
+        buf = ctypes.create_string_buffer(blob, len(blob))
+        self._check(lib().emt_restore(self._h, buf, len(blob)), "emt_restore")
+
+    def close(self):
+        if self._h:
+            lib().emt_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

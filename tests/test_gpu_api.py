@@ -1,0 +1,102 @@
+"""Behaviour of the C ABI on the device: checkpoints, determinism, errors."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from gpu_util import make_engine
+
+pytestmark = pytest.mark.gpu
+
+
+def test_same_seed_same_run(sgemtf, orc):
+    specs = [(f, 30, 40, 1) for f in range(7)]
+    a, _ = make_engine(sgemtf, orc, specs, seed=8)
+    b, _ = make_engine(sgemtf, orc, specs, seed=8)
+    c, _ = make_engine(sgemtf, orc, specs, seed=9)
+    for e in (a, b, c):
+        e.run(40)
+    for i in range(7):
+        assert np.array_equal(a.population(i)[0], b.population(i)[0])
+    assert not all(np.array_equal(a.population(i)[0], c.population(i)[0]) for i in range(7))
+
+
+def test_snapshot_restore_continues_bit_exact(sgemtf, orc):
+    specs = [(f, 16, 24, 1) for f in range(7)]
+    a, _ = make_engine(sgemtf, orc, specs, seed=4, transfer_interval=5)
+    a.run(12)
+    blob = a.snapshot()
+    a.run(13)
+    b, _ = make_engine(sgemtf, orc, specs, seed=4, transfer_interval=5)
+    b.restore(blob)
+    b.run(13)
+    for i in range(7):
+        assert np.array_equal(a.population(i)[0], b.population(i)[0])
+
+
+def test_best_is_population_minimum(sgemtf, orc):
+    specs = [(f, 10, 20, 1) for f in range(7)]
+    eng, tasks = make_engine(sgemtf, orc, specs, seed=6)
+    eng.run(20)
+    allbest = eng.best_all()
+    for i, t in enumerate(tasks):
+        X, f = eng.population(i)
+        fb, xb = eng.best(i)
+        assert allbest[i] == f.min()
+        assert np.array_equal(xb, X[int(np.argmin(f))])
+        assert abs(fb - t.eval64(xb)[0]) <= 1e-9 * max(1.0, abs(fb)) + (1e-5 if t.c.fid == 6 else 0)
+
+
+def test_set_population_evaluates(sgemtf, orc):
+    eng, (t,) = make_engine(sgemtf, orc, [(2, 12, 8, 1)], seed=1)
+    eng.reset()
+    X = np.random.default_rng(0).uniform(t.c.lo, t.c.hi, (8, 12)).astype(np.float32)
+    eng.set_population(0, X)
+    Xg, f = eng.population(0)
+    assert np.array_equal(Xg, X)
+    assert np.array_equal(f, eng.evaluate(0, X))
+
+
+def test_stats_count_evaluations(sgemtf, orc):
+    specs = [(0, 8, 10, 1), (1, 8, 12, 1)]
+    eng, _ = make_engine(sgemtf, orc, specs, seed=1)
+    eng.run(7)
+    s = eng.stats()
+    assert s["evaluations"] == (10 + 12) * (1 + 7)
+    assert s["generations"] == 2 * 7
+
+
+def test_invalid_arguments(sgemtf):
+    eng = sgemtf.Engine(sgemtf.Config(seed=1))
+    with pytest.raises(sgemtf.EngineError) as e:
+        eng.run(1)
+    assert e.value.status == sgemtf.ERR_STATE
+    for bad in [dict(function=9, dim=4, pop=8), dict(function=0, dim=0, pop=8),
+                dict(function=0, dim=129, pop=8), dict(function=0, dim=4, pop=3),
+                dict(function=0, dim=4, pop=257)]:
+        with pytest.raises(sgemtf.EngineError) as e:
+            eng.add_tasks([sgemtf.TaskDesc(**bad)])
+        assert e.value.status == sgemtf.ERR_INVALID_ARG
+    with pytest.raises(sgemtf.EngineError) as e:
+        eng.add_tasks([sgemtf.TaskDesc(0, 4, 8, rotation=sgemtf.ROTATION_DENSE)])
+    assert e.value.status == sgemtf.ERR_INVALID_ARG
+    eng.add_tasks([sgemtf.TaskDesc(0, 4, 8)])
+    with pytest.raises(sgemtf.EngineError) as e:
+        eng.run(-1)
+    assert e.value.status == sgemtf.ERR_INVALID_ARG
+    with pytest.raises(sgemtf.EngineError):
+        eng.best(5)
+    with pytest.raises(sgemtf.EngineError) as e:
+        eng.set_population(0, np.full((8, 4), 1e9, np.float32))
+    assert e.value.status == sgemtf.ERR_INVALID_ARG
+    with pytest.raises(sgemtf.EngineError):
+        eng.restore(b"\0" * 64)
+
+
+def test_empty_evaluate_and_zero_generations(sgemtf, orc):
+    eng, _ = make_engine(sgemtf, orc, [(0, 4, 8, 1)], seed=1)
+    assert eng.evaluate(0, np.zeros((0, 4), np.float32)).shape == (0,)
+    eng.run(0)
+    X0 = eng.population(0)[0]
+    eng.run(0)
+    assert np.array_equal(eng.population(0)[0], X0)
