@@ -6,6 +6,7 @@
 // over 8 shared streams, and the pthread/cudaEvent hand-shake for transfers
 // (:1678-1722).  Here every task advances in the same launch; transfers are
 // epoch boundaries between launches, so no host thread waits on another.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -80,6 +81,11 @@ struct emt_handle {
   DevBuf<uint32_t> d_gen;
   DevBuf<unsigned long long> d_stats;
   DevBuf<int32_t> d_err, d_best_idx;
+  // tensor-core form: Q hi/lo tiles [task][2][Np][Kp] and their TMA map
+  bool use_tc = false;
+  int tc_np = 0, tc_kp = 0;
+  DevBuf<float> d_qtc;
+  CUtensorMap tmap;
 
   int fail(int code, const std::string& msg) {
     err = msg;
@@ -175,6 +181,63 @@ int max_smem_optin(int device) {
   return v;
 }
 
+// TF32 hi part of x, round to nearest with ties away from zero on the
+// magnitude (what cvt.rna.tf32.f32 computes); lo = x - hi is exact in FP32.
+float tf32_hi(float x) {
+  uint32_t b;
+  std::memcpy(&b, &x, 4);
+  b = (b + 0x1000u) & 0xFFFFE000u;
+  float r;
+  std::memcpy(&r, &b, 4);
+  return r;
+}
+
+bool device_has_tcgen05(int device) {
+  int major = 0;
+  if (cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device) != cudaSuccess)
+    return false;
+  return major == 10;
+}
+
+// Whether every island fits the tensor-core form (NP <= 128, one 128-row MMA
+// tile; operands and state within the shared-memory limit).
+bool tc_fits(const std::vector<HostTask>& tasks, int& np, int& kp) {
+  int dmax = 1;
+  for (const auto& t : tasks) dmax = std::max(dmax, t.D);
+  np = emt::round16(dmax);
+  kp = emt::round32(dmax);
+  for (const auto& t : tasks)
+    if (t.NP > 128 || emt::tc_layout(t.D, t.NP, np, kp).total > emt::kSmemLimit) return false;
+  return true;
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// Tensor map over the Q tiles: dims (Kp, Np, 2 * tasks) FP32, box (32, Np, 1),
+// 128-byte swizzle, i.e. one K-major B tile of one task per TMA load.
+int encode_qtc_map(emt_handle* h) {
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                                   cudaEnableDefault, &q);
+  if (e != cudaSuccess || !fn || q != cudaDriverEntryPointSuccess)
+    return h->fail(EMT_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  const cuuint64_t dims[3] = {(cuuint64_t)h->tc_kp, (cuuint64_t)h->tc_np,
+                              (cuuint64_t)(2 * h->tasks.size())};
+  const cuuint64_t strides[2] = {(cuuint64_t)h->tc_kp * 4, (cuuint64_t)h->tc_kp * h->tc_np * 4};
+  const cuuint32_t box[3] = {32, (cuuint32_t)h->tc_np, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = ((EncodeTiledFn)fn)(&h->tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, h->d_qtc.p, dims,
+                                   strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                   CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return h->fail(EMT_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+  return EMT_OK;
+}
+
 int upload(emt_handle* h) {
   if (h->uploaded) return EMT_OK;
   const int n = (int)h->tasks.size();
@@ -209,6 +272,21 @@ int upload(emt_handle* h) {
     d.qt_in_smem = emt::smem_layout(ht.D, ht.NP, true).total <= emt::kSmemLimit ? 1 : 0;
     d.pad_ = 0;
     smem = std::max(smem, emt::smem_layout(ht.D, ht.NP, d.qt_in_smem != 0).total);
+  }
+  h->use_tc = false;
+  if (h->cfg.precision != EMT_ROT_FP32) {
+    int np = 0, kp = 0;
+    const bool ok = device_has_tcgen05(h->device) && tc_fits(h->tasks, np, kp);
+    if (!ok && h->cfg.precision == EMT_ROT_TF32X3)
+      return h->fail(EMT_ERR_UNSUPPORTED, "tensor-core form needs an sm_10x device and islands "
+                                          "with NP <= 128 whose tiles fit in shared memory");
+    if (ok) {
+      h->use_tc = true;
+      h->tc_np = np;
+      h->tc_kp = kp;
+      smem = 0;
+      for (const auto& t : h->tasks) smem = std::max(smem, emt::tc_layout(t.D, t.NP, np, kp).total);
+    }
   }
   h->smem_bytes = smem;
   // longest-first order: the hardware hands CTAs to free SM slots in block
@@ -259,6 +337,27 @@ int upload(emt_handle* h) {
       (e = cudaMemset(h->d_stats.p, 0, sizeof(unsigned long long) * 4)) ||
       (e = cudaMemset(h->d_err.p, 0, sizeof(int32_t))))
     return h->cuda_fail(e, "upload");
+  if (h->use_tc) {
+    const size_t per = (size_t)2 * h->tc_np * h->tc_kp;
+    std::vector<float> hqc(per * n, 0.f);
+    for (int t = 0; t < n; ++t) {
+      const HostTask& ht = h->tasks[t];
+      float* hi = hqc.data() + per * t;
+      float* lo = hi + (size_t)h->tc_np * h->tc_kp;
+      for (int r = 0; r < ht.D; ++r)
+        for (int c = 0; c < ht.D; ++c) {
+          const float v = ht.Q[(size_t)r * ht.D + c];
+          const float vh = tf32_hi(v);
+          hi[(size_t)r * h->tc_kp + c] = vh;
+          lo[(size_t)r * h->tc_kp + c] = v - vh;
+        }
+    }
+    if ((e = h->d_qtc.ensure(hqc.size())) != cudaSuccess) return h->cuda_fail(e, "cudaMalloc");
+    if ((e = cudaMemcpy(h->d_qtc.p, hqc.data(), sizeof(float) * hqc.size(), cudaMemcpyHostToDevice)))
+      return h->cuda_fail(e, "upload");
+    int rc = encode_qtc_map(h);
+    if (rc) return rc;
+  }
   h->uploaded = true;
   h->initialized = false;
   return EMT_OK;
@@ -296,7 +395,13 @@ emt::EpochArgs base_args(emt_handle* h, int mode) {
   a.stats = h->d_stats.p;
   a.err = h->d_err.p;
   a.smem_bytes = h->smem_bytes;
+  a.tc_np = h->tc_np;
+  a.tc_kp = h->tc_kp;
   return a;
+}
+
+int launch_epoch(emt_handle* h, const emt::EpochArgs& a, int grid, void* stream) {
+  return emt_launch_epoch(a, grid, stream, h->use_tc ? (const void*)&h->tmap : nullptr);
 }
 
 int check_task(const emt_handle* h, int32_t task) {
@@ -372,11 +477,9 @@ int emt_create(const emt_config* cfg, emt_handle_t** out) {
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return EMT_ERR_CUDA;
   if (cfg->device < 0 || cfg->device >= ndev) return EMT_ERR_INVALID_ARG;
-  if (cfg->precision == EMT_ROT_TF32X3) return EMT_ERR_UNSUPPORTED;
   emt_handle* h = new (std::nothrow) emt_handle();
   if (!h) return EMT_ERR_OUT_OF_MEMORY;
   h->cfg = *cfg;
-  if (h->cfg.precision == EMT_ROT_AUTO) h->cfg.precision = EMT_ROT_FP32;
   h->device = cfg->device;
   if (cudaSetDevice(h->device) != cudaSuccess || cudaEventCreate(&h->ev0) != cudaSuccess ||
       cudaEventCreate(&h->ev1) != cudaSuccess) {
@@ -477,7 +580,7 @@ int emt_reset(emt_handle_t* h, void* stream) {
   if (rc) return rc;
   h->stream = (cudaStream_t)stream;
   emt::EpochArgs a = base_args(h, emt::MODE_INIT);
-  int e = emt_launch_epoch(a, (int)h->tasks.size(), stream);
+  int e = launch_epoch(h, a, (int)h->tasks.size(), stream);
   if (e) return h->cuda_fail((cudaError_t)e, "init launch");
   h->initialized = true;
   h->gdone = 0;
@@ -514,7 +617,7 @@ int emt_run(emt_handle_t* h, int32_t generations, void* stream) {
       a.elites_in = h->d_elites[h->elite_parity ^ 1].p;
       a.elites_out = h->d_elites[h->elite_parity].p;
     }
-    int e = emt_launch_epoch(a, n, stream);
+    int e = launch_epoch(h, a, n, stream);
     if (e) return h->cuda_fail((cudaError_t)e, "epoch launch");
     if (interval && do_export) h->elite_parity ^= 1;
     h->gdone += (uint32_t)g;
@@ -628,7 +731,7 @@ int emt_set_population(emt_handle_t* h, int32_t task, const float* x) {
   if (e != cudaSuccess) return h->cuda_fail(e, "copy population");
   emt::EpochArgs a = base_args(h, emt::MODE_EVAL);
   a.single_task = task;
-  int le = emt_launch_epoch(a, 1, h->stream);
+  int le = launch_epoch(h, a, 1, h->stream);
   if (le) return h->cuda_fail((cudaError_t)le, "evaluate launch");
   return emt_sync(h);
 }
@@ -687,7 +790,7 @@ int emt_get_stats(emt_handle_t* h, emt_stats* out) {
   if (!h || !out) return EMT_ERR_INVALID_ARG;
   std::memset(out, 0, sizeof(*out));
   out->n_tasks = (int32_t)h->tasks.size();
-  out->precision_used = EMT_ROT_FP32;
+  out->precision_used = h->use_tc ? EMT_ROT_TF32X3 : EMT_ROT_FP32;
   if (h->d_stats.p) {
     int rc = emt_sync(h);
     if (rc) return rc;
@@ -801,6 +904,7 @@ void emt_destroy(emt_handle_t* h) {
   h->d_stats.release();
   h->d_err.release();
   h->d_best_idx.release();
+  h->d_qtc.release();
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   delete h;

@@ -66,6 +66,7 @@ struct EpochArgs {
   unsigned long long* stats;  // [0] rechecks [1] flips [2] transfers [3] evaluations
   int32_t* err;               // first kernel-side check that fired (0 = none)
   size_t smem_bytes;          // dynamic shared memory the launch provides
+  int32_t tc_np, tc_kp;       // tensor-core form: padded N and K of the B tiles
 };
 
 // Arguments of the standalone evaluation kernel (emt_evaluate).
@@ -118,12 +119,59 @@ EMT_HD Layout smem_layout(int D, int NP, bool qt_in_smem = true) {
   return L;
 }
 
+// Shared-memory carve-up of the tensor-core form.  The operand tiles come
+// first (1024-byte aligned): A = 2 (hi/lo) x nkb tiles of MA rows x 128 B,
+// B = 2 x nkb tiles of Np rows x 128 B.  With NP <= 64 the A tiles hold 64
+// rows and an M = 128 MMA reads the next 64 rows past each tile (finite data
+// whose output rows are ignored), so B (or slack) must follow A.  The FP32
+// rotated rows Z alias the A region once the MMAs have completed.
+struct TcLayout {
+  int DP, Np, Kp, nkb, MA;
+  size_t A, B, fit64, z64, X, U, o, fit, tol, ftr, ttr, idx, flag, list, misc, bars, total;
+};
+
+EMT_HD TcLayout tc_layout(int D, int NP, int Np, int Kp) {
+  TcLayout L;
+  L.DP = round4(D);
+  L.Np = Np;
+  L.Kp = Kp;
+  L.nkb = Kp / 32;
+  L.MA = NP <= 64 ? 64 : 128;
+  size_t off = 0;
+  L.A = off;
+  off += (size_t)2 * L.nkb * L.MA * 128;
+  L.B = off;
+  const size_t bsz = (size_t)2 * L.nkb * Np * 128, slack = (size_t)(128 - L.MA) * 128;
+  off += bsz > slack ? bsz : slack;
+  L.fit64 = off; off = align16(off + sizeof(double) * NP);
+  L.z64 = off;   off = align16(off + sizeof(double) * kWarps * L.DP);
+  L.X = off;     off = align16(off + sizeof(float) * NP * L.DP);
+  L.U = off;     off = align16(off + sizeof(float) * NP * L.DP);
+  L.o = off;     off = align16(off + sizeof(float) * L.DP);
+  L.fit = off;   off = align16(off + sizeof(float) * NP);
+  L.tol = off;   off = align16(off + sizeof(float) * NP);
+  L.ftr = off;   off = align16(off + sizeof(float) * NP);
+  L.ttr = off;   off = align16(off + sizeof(float) * NP);
+  L.idx = off;   off = align16(off + sizeof(int) * 4 * NP);
+  L.flag = off;  off = align16(off + sizeof(int) * NP);
+  L.list = off;  off = align16(off + sizeof(int) * NP);
+  L.misc = off;  off = align16(off + sizeof(int) * 8);
+  L.bars = off;  off = align16(off + 32);
+  L.total = off + 1024;  // the kernel aligns its base to 1024 bytes
+  return L;
+}
+
+EMT_HD int round16(int v) { return (v + 15) & ~15; }
+EMT_HD int round32(int v) { return (v + 31) & ~31; }
+
 // Error codes written to EpochArgs::err by the kernels' own checks.
 enum DeviceCheck : int32_t {
   CHECK_OK = 0,
   CHECK_BAD_DESCRIPTOR = 1,
   CHECK_SMEM_TOO_SMALL = 2,
-  CHECK_BAD_PARTNER = 3
+  CHECK_BAD_PARTNER = 3,
+  CHECK_TIMEOUT = 4,      // a bounded mbarrier wait gave up
+  CHECK_TC_SHAPE = 5      // island outside the tensor-core form's limits
 };
 
 // Arguments of the best-member kernel (popSort + messageTransfer,
@@ -144,7 +192,8 @@ struct BestArgs {
 
 }  // namespace emt
 
-// Kernel launchers (emt_kernels.cu).
-int emt_launch_epoch(const emt::EpochArgs& a, int grid, void* stream);
+// Kernel launchers (emt_kernels.cu).  tmap: the CUtensorMap of the B
+// operand tiles (tensor-core form), or null for the FP32 form.
+int emt_launch_epoch(const emt::EpochArgs& a, int grid, void* stream, const void* tmap = nullptr);
 int emt_launch_eval(const emt::EvalArgs& a, void* stream);
 int emt_launch_best(const emt::BestArgs& a, void* stream);

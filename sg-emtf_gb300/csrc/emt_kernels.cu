@@ -12,14 +12,21 @@
 //   1. trial vectors: DE/rand/1/bin, DE/current/1/bin or SBX + polynomial
 //      mutation, from the counter-based Philox stream (bit-exact with the
 //      host replay);
-//   2. rotation Z = (U - o) Q^T: 4x4 register tiles, float4 operand loads;
+//   2. rotation Z = (U - o) Q^T, in one of two forms:
+//      FP32: 4x4 register tiles on CUDA cores, float4 operand loads;
+//      TC:   tcgen05 MMA, kind::tf32, with hi/lo split operands (3 products,
+//            FP32 accumulation in tensor memory); the trial builder writes the
+//            split A operand into 128B-swizzled shared memory tiles, the Q
+//            tiles arrive by TMA once per epoch;
 //   3. function epilogue: one warp per trial, FP32 value + error scale;
 //   4. selection (ties go to the trial, SG-EMTF_DE.cu:679-706): a trial whose
 //      FP32 fitness lies within the rounding window of its parent's is
 //      re-decided in FP64 so that selections do not depend on FP32 rounding.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "emt_functions.cuh"
+#include "emt_tc.cuh"
 
 namespace emt {
 
@@ -27,7 +34,42 @@ struct Smem {
   double *fit64, *z64;
   float *X, *U, *ST, *Z, *QT, *o, *fit, *tol, *ftr, *ttr;
   int *idx, *flag, *list, *misc;
+  // tensor-core form
+  unsigned char *A, *B;
+  uint32_t a_saddr, b_saddr, mma_bar, tma_bar, tmem;
+  int MA, nkb, Np, N, ksteps;
+  uint32_t idesc;
 };
+
+__device__ __forceinline__ Smem carve_tc(unsigned char* base, const TcLayout& L) {
+  Smem s;
+  s.A = base + L.A;
+  s.B = base + L.B;
+  s.fit64 = (double*)(base + L.fit64);
+  s.z64 = (double*)(base + L.z64);
+  s.X = (float*)(base + L.X);
+  s.U = (float*)(base + L.U);
+  s.ST = nullptr;
+  s.Z = (float*)(base + L.A);  // rotated rows alias the A operand after the MMAs
+  s.QT = nullptr;
+  s.o = (float*)(base + L.o);
+  s.fit = (float*)(base + L.fit);
+  s.tol = (float*)(base + L.tol);
+  s.ftr = (float*)(base + L.ftr);
+  s.ttr = (float*)(base + L.ttr);
+  s.idx = (int*)(base + L.idx);
+  s.flag = (int*)(base + L.flag);
+  s.list = (int*)(base + L.list);
+  s.misc = (int*)(base + L.misc);
+  s.a_saddr = tc::smem_addr(s.A);
+  s.b_saddr = tc::smem_addr(s.B);
+  s.mma_bar = tc::smem_addr(base + L.bars);
+  s.tma_bar = s.mma_bar + 8;
+  s.MA = L.MA;
+  s.nkb = L.nkb;
+  s.Np = L.Np;
+  return s;
+}
 
 __device__ __forceinline__ Smem carve(unsigned char* base, const Layout& L) {
   Smem s;
@@ -95,12 +137,89 @@ __device__ void rotate_f32(const Smem& s, int D, int DP, int NPP, int nrows) {
   }
 }
 
-// Evaluates rows [0, nrows) of `rows` (shared memory, stride DP) whose
-// differences rows - o are already in ST: rotation, then one warp per row.
-__device__ void evaluate_rows(const Smem& s, const FnConst& fc, const float* rows, int nrows,
-                              int DP, int NPP, float* fout, float* tout) {
-  rotate_f32(s, fc.D, DP, NPP, nrows);
+// Stores the rotation input s = x_j - o_j of row i: FP32 form into ST[j][i];
+// tensor-core form as a TF32 hi/lo pair into the swizzled A tiles
+// (hi = round-to-nearest TF32, lo = s - hi exactly; the MMA reads lo's top
+// 19 bits).
+template <bool TC>
+__device__ __forceinline__ void stage(const Smem& s, int i, int j, float v, int NPP) {
+  if constexpr (TC) {
+    const float hi = tc::tf32_round(v);
+    const float lo = v - hi;
+    const uint32_t off = tc::sw128_offset(i, j & 31);
+    unsigned char* t = s.A + (size_t)((j >> 5) * 2) * s.MA * 128;
+    *reinterpret_cast<float*>(t + off) = hi;
+    *reinterpret_cast<float*>(t + (size_t)s.MA * 128 + off) = lo;
+  } else {
+    s.ST[j * NPP + i] = v;
+  }
+}
+
+template <bool TC>
+__device__ void stage_differences(const Smem& s, const float* rows, int nrows, int D, int DP,
+                                  int NPP) {
+  for (int it = threadIdx.x; it < nrows * D; it += kThreads) {
+    const int j = it / nrows, i = it - j * nrows;
+    stage<TC>(s, i, j, fsub(rows[i * DP + j], s.o[j]), NPP);
+  }
+}
+
+// Tensor-core rotation of rows [0, nrows): three tcgen05 MMA passes
+// (hi.hi + hi.lo + lo.hi) over the K steps that cover D, one issuing
+// thread, completion on an mbarrier; then warps 0-3 drain the accumulator
+// (TMEM lane = row) into Z.  phase: the mbarrier parity this CTA expects.
+__device__ void rotate_tc(const Smem& s, int D, int DP, int nrows, uint32_t& phase) {
+  tc::fence_async_smem();  // generic-proxy operand writes -> async proxy
   __syncthreads();
+  const bool dead = s.misc[2] != 0;  // an earlier wait gave up: skip the MMAs
+  if (threadIdx.x == 0 && !dead) {
+    tc::fence_after();
+    uint32_t acc = 0;
+    const int pa[3] = {0, 0, 1}, pb[3] = {0, 1, 0};
+    for (int p = 0; p < 3; ++p)
+      for (int st = 0; st < s.ksteps; ++st) {
+        const int kb = st >> 2, ks = st & 3;
+        const uint64_t ad =
+            tc::sdesc_sw128(s.a_saddr + (uint32_t)((kb * 2 + pa[p]) * s.MA * 128 + ks * 32));
+        const uint64_t bd =
+            tc::sdesc_sw128(s.b_saddr + (uint32_t)((pb[p] * s.nkb + kb) * s.Np * 128 + ks * 32));
+        tc::mma_tf32(s.tmem, ad, bd, s.idesc, acc);
+        acc = 1;
+      }
+    tc::mma_commit(s.mma_bar);
+  }
+  if (!dead) {
+    if (!tc::mbar_wait(s.mma_bar, phase) && threadIdx.x == 0) s.misc[2] = 1;
+    phase ^= 1u;
+  }
+  tc::fence_after();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp < 4 && !dead) {
+    const int row = 32 * warp + lane;
+    for (int c0 = 0; c0 < s.N; c0 += 16) {
+      float v[16];
+      tc::tmem_ld16(s.tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, v);
+      if (row < nrows)
+#pragma unroll
+        for (int q = 0; q < 16; ++q)
+          if (c0 + q < D) s.Z[row * DP + c0 + q] = v[q];
+    }
+  }
+  tc::fence_before();
+  __syncthreads();
+}
+
+// Evaluates rows [0, nrows) of `rows` (shared memory, stride DP) whose
+// differences rows - o are already staged: rotation, then one warp per row.
+template <bool TC>
+__device__ void evaluate_rows(const Smem& s, const FnConst& fc, const float* rows, int nrows,
+                              int DP, int NPP, float* fout, float* tout, uint32_t& phase) {
+  if constexpr (TC) {
+    rotate_tc(s, fc.D, DP, nrows, phase);
+  } else {
+    rotate_f32(s, fc.D, DP, NPP, nrows);
+    __syncthreads();
+  }
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int i = warp; i < nrows; i += kWarps) {
     float t;
@@ -113,16 +232,8 @@ __device__ void evaluate_rows(const Smem& s, const FnConst& fc, const float* row
   __syncthreads();
 }
 
-// ST[j][i] = rows[i][j] - o[j] for i < nrows, j < D.
-__device__ void stage_differences(const Smem& s, const float* rows, int nrows, int D, int DP,
-                                  int NPP) {
-  for (int it = threadIdx.x; it < nrows * D; it += kThreads) {
-    const int j = it / nrows, i = it - j * nrows;
-    s.ST[j * NPP + i] = fsub(rows[i * DP + j], s.o[j]);
-  }
-}
-
-// Trial vectors of generation G into U (and U - o into ST).
+// Trial vectors of generation G into U (and U - o into the rotation input).
+template <bool TC>
 __device__ void build_trials(const Smem& s, const EpochArgs& a, const TaskDev& td, int task,
                              uint32_t G, int DP, int NPP) {
   const int D = td.D, NP = td.NP;
@@ -155,7 +266,7 @@ __device__ void build_trials(const Smem& s, const EpochArgs& a, const TaskDev& t
           const float m = clamp_box(ffma(a.F, fsub(x2[j], x3[j]), xb[j]), lo, hi);
           const float tr = (u01(word(w, q)) < a.CR || j == jr) ? m : xi[j];
           s.U[i * DP + j] = tr;
-          s.ST[j * NPP + i] = fsub(tr, s.o[j]);
+          stage<TC>(s, i, j, fsub(tr, s.o[j]), NPP);
         }
       }
     }
@@ -210,7 +321,7 @@ __device__ void build_trials(const Smem& s, const EpochArgs& a, const TaskDev& t
         c = clamp_box(ffma(dq, range, c), lo, hi);
       }
       s.U[i * DP + j] = c;
-      s.ST[j * NPP + i] = fsub(c, s.o[j]);
+      stage<TC>(s, i, j, fsub(c, s.o[j]), NPP);
     }
   }
 }
@@ -313,8 +424,9 @@ __device__ __forceinline__ int transfer_k(float rate, int NP) {
   return k < 1 ? 1 : (k > NP ? NP : k);
 }
 
-__global__ void __launch_bounds__(kThreads) epoch_kernel(const EpochArgs a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+template <bool TC>
+__device__ __forceinline__ void epoch_body(const EpochArgs& a, const void* tmap,
+                                           unsigned char* smem_raw) {
   const int task = a.single_task >= 0 ? a.single_task
                                       : (a.order ? a.order[blockIdx.x] : (int)blockIdx.x);
   if (task < 0 || task >= a.n_tasks) {
@@ -327,14 +439,62 @@ __global__ void __launch_bounds__(kThreads) epoch_kernel(const EpochArgs a) {
     return;
   }
   const int D = td.D, NP = td.NP;
-  const Layout L = smem_layout(D, NP, td.qt_in_smem != 0);
-  if (L.total > a.smem_bytes) {
-    if (threadIdx.x == 0) report(a.err, CHECK_SMEM_TOO_SMALL);
-    return;
+  Smem s;
+  int DP, NPP;
+  uint32_t ncols = 0;
+  if constexpr (TC) {
+    if (NP > 128 || round16(D) > a.tc_np || round32(D) > a.tc_kp) {
+      if (threadIdx.x == 0) report(a.err, CHECK_TC_SHAPE);
+      return;
+    }
+    const TcLayout L = tc_layout(D, NP, a.tc_np, a.tc_kp);
+    if (L.total > a.smem_bytes) {
+      if (threadIdx.x == 0) report(a.err, CHECK_SMEM_TOO_SMALL);
+      return;
+    }
+    unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    s = carve_tc(base, L);
+    s.QT = const_cast<float*>(a.qt + td.q_off);  // FP32 Q^T for the re-checks
+    DP = L.DP;
+    NPP = round4(NP);
+    s.N = round16(D);
+    s.ksteps = (D + 7) >> 3;
+    s.idesc = tc::idesc_tf32(128, s.N);
+    ncols = 32;
+    while (ncols < (uint32_t)a.tc_np) ncols <<= 1;
+    // zero the operand tiles once: padded K columns meet zero Q columns, so
+    // they only need to hold finite values
+    for (size_t it = threadIdx.x; it < (L.B - L.A) / 16; it += kThreads)
+      reinterpret_cast<float4*>(s.A)[it] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (threadIdx.x == 0) {
+      tc::mbar_init(s.mma_bar, 1);
+      tc::mbar_init(s.tma_bar, 1);
+      s.misc[2] = 0;
+    }
+    if ((threadIdx.x >> 5) == 0) tc::tmem_alloc(reinterpret_cast<uint32_t*>(s.misc + 4), ncols);
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    s.tmem = *reinterpret_cast<volatile uint32_t*>(s.misc + 4);
+    // B operand: Q hi/lo tiles of this task by TMA (box 32 x Np x 1 per tile)
+    if (threadIdx.x == 0) {
+      tc::mbar_expect_tx(s.tma_bar, (uint32_t)(2 * s.nkb * s.Np * 128));
+      for (int h = 0; h < 2; ++h)
+        for (int kb = 0; kb < s.nkb; ++kb)
+          tc::tma_load_3d(s.b_saddr + (uint32_t)((h * s.nkb + kb) * s.Np * 128), tmap, 32 * kb, 0,
+                          2 * task + h, s.tma_bar);
+    }
+  } else {
+    const Layout L = smem_layout(D, NP, td.qt_in_smem != 0);
+    if (L.total > a.smem_bytes) {
+      if (threadIdx.x == 0) report(a.err, CHECK_SMEM_TOO_SMALL);
+      return;
+    }
+    s = carve(smem_raw, L);
+    if (!td.qt_in_smem) s.QT = const_cast<float*>(a.qt + td.q_off);
+    DP = L.DP;
+    NPP = L.NPP;
   }
-  const int DP = L.DP, NPP = L.NPP;
-  Smem s = carve(smem_raw, L);
-  if (!td.qt_in_smem) s.QT = const_cast<float*>(a.qt + td.q_off);
   FnConst fc;
   fc.fid = td.fid;
   fc.D = D;
@@ -343,14 +503,16 @@ __global__ void __launch_bounds__(kThreads) epoch_kernel(const EpochArgs a) {
   fc.qnorm = td.qnorm;
   fc.rel = a.recheck_rel;
   fc.woff64 = td.woff64;
+  uint32_t phase = 0;
 
   // ---- load the task into shared memory ----
   const float* gq = a.qt + td.q_off;
-  if (td.qt_in_smem)
+  if (!TC && td.qt_in_smem)
     for (int it = threadIdx.x; it < D * (DP >> 2); it += kThreads)
       reinterpret_cast<float4*>(s.QT)[it] = reinterpret_cast<const float4*>(gq)[it];
   for (int j = threadIdx.x; j < DP; j += kThreads) s.o[j] = j < D ? a.shift[td.o_off + j] : 0.f;
-  for (int it = threadIdx.x; it < DP * NPP; it += kThreads) s.ST[it] = 0.f;
+  if (!TC)
+    for (int it = threadIdx.x; it < DP * NPP; it += kThreads) s.ST[it] = 0.f;
   float* gpop = a.pop + td.pop_off;
   if (a.mode == MODE_INIT) {
     const float r = fsub(td.hi, td.lo);
@@ -376,15 +538,18 @@ __global__ void __launch_bounds__(kThreads) epoch_kernel(const EpochArgs a) {
     }
   }
   for (int it = threadIdx.x; it < NP * DP; it += kThreads) s.U[it] = 0.f;
+  if constexpr (TC) {
+    if (!tc::mbar_wait(s.tma_bar, 0) && threadIdx.x == 0) s.misc[2] = 1;
+  }
   __syncthreads();
 
   unsigned long long* st_re = a.stats ? a.stats + 0 : nullptr;
   unsigned long long* st_fl = a.stats ? a.stats + 1 : nullptr;
 
   if (a.mode == MODE_INIT || a.mode == MODE_EVAL) {
-    stage_differences(s, s.X, NP, D, DP, NPP);
+    stage_differences<TC>(s, s.X, NP, D, DP, NPP);
     __syncthreads();
-    evaluate_rows(s, fc, s.X, NP, DP, NPP, s.fit, s.tol);
+    evaluate_rows<TC>(s, fc, s.X, NP, DP, NPP, s.fit, s.tol, phase);
     for (int i = threadIdx.x; i < NP; i += kThreads)
       s.fit64[i] = __longlong_as_double(0x7FF8000000000000ll);
     if (threadIdx.x == 0) {
@@ -419,9 +584,9 @@ __global__ void __launch_bounds__(kThreads) epoch_kernel(const EpochArgs a) {
           s.U[c * DP + j] = v;
         }
         __syncthreads();
-        stage_differences(s, s.U, k, D, DP, NPP);
+        stage_differences<TC>(s, s.U, k, D, DP, NPP);
         __syncthreads();
-        evaluate_rows(s, fc, s.U, k, DP, NPP, s.ftr, s.ttr);
+        evaluate_rows<TC>(s, fc, s.U, k, DP, NPP, s.ftr, s.ttr, phase);
         int* target = s.idx + NP;  // member of rank NP - k + c
         for (int c = threadIdx.x; c < k; c += kThreads) target[c] = byrank[NP - k + c];
         __syncthreads();
@@ -434,9 +599,9 @@ __global__ void __launch_bounds__(kThreads) epoch_kernel(const EpochArgs a) {
     // ---- generations ----
     for (int g = 0; g < a.gens; ++g) {
       const uint32_t G = gen0 + (uint32_t)g + 1u;
-      build_trials(s, a, td, task, G, DP, NPP);
+      build_trials<TC>(s, a, td, task, G, DP, NPP);
       __syncthreads();
-      evaluate_rows(s, fc, s.U, NP, DP, NPP, s.ftr, s.ttr);
+      evaluate_rows<TC>(s, fc, s.U, NP, DP, NPP, s.ftr, s.ttr, phase);
       select_and_replace(s, a, fc, NP, nullptr, false, DP, st_re, st_fl);
     }
     if (threadIdx.x == 0) {
@@ -465,6 +630,26 @@ __global__ void __launch_bounds__(kThreads) epoch_kernel(const EpochArgs a) {
     a.tol32[td.fit_off + i] = s.tol[i];
     a.fit64[td.fit_off + i] = s.fit64[i];
   }
+  if constexpr (TC) {
+    if (threadIdx.x == 0 && s.misc[2]) report(a.err, CHECK_TIMEOUT);
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(s.tmem, ncols);
+  }
+}
+
+// FP32 form: three islands of D = 50, NP = 64 share an SM (~68 KB each).
+__global__ void __launch_bounds__(kThreads, 3) epoch_kernel(const EpochArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  epoch_body<false>(a, nullptr, smem_raw);
+}
+
+// Tensor-core form: two islands per SM (~100 KB of operands and state each).
+__global__ void __launch_bounds__(kThreads, 2) epoch_kernel_tc(const EpochArgs a,
+                                                                const __grid_constant__ CUtensorMap tmap) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  epoch_body<true>(a, &tmap, smem_raw);
 }
 
 // Evaluates n caller points of one task in chunks of up to 64 rows per CTA
@@ -504,9 +689,10 @@ __global__ void __launch_bounds__(kThreads) eval_kernel(const EvalArgs a) {
     s.U[it] = (i < nr && j < D) ? a.x[(size_t)(r0 + i) * D + j] : 0.f;
   }
   __syncthreads();
-  stage_differences(s, s.U, nr, D, DP, NPP);
+  stage_differences<false>(s, s.U, nr, D, DP, NPP);
   __syncthreads();
-  evaluate_rows(s, fc, s.U, nr, DP, NPP, s.ftr, s.ttr);
+  uint32_t phase = 0;
+  evaluate_rows<false>(s, fc, s.U, nr, DP, NPP, s.ftr, s.ttr, phase);
   for (int i = threadIdx.x; i < nr; i += kThreads) a.f[r0 + i] = s.ftr[i];
   if (a.z)
     for (int it = threadIdx.x; it < nr * D; it += kThreads) {
@@ -563,13 +749,22 @@ int emt_launch_best(const emt::BestArgs& a, void* stream) {
   return (int)cudaGetLastError();
 }
 
-int emt_launch_epoch(const emt::EpochArgs& a, int grid, void* stream) {
+int emt_launch_epoch(const emt::EpochArgs& a, int grid, void* stream, const void* tmap) {
   if (grid <= 0) return 0;
-  static_assert(sizeof(emt::EpochArgs) < 4096, "kernel parameter block");
-  cudaError_t e = cudaFuncSetAttribute(emt::epoch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)a.smem_bytes);
-  if (e != cudaSuccess) return (int)e;
-  emt::epoch_kernel<<<grid, emt::kThreads, a.smem_bytes, (cudaStream_t)stream>>>(a);
+  static_assert(sizeof(emt::EpochArgs) < 2048, "kernel parameter block");
+  cudaError_t e;
+  if (tmap) {
+    e = cudaFuncSetAttribute(emt::epoch_kernel_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)a.smem_bytes);
+    if (e != cudaSuccess) return (int)e;
+    emt::epoch_kernel_tc<<<grid, emt::kThreads, a.smem_bytes, (cudaStream_t)stream>>>(
+        a, *reinterpret_cast<const CUtensorMap*>(tmap));
+  } else {
+    e = cudaFuncSetAttribute(emt::epoch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)a.smem_bytes);
+    if (e != cudaSuccess) return (int)e;
+    emt::epoch_kernel<<<grid, emt::kThreads, a.smem_bytes, (cudaStream_t)stream>>>(a);
+  }
   return (int)cudaGetLastError();
 }
 

@@ -1,0 +1,90 @@
+"""Tensor-core form (tcgen05 kind::tf32, hi/lo split, 3 products, FP32
+accumulation in tensor memory): fitness within the stated tolerance of the
+FP64 oracle, and generations bit-exact with the FP64-decided replay."""
+import numpy as np
+import pytest
+
+from gpu_util import make_engine, oracle_params, tolerance
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(1, 4), (2, 8), (10, 16), (33, 40), (50, 64), (50, 100), (64, 128)]
+
+
+def tc_engine(sgemtf, orc, specs, seed=1, **cfg):
+    eng, tasks = make_engine(sgemtf, orc, specs, seed=seed, precision=sgemtf.ROT_TF32X3, **cfg)
+    return eng, tasks
+
+
+@pytest.mark.parametrize("D,NP", SHAPES)
+def test_tc_fitness_matches_fp64(sgemtf, orc, D, NP):
+    specs = [(f, D, NP, 1) for f in range(7)]
+    eng, tasks = tc_engine(sgemtf, orc, specs, seed=D * 7 + NP)
+    eng.reset()
+    assert eng.stats()["precision_used"] == sgemtf.ROT_TF32X3
+    rng = np.random.default_rng(D + NP)
+    for i, t in enumerate(tasks):
+        X = rng.uniform(t.c.lo, t.c.hi, (NP, D)).astype(np.float32)
+        X[0] = t.o
+        eng.set_population(i, X)      # evaluated by the tensor-core epoch kernel
+        Xg, f = eng.population(i)
+        assert np.array_equal(Xg, X)
+        worst = 0.0
+        for r in range(NP):
+            f64, s, _ = t.eval64(X[r])
+            assert abs(float(f[r]) - f64) <= tolerance(orc, t, X[r], s), (i, r, float(f[r]), f64)
+            if t.c.fid != orc.WEIERSTRASS and s > 0:
+                worst = max(worst, abs(float(f[r]) - f64) / s)
+        assert worst <= 1e-5
+
+
+@pytest.mark.parametrize("alg", [0, 1, 2])
+def test_tc_replay_bit_exact(sgemtf, orc, alg):
+    specs = [(f, 50, 64, 1) for f in range(7)]
+    eng, tasks = tc_engine(sgemtf, orc, specs, seed=13, algorithm=alg)
+    eng.reset()
+    X0 = [eng.population(i)[0] for i in range(7)]
+    gens = 15
+    eng.run(gens)
+    p = oracle_params(orc, eng)
+    for i, t in enumerate(tasks):
+        x = X0[i].copy()
+        f64 = np.array([t.eval64(r)[0] for r in x])
+        f32 = f64.astype(np.float32)
+        for g in range(1, gens + 1):
+            orc.generation(p, t, x, f32, f64, g, 0)
+        assert np.array_equal(eng.population(i)[0], x), (alg, i)
+
+
+def test_tc_and_fp32_forms_select_identically(sgemtf, orc):
+    """Both rotation forms take the FP64 decision on near ties, so their
+    populations agree bit for bit."""
+    specs = [(f, 30, 48, 1) for f in range(7)]
+    a, _ = make_engine(sgemtf, orc, specs, seed=3, precision=sgemtf.ROT_FP32)
+    b, _ = tc_engine(sgemtf, orc, specs, seed=3)
+    a.run(40)
+    b.run(40)
+    for i in range(7):
+        assert np.array_equal(a.population(i)[0], b.population(i)[0]), i
+
+
+def test_tc_transfer_runs(sgemtf, orc):
+    specs = [(f, 20, 32, 1) for f in range(7)]
+    a, _ = make_engine(sgemtf, orc, specs, seed=5, transfer_interval=5, precision=sgemtf.ROT_FP32)
+    b, _ = tc_engine(sgemtf, orc, specs, seed=5, transfer_interval=5)
+    a.run(20)
+    b.run(20)
+    for i in range(7):
+        assert np.array_equal(a.population(i)[0], b.population(i)[0]), i
+
+
+def test_tc_rejects_unsupported_shapes(sgemtf):
+    eng = sgemtf.Engine(sgemtf.Config(seed=1, precision=sgemtf.ROT_TF32X3))
+    eng.add_tasks([sgemtf.TaskDesc(0, 50, 200)])
+    with pytest.raises(sgemtf.EngineError) as e:
+        eng.reset()
+    assert e.value.status == sgemtf.ERR_UNSUPPORTED
+    auto = sgemtf.Engine(sgemtf.Config(seed=1, precision=sgemtf.ROT_AUTO))
+    auto.add_tasks([sgemtf.TaskDesc(0, 50, 200)])
+    auto.run(2)
+    assert auto.stats()["precision_used"] == sgemtf.ROT_FP32
