@@ -36,71 +36,60 @@ constexpr uint32_t FLAG_REF_ACKLEY_E = 0x4u;
 constexpr uint32_t FLAG_REF_BOXES = 0x8u;
 constexpr uint32_t FLAG_NO_RECHECK = 0x10u;
 
-// Weierstrass terms k = 0..20 of one gene: sum of 0.5^k cos(2 pi 3^k (z + 1/2))
-// and of their absolute values.  cos(2 pi 3^k (z + 1/2)) = -cos(pi y_k) with
-// y_k = 2 * 3^k * |z| (3^k is odd).  y_k mod 2 is computed exactly from the
-// FP32 significand of z for k <= 6; terms k >= 7 follow the angle-tripling
-// identity cos(3t) = cos t (4 cos^2 t - 3), whose error grows 3x per step but
-// is weighted 0.5^k (total below 1.5e-6 per gene).
-__device__ __forceinline__ void weier_gene_f32(float z, float& sum, float& sabs) {
+// Weierstrass terms k = 0..20 of one gene: sum of 0.5^k cos(2 pi 3^k (z + 1/2)).
+// cos(2 pi 3^k (z + 1/2)) = -cos(pi y_k) with y_k = 2 * 3^k * |z| (3^k is odd).
+// Anchors k = 0, 5, 10, 15 reduce y_k mod 2 exactly from the FP32 significand
+// of z (r_k = M 3^k mod 2^(sh+1), unsigned wrap-around arithmetic) and take
+// cospif; the other terms follow the angle-tripling identity
+// cos(3t) = cos t (4 cos^2 t - 3), whose error grows 3x per step but at most
+// 4 steps from an anchor and weighted 0.5^k: below 14 anchor errors per gene.
+__device__ __forceinline__ float weier_gene_f32(float z) {
   const float az = fabsf(z);
   const uint32_t bits = __float_as_uint(az);
   const uint32_t E = bits >> 23;
   const uint32_t M = (bits & 0x7FFFFFu) | 0x800000u;
   const int sh = 149 - (int)E;  // y_0 = M / 2^sh for normal az
-  float s = 0.f, sa = 0.f, ak = 1.f, c = 1.f;
-  if (E == 0u || sh > 61) {
-    float p3 = 2.f;
-#pragma unroll
-    for (int k = 0; k <= 6; ++k) {
-      c = cospif(p3 * az);
-      s = fmaf(ak, -c, s);
-      sa = fmaf(ak, fabsf(c), sa);
-      ak *= 0.5f;
-      p3 *= 3.f;
-    }
-  } else if (sh <= 0) {
-    c = (sh == 0 && (M & 1u)) ? -1.f : 1.f;  // y_k integer, parity of M 3^k
-#pragma unroll
-    for (int k = 0; k <= 6; ++k) {
-      s = fmaf(ak, -c, s);
-      sa += ak;
-      ak *= 0.5f;
-    }
+  float y[4];
+  if (E == 0u || sh > 61) {  // |z| < 2^-37: y_k is tiny, plain FP32 is exact enough
+    y[0] = 2.f * az;
+    y[1] = 486.f * az;
+    y[2] = 118098.f * az;
+    y[3] = 28697814.f * az;
+  } else if (sh <= 0) {  // |z| >= 2^22: y_k integer, parity of M 3^k = parity of M (sh = 0)
+    const float p = (sh == 0 && (M & 1u)) ? 1.f : 0.f;
+    y[0] = y[1] = y[2] = y[3] = p;
   } else if (sh <= 31) {
     const uint32_t mask = (2u << sh) - 1u;
     const float scale = __uint_as_float((uint32_t)(127 - sh) << 23);
     uint32_t r = M & mask;
 #pragma unroll
-    for (int k = 0; k <= 6; ++k) {
-      c = cospif((float)r * scale);
-      s = fmaf(ak, -c, s);
-      sa = fmaf(ak, fabsf(c), sa);
-      ak *= 0.5f;
-      r = (r * 3u) & mask;
+    for (int a = 0; a < 4; ++a) {
+      y[a] = (float)r * scale;
+      r = (r * 243u) & mask;  // 3^5
     }
   } else {
     const unsigned long long mask = (2ull << sh) - 1ull;
     const float scale = __uint_as_float((uint32_t)(127 - sh) << 23);
     unsigned long long r = M;
 #pragma unroll
-    for (int k = 0; k <= 6; ++k) {
-      c = cospif((float)r * scale);
-      s = fmaf(ak, -c, s);
-      sa = fmaf(ak, fabsf(c), sa);
-      ak *= 0.5f;
-      r = (r * 3ull) & mask;
+    for (int a = 0; a < 4; ++a) {
+      y[a] = (float)r * scale;
+      r = (r * 243ull) & mask;
     }
   }
+  // k = 0 anchor, then k = 1..20 with anchors at k = 5, 10, 15
+  float c = cospif(y[0]);
+  float s = -c, ak = 1.f;
 #pragma unroll
-  for (int k = 7; k <= 20; ++k) {
-    c = c * fmaf(4.f * c, c, -3.f);
-    s = fmaf(ak, -c, s);
-    sa = fmaf(ak, fabsf(c), sa);
+  for (int k = 1; k <= 20; ++k) {
     ak *= 0.5f;
+    if (k == 5 || k == 10 || k == 15)
+      c = cospif(y[k / 5]);
+    else
+      c = c * fmaf(4.f * c, c, -3.f);
+    s = fmaf(-ak, c, s);
   }
-  sum = s;
-  sabs = sa;
+  return s;
 }
 
 __device__ __forceinline__ float warp_sum(float v) {
@@ -149,138 +138,147 @@ struct FnConst {
   double woff64;
 };
 
-// FP32 fitness of one rotated row z[0..D) (shared memory), evaluated by the
-// calling warp; x is the unrotated row and o the shift.  Returns f; *tol
-// gets the half-width of the near-tie window, rel * scale, where scale is the
-// sum of absolute sub-terms of f and rel the stated accuracy of the FP32 form
-// (1e-5; the parity tests check |f - f64| <= 1e-5 scale).  Weierstrass adds
-// the conditioning bound of its 3^k-amplified terms (weier_rotation_bound).
-// Near an optimum the forms below avoid cancellation: Ackley uses expm1 of
-// sum z^2 and of sum sin^2(pi z), Griewank 1 - prod cos = -expm1(sum
-// log1p(-2 sin^2(theta/2))), Rastrigin z^2 + 20 sin^2(pi z).
-__device__ float eval_row_f32(const FnConst& fc, const float* __restrict__ z,
-                              const float* __restrict__ x, const float* __restrict__ o,
-                              float* tol) {
-  const int lane = threadIdx.x & 31;
+// FP32 fitness of rows [0, nrows) of Z (rotated, shared memory, stride DP),
+// evaluated by the whole CTA: tpr consecutive threads share a row (4 rows
+// per warp-octet for nrows <= 64), each summing a contiguous chunk of genes,
+// then a tpr-lane butterfly.  x rows (unrotated) and o give x - o for the
+// Weierstrass rounding bound.  fout/tout receive f and the half-width of the
+// near-tie window, rel * scale, where scale is the sum of absolute
+// sub-terms of f and rel the stated accuracy of the FP32 form (1e-5; the
+// parity tests check |f - f64| <= 1e-5 scale).  Weierstrass adds the
+// conditioning bound of its 3^k-amplified terms (weier_rotation_bound) and
+// bounds its terms' magnitudes by 2 per gene.  Near an optimum the forms
+// below avoid cancellation: Ackley uses expm1 of sum z^2 and of sum
+// sin^2(pi z), Griewank 1 - prod cos = -expm1(sum log1p(-2 sin^2(theta/2))),
+// Rastrigin z^2 + 20 sin^2(pi z).
+template <int kBlock>
+__device__ void eval_rows_f32(const FnConst& fc, const float* __restrict__ Z,
+                              const float* __restrict__ rows, const float* __restrict__ o,
+                              int nrows, int DP, float* __restrict__ fout,
+                              float* __restrict__ tout) {
   const int D = fc.D;
-  float a = 0.f, b = 0.f, c = 1.f, sa = 0.f, ss = 0.f;
-  int neg = 0;
-  switch (fc.fid) {
-    case F_SPHERE:
-      for (int j = lane; j < D; j += 32) {
-        const float v = z[j];
-        a = fmaf(v, v, a);
-      }
-      sa = a;
-      break;
-    case F_RASTRIGIN:
-      for (int j = lane; j < D; j += 32) {
-        const float v = z[j], sp = sinpif(v), z2 = v * v;
-        const float t = fmaf(20.f * sp, sp, z2);
-        a += t;
-        sa += t;
-      }
-      break;
-    case F_ACKLEY:
-      for (int j = lane; j < D; j += 32) {
-        const float v = z[j], sp = sinpif(v);
-        a = fmaf(v, v, a);
-        b = fmaf(sp, sp, b);           // sum sin^2(pi z)
-      }
-      break;
-    case F_GRIEWANK:
-      for (int j = lane; j < D; j += 32) {
-        const float v = z[j];
-        a = fmaf(v, v, a);
-        if (!(fc.flags & FLAG_REF_GRIEWANK_NO_PRODUCT)) {
-          const float th = __fdiv_rn(v, sqrtf((float)(j + 1)));
-          const float ct = cosf(th);
-          c *= ct;
-          if (ct > 0.f) {
-            const float sh = sinf(0.5f * th);
-            b += log1pf(-2.f * sh * sh);
-          } else {
-            neg = 1;
+  const int tpr = nrows <= kBlock / 4 ? 4 : (nrows <= kBlock / 2 ? 2 : 1);
+  const int per_pass = kBlock / tpr;
+  const int sub = threadIdx.x & (tpr - 1);
+  const int chunk = (D + tpr - 1) / tpr;
+  const int j0 = sub * chunk, j1 = min(D, j0 + chunk);
+  const bool griewank_prod = !(fc.flags & FLAG_REF_GRIEWANK_NO_PRODUCT);
+  for (int base = 0; base < nrows; base += per_pass) {
+    const int row = base + (int)threadIdx.x / tpr;
+    float a = 0.f, b = 0.f, c = 1.f, sa = 0.f, ss = 0.f;
+    int neg = 0;
+    if (row < nrows) {
+      const float* z = Z + row * DP;
+      switch (fc.fid) {
+        case F_SPHERE:
+          for (int j = j0; j < j1; ++j) a = fmaf(z[j], z[j], a);
+          sa = a;
+          break;
+        case F_RASTRIGIN:
+          for (int j = j0; j < j1; ++j) {
+            const float v = z[j], sp = sinpif(v);
+            a += fmaf(20.f * sp, sp, v * v);
           }
+          sa = a;
+          break;
+        case F_ACKLEY:
+          for (int j = j0; j < j1; ++j) {
+            const float v = z[j], sp = sinpif(v);
+            a = fmaf(v, v, a);
+            b = fmaf(sp, sp, b);  // sum sin^2(pi z)
+          }
+          break;
+        case F_GRIEWANK:
+          for (int j = j0; j < j1; ++j) {
+            const float v = z[j];
+            a = fmaf(v, v, a);
+            if (griewank_prod) {
+              const float th = __fdiv_rn(v, sqrtf((float)(j + 1)));
+              const float ct = cosf(th);
+              c *= ct;
+              if (ct > 0.f) {
+                const float sh = sinf(0.5f * th);
+                b += log1pf(-2.f * sh * sh);
+              } else {
+                neg = 1;
+              }
+            }
+          }
+          break;
+        case F_ROSENBROCK:
+          for (int j = j0; j < j1 && j + 1 < D; ++j) {
+            const float v = z[j], n = z[j + 1];
+            const float t1 = fmaf(v, v, -n), t2 = v - 1.f;
+            const float t = fmaf(100.f * t1, t1, t2 * t2);
+            a += t;
+            sa += t + 200.f * fabsf(t1) * fmaf(v, v, fabsf(n)) + 2.f * fabsf(t2) * (fabsf(v) + 1.f);
+          }
+          break;
+        case F_SCHWEFEL:
+          for (int j = j0; j < j1; ++j) {
+            const float v = z[j], t = v * sinf(sqrtf(fabsf(v)));
+            a += t;
+            sa += fabsf(t);
+          }
+          break;
+        case F_WEIERSTRASS: {
+          const float* x = rows + row * DP;
+          for (int j = j0; j < j1; ++j) {
+            a += weier_gene_f32(z[j]);
+            const float d = x[j] - o[j];
+            ss = fmaf(d, d, ss);
+          }
+          break;
         }
+        default:
+          break;
       }
-      break;
-    case F_ROSENBROCK:
-      for (int j = lane; j + 1 < D; j += 32) {
-        const float v = z[j], n = z[j + 1];
-        const float t1 = fmaf(v, v, -n), t2 = v - 1.f;
-        const float t = fmaf(100.f * t1, t1, t2 * t2);
-        a += t;
-        sa += t + 200.f * fabsf(t1) * fmaf(v, v, fabsf(n)) + 2.f * fabsf(t2) * (fabsf(v) + 1.f);
-      }
-      break;
-    case F_SCHWEFEL:
-      for (int j = lane; j < D; j += 32) {
-        const float v = z[j], r = sqrtf(fabsf(v)), sr = sinf(r), t = v * sr;
-        a += t;
-        sa += fabsf(t);
-      }
-      break;
-    case F_WEIERSTRASS:
-      for (int j = lane; j < D; j += 32) {
-        float t, ta;
-        weier_gene_f32(z[j], t, ta);
-        a += t;
-        sa += ta;
-        const float d = x[j] - o[j];
-        ss = fmaf(d, d, ss);
-      }
-      break;
-    default:
-      break;
-  }
-  a = warp_sum(a);
-  sa = warp_sum(sa);
-  float f, scale;
-  switch (fc.fid) {
-    case F_ACKLEY: {
-      b = warp_sum(b);
-      const float e = 2.71828183f;
-      const float eref = (fc.flags & FLAG_REF_ACKLEY_E) ? 2.718282f - e : 0.f;
-      const float r = sqrtf(a / (float)D);
-      const float t1 = -20.f * expm1f(-0.2f * r);       // 20 - 20 exp(-0.2 sqrt(A/D))
-      const float t2 = -e * expm1f(-2.f * b / (float)D); // e - exp(sum cos(2 pi z) / D)
-      f = t1 + t2 + eref;
-      scale = t1 + t2 + fabsf(eref);
-      break;
     }
-    case F_GRIEWANK: {
-      float om;  // 1 - prod cos
-      if (fc.flags & FLAG_REF_GRIEWANK_NO_PRODUCT) {
-        om = 0.f;
-        scale = a / 4000.f;
-      } else {
-        b = warp_sum(b);
-        c = warp_prod(c);
-        neg = __any_sync(0xFFFFFFFFu, neg);
-        om = neg ? 1.f - c : -expm1f(b);
-        scale = a / 4000.f + fabsf(om) + (neg ? fabsf(c) + 1.f : 0.f);
-      }
-      f = om + a / 4000.f;
-      break;
+    for (int m = 1; m < tpr; m <<= 1) {
+      a += __shfl_xor_sync(0xFFFFFFFFu, a, m);
+      b += __shfl_xor_sync(0xFFFFFFFFu, b, m);
+      c *= __shfl_xor_sync(0xFFFFFFFFu, c, m);
+      sa += __shfl_xor_sync(0xFFFFFFFFu, sa, m);
+      ss += __shfl_xor_sync(0xFFFFFFFFu, ss, m);
+      neg |= __shfl_xor_sync(0xFFFFFFFFu, neg, m);
     }
-    case F_SCHWEFEL:
-      f = 418.9829f * (float)D - a;
-      scale = 418.9829f * (float)D + sa;
-      break;
-    case F_WEIERSTRASS:
-      f = a + fc.woff;
-      scale = sa + fabsf(fc.woff);
-      break;
-    default:  // sphere, rastrigin, rosenbrock: non-negative sums
-      f = a;
-      scale = sa;
-      break;
+    if (row < nrows && sub == 0) {
+      float f, scale;
+      switch (fc.fid) {
+        case F_ACKLEY: {
+          const float e = 2.71828183f;
+          const float eref = (fc.flags & FLAG_REF_ACKLEY_E) ? 2.718282f - e : 0.f;
+          const float t1 = -20.f * expm1f(-0.2f * sqrtf(a / (float)D));  // 20 - 20 exp(-0.2 r)
+          const float t2 = -e * expm1f(-2.f * b / (float)D);            // e - exp(B / D)
+          f = t1 + t2 + eref;
+          scale = t1 + t2 + fabsf(eref);
+          break;
+        }
+        case F_GRIEWANK: {
+          const float om = !griewank_prod ? 0.f : (neg ? 1.f - c : -expm1f(b));  // 1 - prod cos
+          f = om + a / 4000.f;
+          scale = a / 4000.f + fabsf(om) + ((griewank_prod && neg) ? fabsf(c) + 1.f : 0.f);
+          break;
+        }
+        case F_SCHWEFEL:
+          f = 418.9829f * (float)D - a;
+          scale = 418.9829f * (float)D + sa;
+          break;
+        case F_WEIERSTRASS:
+          f = a + fc.woff;
+          scale = 2.f * (float)D + fabsf(fc.woff);
+          break;
+        default:  // sphere, rastrigin, rosenbrock: non-negative sums
+          f = a;
+          scale = sa;
+          break;
+      }
+      float t = fc.rel * scale;
+      if (fc.fid == F_WEIERSTRASS) t += weier_rotation_bound(D, fc.qnorm, sqrtf(ss));
+      fout[row] = f;
+      tout[row] = t;
+    }
   }
-  float t = fc.rel * scale;
-  if (fc.fid == F_WEIERSTRASS) t += weier_rotation_bound(D, fc.qnorm, sqrtf(warp_sum(ss)));
-  *tol = t;
-  return f;
 }
 
 // s + e = a + b exactly (Knuth's TwoSum).

@@ -144,7 +144,16 @@ EMT_HD TcLayout tc_layout(int D, int NP, int Np, int Kp) {
   const size_t bsz = (size_t)2 * L.nkb * Np * 128, slack = (size_t)(128 - L.MA) * 128;
   off += bsz > slack ? bsz : slack;
   L.fit64 = off; off = align16(off + sizeof(double) * NP);
-  L.z64 = off;   off = align16(off + sizeof(double) * kWarps * L.DP);
+  // FP64 re-check scratch: idle A-region space past Z (the re-checks run
+  // after the epilogue has consumed Z and before the next operands are staged)
+  const size_t zend = align16(L.A + sizeof(float) * NP * L.DP);
+  const size_t zbuf = sizeof(double) * kWarps * L.DP;
+  if (zend + zbuf <= L.B) {
+    L.z64 = zend;
+  } else {
+    L.z64 = off;
+    off = align16(off + zbuf);
+  }
   L.X = off;     off = align16(off + sizeof(float) * NP * L.DP);
   L.U = off;     off = align16(off + sizeof(float) * NP * L.DP);
   L.o = off;     off = align16(off + sizeof(float) * L.DP);

@@ -155,12 +155,44 @@ __device__ __forceinline__ void stage(const Smem& s, int i, int j, float v, int 
   }
 }
 
+// Four consecutive inputs s_{4b..4b+3} of row i (zeros beyond D).  In the
+// tensor-core form they fill one 16-byte chunk of the swizzled tile, so a
+// quarter-warp on 8 consecutive rows writes 8 distinct chunks (no bank
+// conflicts).
+template <bool TC>
+__device__ __forceinline__ void stage4(const Smem& s, int i, int b, float4 v, int NPP) {
+  if constexpr (TC) {
+    float4 hi, lo;
+    hi.x = tc::tf32_round(v.x); lo.x = v.x - hi.x;
+    hi.y = tc::tf32_round(v.y); lo.y = v.y - hi.y;
+    hi.z = tc::tf32_round(v.z); lo.z = v.z - hi.z;
+    hi.w = tc::tf32_round(v.w); lo.w = v.w - hi.w;
+    const uint32_t off = (uint32_t)((i >> 3) * 1024 + (i & 7) * 128 + (((b & 7) ^ (i & 7)) << 4));
+    unsigned char* t = s.A + (size_t)((b >> 3) * 2) * s.MA * 128 + off;
+    *reinterpret_cast<float4*>(t) = hi;
+    *reinterpret_cast<float4*>(t + (size_t)s.MA * 128) = lo;
+  } else {
+    s.ST[(4 * b + 0) * NPP + i] = v.x;
+    s.ST[(4 * b + 1) * NPP + i] = v.y;
+    s.ST[(4 * b + 2) * NPP + i] = v.z;
+    s.ST[(4 * b + 3) * NPP + i] = v.w;
+  }
+}
+
 template <bool TC>
 __device__ void stage_differences(const Smem& s, const float* rows, int nrows, int D, int DP,
                                   int NPP) {
-  for (int it = threadIdx.x; it < nrows * D; it += kThreads) {
-    const int j = it / nrows, i = it - j * nrows;
-    stage<TC>(s, i, j, fsub(rows[i * DP + j], s.o[j]), NPP);
+  const int nb = DP >> 2;
+  for (int it = threadIdx.x; it < nrows * nb; it += kThreads) {
+    const int b = it / nrows, i = it - b * nrows;
+    const float4 x = reinterpret_cast<const float4*>(rows + i * DP)[b];
+    const float4 o = reinterpret_cast<const float4*>(s.o)[b];
+    float4 v;
+    v.x = 4 * b + 0 < D ? fsub(x.x, o.x) : 0.f;
+    v.y = 4 * b + 1 < D ? fsub(x.y, o.y) : 0.f;
+    v.z = 4 * b + 2 < D ? fsub(x.z, o.z) : 0.f;
+    v.w = 4 * b + 3 < D ? fsub(x.w, o.w) : 0.f;
+    stage4<TC>(s, i, b, v, NPP);
   }
 }
 
@@ -169,6 +201,17 @@ __device__ void stage_differences(const Smem& s, const float* rows, int nrows, i
 // thread, completion on an mbarrier; then warps 0-3 drain the accumulator
 // (TMEM lane = row) into Z.  phase: the mbarrier parity this CTA expects.
 __device__ void rotate_tc(const Smem& s, int D, int DP, int nrows, uint32_t& phase) {
+  // Columns [D, Kp) of every staged row must hold finite values (they meet
+  // the zero columns of Q): the FP64 re-check scratch shares this region, so
+  // clear them here, whatever path staged the row.
+  const int kp = s.nkb * 32, npad = kp - D;
+  for (int it = threadIdx.x; it < nrows * npad; it += kThreads) {
+    const int i = it / npad, j = D + (it - i * npad);
+    const uint32_t off = tc::sw128_offset(i, j & 31);
+    unsigned char* t = s.A + (size_t)((j >> 5) * 2) * s.MA * 128;
+    *reinterpret_cast<float*>(t + off) = 0.f;
+    *reinterpret_cast<float*>(t + (size_t)s.MA * 128 + off) = 0.f;
+  }
   tc::fence_async_smem();  // generic-proxy operand writes -> async proxy
   __syncthreads();
   const bool dead = s.misc[2] != 0;  // an earlier wait gave up: skip the MMAs
@@ -194,15 +237,17 @@ __device__ void rotate_tc(const Smem& s, int D, int DP, int nrows, uint32_t& pha
   }
   tc::fence_after();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (warp < 4 && !dead) {
+  if (warp < 4 && 32 * warp < nrows && !dead) {  // warp-uniform: the loads are .sync.aligned
     const int row = 32 * warp + lane;
     for (int c0 = 0; c0 < s.N; c0 += 16) {
       float v[16];
       tc::tmem_ld16(s.tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, v);
       if (row < nrows)
 #pragma unroll
-        for (int q = 0; q < 16; ++q)
-          if (c0 + q < D) s.Z[row * DP + c0 + q] = v[q];
+        for (int q = 0; q < 4; ++q)
+          if (c0 + 4 * q < DP)
+            reinterpret_cast<float4*>(s.Z + row * DP)[(c0 >> 2) + q] =
+                make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
     }
   }
   tc::fence_before();
@@ -220,15 +265,7 @@ __device__ void evaluate_rows(const Smem& s, const FnConst& fc, const float* row
     rotate_f32(s, fc.D, DP, NPP, nrows);
     __syncthreads();
   }
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int i = warp; i < nrows; i += kWarps) {
-    float t;
-    const float f = eval_row_f32(fc, s.Z + i * DP, rows + i * DP, s.o, &t);
-    if (lane == 0) {
-      fout[i] = f;
-      tout[i] = t;
-    }
-  }
+  eval_rows_f32<kThreads>(fc, s.Z, rows, s.o, nrows, DP, fout, tout);
   __syncthreads();
 }
 
@@ -259,16 +296,20 @@ __device__ void build_trials(const Smem& s, const EpochArgs& a, const TaskDev& t
       const float* x2 = s.X + r2 * DP;
       const float* x3 = s.X + r3 * DP;
       const float* xi = s.X + i * DP;
+      float tr[4], sv[4];
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const int j = 4 * b + q;
+        tr[q] = 0.f;
+        sv[q] = 0.f;
         if (j < D) {
           const float m = clamp_box(ffma(a.F, fsub(x2[j], x3[j]), xb[j]), lo, hi);
-          const float tr = (u01(word(w, q)) < a.CR || j == jr) ? m : xi[j];
-          s.U[i * DP + j] = tr;
-          stage<TC>(s, i, j, fsub(tr, s.o[j]), NPP);
+          tr[q] = (u01(word(w, q)) < a.CR || j == jr) ? m : xi[j];
+          sv[q] = fsub(tr[q], s.o[j]);
         }
       }
+      reinterpret_cast<float4*>(s.U + i * DP)[b] = make_float4(tr[0], tr[1], tr[2], tr[3]);
+      stage4<TC>(s, i, b, make_float4(sv[0], sv[1], sv[2], sv[3]), NPP);
     }
     return;
   }
