@@ -879,6 +879,20 @@ int emt_restore(emt_handle_t* h, const void* buf, size_t bytes) {
   h->gdone = (uint32_t)hdr[2];
   h->initialized = true;
   h->elite_parity = 0;
+  // At a transfer boundary the next epoch imports the elites exported at the
+  // end of the last one: export them again from the restored islands (they
+  // rank by the same restored FP32 fitness, so the rows are identical).
+  const int interval = (h->cfg.transfer_interval > 0 && h->tasks.size() > 1) ? h->cfg.transfer_interval : 0;
+  if (interval && h->gdone > 0 && h->gdone % (uint32_t)interval == 0) {
+    emt::EpochArgs a = base_args(h, emt::MODE_EPOCH);
+    a.gens = 0;
+    a.transfer_export = 1;
+    a.elites_out = h->d_elites[0].p;
+    int e = launch_epoch(h, a, (int)h->tasks.size(), h->stream);
+    if (e) return h->cuda_fail((cudaError_t)e, "elite export");
+    h->elite_parity = 1;
+    return emt_sync(h);
+  }
   return EMT_OK;
 }
 

@@ -1,0 +1,56 @@
+"""Builds tests/golden/reference_records_T100.json from the reference's own
+recorded GA runs, data process/ANO_Tnum/data_record_T_ANO_100.txt (18 runs x
+100 tasks x 22 columns: best fitness at generations 0, 50, ..., 1000, then
+the 481st-best member of the initial population; writer commented at
+proposed model/SG-EMTF.cu:2015-2026).
+
+The task -> function map is the reference's: glibc srand(0); rand() % 7 per
+task with task 0 forced to type 6 (SG-EMTF.cu:307-313).  Reference types are
+stored as recorded (0 Sphere, 1 Rosenbrock, 2 Ackley, 3 Rastrigin,
+4 Griewank, 5 Weierstrass, 6 Schwefel).
+
+Run here (the reference is mounted only on the build machine):
+    python tests/golden/make_reference_records.py
+"""
+import ctypes
+import json
+import os
+
+SRC = "/root/reference/data process/ANO_Tnum/data_record_T_ANO_100.txt"
+OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_records_T100.json")
+
+
+def reference_types(n):
+    libc = ctypes.CDLL("libc.so.6")
+    libc.srand(0)
+    t = [libc.rand() % 7 for _ in range(n)]
+    t[0] = 6
+    return t
+
+
+def main():
+    runs, cur = [], []
+    for line in open(SRC):
+        line = line.strip()
+        if not line:
+            if cur:
+                runs.append(cur)
+                cur = []
+            continue
+        cur.append([float(v) for v in line.split()])
+    if cur:
+        runs.append(cur)
+    assert all(len(r) == 100 and all(len(row) == 22 for row in r) for r in runs), "layout"
+    out = {
+        "source": "data process/ANO_Tnum/data_record_T_ANO_100.txt",
+        "columns": "gen0_best, gen1000_best, gen0_rank481",
+        "types": reference_types(100),
+        "runs": [[[row[0], row[20], row[21]] for row in r] for r in runs],
+    }
+    with open(OUT, "w") as f:
+        json.dump(out, f, separators=(",", ":"))
+    print(OUT, len(runs), "runs")
+
+
+if __name__ == "__main__":
+    main()

@@ -34,6 +34,22 @@ def test_snapshot_restore_continues_bit_exact(sgemtf, orc):
         assert np.array_equal(a.population(i)[0], b.population(i)[0])
 
 
+@pytest.mark.parametrize("at", [10, 15])
+def test_snapshot_at_transfer_boundary(sgemtf, orc, at):
+    """A snapshot taken right at a transfer boundary resumes with the same
+    elite exchange as the uninterrupted run."""
+    specs = [(f, 12, 20, 1) for f in range(7)]
+    a, _ = make_engine(sgemtf, orc, specs, seed=17, transfer_interval=5)
+    a.run(at)
+    blob = a.snapshot()
+    a.run(12)
+    b, _ = make_engine(sgemtf, orc, specs, seed=17, transfer_interval=5)
+    b.restore(blob)
+    b.run(12)
+    for i in range(7):
+        assert np.array_equal(a.population(i)[0], b.population(i)[0])
+
+
 def test_best_is_population_minimum(sgemtf, orc):
     specs = [(f, 10, 20, 1) for f in range(7)]
     eng, tasks = make_engine(sgemtf, orc, specs, seed=6)
