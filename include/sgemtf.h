@@ -23,7 +23,8 @@
  *     the optional CUDA stream (a cudaStream_t passed as void*; NULL = the
  *     legacy default stream).
  *   - A handle is used by one host thread at a time.  Calls on different
- *     handles are independent: the library keeps no global mutable state.
+ *     handles are independent: apart from emt_run_noalloc's shared device
+ *     array, the library keeps no global mutable state.
  *   - Random numbers come from a counter-based Philox4x32-10 stream keyed by
  *     emt_config.seed, so a run is reproducible bit for bit: the same seed and
  *     call sequence give the same populations on every run.
@@ -187,6 +188,28 @@ EMT_API int emt_reset(emt_handle_t* h, void* stream);
  * (:462-486) and knowledgeTransfer (:1514-1591), for all tasks at once.
  * Asynchronous on `stream`; emt_sync waits and reports device errors. */
 EMT_API int emt_run(emt_handle_t* h, int32_t generations, void* stream);
+
+/* Same as emt_run, but allocates nothing.  For callers that cannot allocate
+ * device memory while they run: a service whose GPU memory is reserved up
+ * front by its own pool allocator, or a host loop that must not call
+ * cudaMalloc/cudaFree because those calls synchronize the device.  No
+ * counterpart in the reference.
+ *
+ * The handle must have been prepared with emt_reset (which allocates the
+ * islands); this call then only launches kernels and copies device to
+ * device.  The elite exchange between epochs goes through one file-scope
+ * device array of 2 x EMT_NOALLOC_EXCHANGE_FLOATS floats (4 MiB) that every
+ * GPU loading the library holds until the process exits.  Limit: the sum
+ * over tasks of NP * round4(D) must not exceed EMT_NOALLOC_EXCHANGE_FLOATS,
+ * else EMT_ERR_UNSUPPORTED and nothing runs.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) with that
+ * device current; make that first call before any stream capture.  All
+ * calls share the array and it keeps the last call's contents: calls that
+ * overlap on the GPU (other handles, other streams) race on it.  Nothing in
+ * it needs to start at zero: each call first copies in the exchange state
+ * its handle carries.  Results are bit-identical to emt_run. */
+#define EMT_NOALLOC_EXCHANGE_FLOATS (1 << 19)
+EMT_API int emt_run_noalloc(emt_handle_t* h, int32_t generations, void* stream);
 
 /* Waits for the handle's work and reports a kernel's error word. */
 EMT_API int emt_sync(emt_handle_t* h);

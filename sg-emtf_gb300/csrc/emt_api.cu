@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <numeric>
 #include <string>
@@ -622,6 +623,104 @@ int emt_run(emt_handle_t* h, int32_t generations, void* stream) {
     if (interval && do_export) h->elite_parity ^= 1;
     h->gdone += (uint32_t)g;
     left -= g;
+  }
+  cudaEventRecord(h->ev1, h->stream);
+  h->timing_pending = true;
+  return EMT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// emt_run_noalloc: the epoch loop of emt_run with the elite-exchange scratch
+// in a file-scope device array instead of the handle's allocation.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) float g_noalloc_exchange[2 * EMT_NOALLOC_EXCHANGE_FLOATS];
+
+static std::mutex g_noalloc_mu;
+static float* g_noalloc_ptr[256];  // device address of g_noalloc_exchange per ordinal
+
+// Host code cannot use g_noalloc_exchange's name as a device address (it is a
+// host-side stand-in): look the address up once per device, with that device
+// current, and reuse it.
+static int noalloc_scratch(emt_handle* h, float** out) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (h->device < 0 || h->device >= 256) return h->fail(EMT_ERR_INVALID_ARG, "device ordinal");
+  if (!g_noalloc_ptr[h->device]) {
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return h->cuda_fail(e, "cudaSetDevice");
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_exchange);
+    if (e != cudaSuccess || !p) return h->cuda_fail(e, "cudaGetSymbolAddress");
+    g_noalloc_ptr[h->device] = (float*)p;
+  }
+  *out = g_noalloc_ptr[h->device];
+  return EMT_OK;
+}
+
+int emt_run_noalloc(emt_handle_t* h, int32_t generations, void* stream) {
+  if (!h) return EMT_ERR_INVALID_ARG;
+  if (generations < 0) return h->fail(EMT_ERR_INVALID_ARG, "negative generation count");
+  if (!h->initialized || !h->uploaded)
+    return h->fail(EMT_ERR_STATE, "emt_run_noalloc needs a handle prepared by emt_reset");
+  const int n = (int)h->tasks.size();
+  const int interval = (h->cfg.transfer_interval > 0 && n > 1) ? h->cfg.transfer_interval : 0;
+  float* buf[2] = {nullptr, nullptr};
+  size_t need = 0;
+  if (interval) {
+    for (const auto& t : h->table) need += (size_t)t.NP * t.DP;
+    if (need > (size_t)EMT_NOALLOC_EXCHANGE_FLOATS)
+      return h->fail(EMT_ERR_UNSUPPORTED,
+                     "emt_run_noalloc: the elite exchange needs " + std::to_string(need) +
+                         " floats per buffer; the static buffer holds " +
+                         std::to_string(EMT_NOALLOC_EXCHANGE_FLOATS));
+    float* base = nullptr;
+    int rc = noalloc_scratch(h, &base);
+    if (rc) return rc;
+    buf[0] = base;
+    buf[1] = base + EMT_NOALLOC_EXCHANGE_FLOATS;
+  }
+  h->stream = (cudaStream_t)stream;
+  cudaError_t ce = cudaSetDevice(h->device);
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "cudaSetDevice");
+  // the exchange state the handle carries in: elites of the last boundary
+  if (interval && h->gdone > 0 && h->gdone % (uint32_t)interval == 0) {
+    const int in = h->elite_parity ^ 1;
+    ce = cudaMemcpyAsync(buf[in], h->d_elites[in].p, sizeof(float) * need, cudaMemcpyDeviceToDevice,
+                         h->stream);
+    if (ce != cudaSuccess) return h->cuda_fail(ce, "exchange copy in");
+  }
+  cudaEventRecord(h->ev0, h->stream);
+  bool exported_last = false;
+  int left = generations;
+  while (left > 0) {
+    int g = left;
+    bool do_import = false, do_export = false;
+    if (interval) {
+      do_import = h->gdone > 0 && (h->gdone % (uint32_t)interval) == 0;
+      int to_boundary = interval - (int)(h->gdone % (uint32_t)interval);
+      g = std::min(left, to_boundary);
+      do_export = ((h->gdone + (uint32_t)g) % (uint32_t)interval) == 0;
+    }
+    emt::EpochArgs a = base_args(h, emt::MODE_EPOCH);
+    a.gens = g;
+    if (interval) {
+      a.transfer_import = do_import ? 1 : 0;
+      a.transfer_export = do_export ? 1 : 0;
+      a.elites_in = buf[h->elite_parity ^ 1];
+      a.elites_out = buf[h->elite_parity];
+    }
+    int e = launch_epoch(h, a, n, stream);
+    if (e) return h->cuda_fail((cudaError_t)e, "epoch launch");
+    exported_last = interval && do_export;
+    if (exported_last) h->elite_parity ^= 1;
+    h->gdone += (uint32_t)g;
+    left -= g;
+  }
+  // the exchange state the handle carries out, for its next emt_run
+  if (exported_last) {
+    const int in = h->elite_parity ^ 1;
+    ce = cudaMemcpyAsync(h->d_elites[in].p, buf[in], sizeof(float) * need, cudaMemcpyDeviceToDevice,
+                         h->stream);
+    if (ce != cudaSuccess) return h->cuda_fail(ce, "exchange copy out");
   }
   cudaEventRecord(h->ev1, h->stream);
   h->timing_pending = true;

@@ -32,10 +32,11 @@ FLAG_REF_ACKLEY_E = 0x4
 FLAG_REF_BOXES = 0x8
 FLAG_NO_RECHECK = 0x10
 MAX_DIM, MAX_POP = 128, 256
+NOALLOC_EXCHANGE_FLOATS = 1 << 19
 
 EXPORTED = [
     "emt_config_default", "emt_function_from_reference", "emt_function_box", "emt_create",
-    "emt_add_tasks", "emt_reset", "emt_run", "emt_sync", "emt_get_best", "emt_get_best_all",
+    "emt_add_tasks", "emt_reset", "emt_run", "emt_run_noalloc", "emt_sync", "emt_get_best", "emt_get_best_all",
     "emt_get_population", "emt_set_population", "emt_get_task_params", "emt_evaluate",
     "emt_get_stats", "emt_snapshot_size", "emt_snapshot", "emt_restore", "emt_last_error",
     "emt_status_string", "emt_destroy",
@@ -125,6 +126,7 @@ def lib():
         L.emt_add_tasks.argtypes = [vp, i32, ctypes.POINTER(TaskDescC)]
         L.emt_reset.argtypes = [vp, vp]
         L.emt_run.argtypes = [vp, i32, vp]
+        L.emt_run_noalloc.argtypes = [vp, i32, vp]
         L.emt_sync.argtypes = [vp]
         L.emt_get_best.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_double), f32p]
         L.emt_get_best_all.argtypes = [vp, f32p]
@@ -188,6 +190,12 @@ class Engine:
 
     def run(self, generations, stream=None, sync=True):
         self._check(lib().emt_run(self._h, int(generations), stream), "emt_run")
+        if sync:
+            self.sync()
+
+    def run_noalloc(self, generations, stream=None, sync=True):
+        """emt_run_noalloc: allocates nothing (needs a prior reset())."""
+        self._check(lib().emt_run_noalloc(self._h, int(generations), stream), "emt_run_noalloc")
         if sync:
             self.sync()
 
