@@ -251,14 +251,16 @@ def main():
         for _ in range(k):
             flush.zero_()  # L2 (129 MB) flush between steps
             e0 = torch.cuda.Event(enable_timing=True)
+            em = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            eng.reset(sp)
-            eng.run(gens, sp, sync=False)
+            eng.reset(sp)          # init launch: population draw + evaluation
+            em.record(stream)
+            eng.run(gens, sp, sync=False)  # the epoch launch (all generations)
             e1.record(stream)
-            evs.append((e0, e1))
+            evs.append((e0, em, e1))
         torch.cuda.synchronize()
-        return [a.elapsed_time(b) for a, b in evs]
+        return [a.elapsed_time(c) for a, _, c in evs], [b.elapsed_time(c) for _, b, c in evs]
 
     evals_per_step = n * POP * (gens + 1)
     results = {}
@@ -274,7 +276,7 @@ def main():
         torch.cuda.synchronize()
         with ClockSampler(local) as clk:
             t0 = time.perf_counter()
-            ms = time_steps(eng, args.steps)
+            ms, epoch_ms = time_steps(eng, args.steps)
             barrier()
             torch.cuda.synchronize()
             wall = time.perf_counter() - t0
@@ -284,7 +286,8 @@ def main():
             t = torch.tensor([dev_ms], device="cuda")
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             dev_ms = float(t.item())
-        results[name] = {"ms": ms, "dev_ms": dev_ms, "wall": wall, "stats": st,
+        results[name] = {"ms": ms, "epoch_ms": float(np.mean(epoch_ms)), "dev_ms": dev_ms,
+                         "wall": wall, "stats": st,
                          "clocks": clk.summary(), "precision_used": st["precision_used"]}
         eng.close()
     head = "tf32x3" if "tf32x3" in results and results["tf32x3"]["precision_used"] == 1 else "fp32"
@@ -329,18 +332,26 @@ def main():
 
     peaks, peak_kind = measured_peaks()
     ms_step = r["dev_ms"] / args.steps
-    achieved_tflops = FLOPS_PER_EVAL * evals_per_step / (ms_step * 1e-3) / 1e12
+    # dominant kernel: the epoch launch (all generations), timed with events
+    # on the launching stream; algorithmic work = 2 D^2 flop per evaluation
+    epoch_s = r["epoch_ms"] * 1e-3
+    evals_epoch = n * POP * gens
+    dp = (DIM + 3) // 4 * 4
+    state_bytes = n * (DIM * dp * 4 + dp * 4 + 2 * POP * dp * 4 + POP * 16 * 2)
     if head == "tf32x3":
-        roof = {"bound": "tensor", "achieved": achieved_tflops, "peak": peaks["bf16_tflops"],
-                "unit": "TFLOP/s", "frac": achieved_tflops / peaks["bf16_tflops"],
-                "traffic": None, "peak_kind": peak_kind + " (bf16 dense; tf32 nominal is half)"}
+        achieved = FLOPS_PER_EVAL * evals_epoch / epoch_s / 1e12
+        roof = {"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"],
+                "unit": "TFLOP/s", "frac": achieved / peaks["bf16_tflops"],
+                # ncu dram read bytes of one epoch launch (31.1 MB for 608 tasks,
+                # scaled to the workload's tasks; the state is read once)
+                "traffic": 31.1e6 * n / 608,
+                "peak_kind": peak_kind + " bf16 dense (tf32 nominal is half of it)",
+                "note": "the tensor pipe is ~4% busy; the kernel is bound by CUDA-core "
+                        "issue (function epilogue, trial builder, near-tie re-checks)"}
     else:
-        # FP32 form: compulsory HBM traffic of the step (state in, state out)
-        dp = (DIM + 3) // 4 * 4
-        bytes_step = n * (DIM * dp * 4 + dp * 4 + 2 * POP * dp * 4 + POP * 16 * 2)
-        gbs = bytes_step / (ms_step * 1e-3) / 1e9
+        gbs = state_bytes / epoch_s / 1e9
         roof = {"bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": gbs / peaks["hbm_gbs"], "traffic": None,
+                "frac": gbs / peaks["hbm_gbs"], "traffic": 23.1e6 * n / 912,
                 "peak_kind": peak_kind, "note": "state is resident in shared memory across "
                 "generations; the kernel is bound by CUDA-core issue, not HBM"}
     line = {
@@ -355,6 +366,7 @@ def main():
                    "evals_per_step_per_gpu": evals_per_step, "l2": "flushed (256 MB write) "
                    "before every step", "form": head, "parallelism": "task-sharded x%d" % world},
         "forms": {k: {"value": total_evals / (v["dev_ms"] * 1e-3), "ms_per_step": v["dev_ms"] / args.steps,
+                      "epoch_kernel_ms": v["epoch_ms"],
                       "rechecks": v["stats"]["rechecks"], "recheck_flips": v["stats"]["recheck_flips"],
                       "precision_used": v["precision_used"]} for k, v in results.items()},
         "roofline": roof,

@@ -113,6 +113,8 @@ typedef enum emt_rotation {
 #define EMT_FLAG_REF_ACKLEY_E 0x4u            /* E = 2.718282 (SG-EMTF.cu:54) */
 #define EMT_FLAG_REF_BOXES 0x8u               /* box table of SG-EMTF.cu:197-214 */
 #define EMT_FLAG_NO_RECHECK 0x10u             /* select on FP32 fitness only */
+#define EMT_FLAG_RIGOROUS_WINDOW 0x20u        /* Weierstrass near-tie window from the
+                                                 rigorous 3^k conditioning bound */
 
 typedef struct emt_config {
   int32_t algorithm;         /* emt_algorithm                                */

@@ -587,7 +587,8 @@ static double recheck_window(const orc_params* p, const orc_task* t, const float
   double rel = p->recheck_rel > 0 ? p->recheck_rel : 1e-5;
   double w = rel * (double)s32;
   (void)f32;
-  if (t->fid == ORC_WEIERSTRASS) w += orc_weierstrass_rotation_bound(t, x);
+  if (t->fid == ORC_WEIERSTRASS)
+    w = (p->flags & ORC_FLAG_RIGOROUS_WINDOW) ? w + orc_weierstrass_rotation_bound(t, x) : 5.0 * w;
   return w;
 }
 

@@ -51,6 +51,7 @@ enum { ORC_DE_RAND1 = 0, ORC_DE_CURRENT1 = 1, ORC_GA = 2 };
 #define ORC_FLAG_REF_ACKLEY_E 0x4u
 #define ORC_FLAG_REF_BOXES 0x8u
 #define ORC_FLAG_NO_RECHECK 0x10u
+#define ORC_FLAG_RIGOROUS_WINDOW 0x20u
 
 /* ---- Philox4x32-10 and the stream layout shared with the engine ----
  * key = (seed low 32 bits, seed high 32 bits)

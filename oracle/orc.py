@@ -22,6 +22,7 @@ FLAG_REF_WEIERSTRASS_CONST = 0x2
 FLAG_REF_ACKLEY_E = 0x4
 FLAG_REF_BOXES = 0x8
 FLAG_NO_RECHECK = 0x10
+FLAG_RIGOROUS_WINDOW = 0x20
 
 P_POP_INIT, P_SHIFT, P_QR_NORMAL, P_DE_INDEX, P_DE_CR = 1, 2, 3, 4, 5
 P_GA_PARENT, P_GA_SBX, P_GA_PM, P_TRANSFER_PARTNER, P_TRANSFER_MIX = 6, 7, 8, 9, 10

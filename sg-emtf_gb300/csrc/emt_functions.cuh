@@ -6,8 +6,10 @@
 // rounding error of f and sets the FP64 re-check window.
 //
 // FP64-class form (re-check of near-tie selections): the rotation by a
-// compensated double-FP32 dot product (dot2_rotation) and the terms in double
-// precision; Weierstrass reduces each argument exactly (eval_row_weier_precise).
+// compensated double-FP32 dot product (precise_rotation); then tier 2, FP32
+// terms with a per-row error bound, and only if that cannot decide, tier 3,
+// the terms in double precision.  Weierstrass reduces each argument exactly
+// (eval_weier_precise).
 //
 // Definitions follow the reference's evaluation() (proposed model/
 // SG-EMTF.cu:898-1111): Sphere :918, Rosenbrock :939, Ackley :963 (E =
@@ -35,6 +37,7 @@ constexpr uint32_t FLAG_REF_WEIERSTRASS_CONST = 0x2u;
 constexpr uint32_t FLAG_REF_ACKLEY_E = 0x4u;
 constexpr uint32_t FLAG_REF_BOXES = 0x8u;
 constexpr uint32_t FLAG_NO_RECHECK = 0x10u;
+constexpr uint32_t FLAG_RIGOROUS_WINDOW = 0x20u;
 
 // Weierstrass terms k = 0..20 of one gene: sum of 0.5^k cos(2 pi 3^k (z + 1/2)).
 // cos(2 pi 3^k (z + 1/2)) = -cos(pi y_k) with y_k = 2 * 3^k * |z| (3^k is odd).
@@ -145,9 +148,12 @@ struct FnConst {
 // Weierstrass rounding bound.  fout/tout receive f and the half-width of the
 // near-tie window, rel * scale, where scale is the sum of absolute
 // sub-terms of f and rel the stated accuracy of the FP32 form (1e-5; the
-// parity tests check |f - f64| <= 1e-5 scale).  Weierstrass adds the
-// conditioning bound of its 3^k-amplified terms (weier_rotation_bound) and
-// bounds its terms' magnitudes by 2 per gene.  Near an optimum the forms
+// parity tests check |f - f64| <= 1e-5 scale).  Weierstrass, whose terms
+// amplify the rotation's rounding by 3^k, gets 5 x rel * scale (five times
+// the largest error measured on the FP32 form; the parity tests check it),
+// or with EMT_FLAG_RIGOROUS_WINDOW the rigorous conditioning bound
+// (weier_rotation_bound), which sends most late-run selections to the
+// re-check.  Weierstrass term magnitudes are bounded by 2 per gene.  Near an optimum the forms
 // below avoid cancellation: Ackley uses expm1 of sum z^2 and of sum
 // sin^2(pi z), Griewank 1 - prod cos = -expm1(sum log1p(-2 sin^2(theta/2))),
 // Rastrigin z^2 + 20 sin^2(pi z).
@@ -274,7 +280,9 @@ __device__ void eval_rows_f32(const FnConst& fc, const float* __restrict__ Z,
           break;
       }
       float t = fc.rel * scale;
-      if (fc.fid == F_WEIERSTRASS) t += weier_rotation_bound(D, fc.qnorm, sqrtf(ss));
+      if (fc.fid == F_WEIERSTRASS)
+        t = (fc.flags & FLAG_RIGOROUS_WINDOW) ? t + weier_rotation_bound(D, fc.qnorm, sqrtf(ss))
+                                              : 5.f * t;
       fout[row] = f;
       tout[row] = t;
     }
@@ -332,91 +340,115 @@ __device__ __forceinline__ float weier_gene_precise(double z) {
   return s;
 }
 
-// z_n = sum_k q_nk (x_k - o_k) to FP64-class accuracy on the FP32 pipe: the
-// compensated dot product of Ogita, Rump and Oishi ("Dot2", SIAM J. Sci.
-// Comput. 26, 2005) over the exact split x_k - o_k = sh_k + sl_k, so that
-// |z - z_exact| <~ u |z| + gamma_D^2 sum_k |q_nk||x_k - o_k|.  This GPU's
-// FP64 pipe runs at a small fraction of its FP32 rate, so ~12 FP32
-// operations per product beat one FP64 FMA.
-__device__ __forceinline__ double dot2_rotation(const float* __restrict__ x,
-                                                const float* __restrict__ o,
-                                                const float* __restrict__ qt, int DP, int D,
-                                                int n) {
-  float S = 0.f, C = 0.f;
+// Two outputs z_n, z_m (m = n + 32, or none) of sum_k q_nk (x_k - o_k) to
+// FP64-class accuracy on the FP32 pipe: the compensated dot product of Ogita,
+// Rump and Oishi ("Dot2", SIAM J. Sci. Comput. 26, 2005) over the exact split
+// x_k - o_k = sh_k + sl_k, so |z - z_exact| <~ u |z| + gamma_D^2 sum |q||x - o|.
+// The two chains are interleaved for instruction-level parallelism.  This
+// GPU's FP64 pipe runs at ~1/45 of its FP32 rate, so ~12 FP32 operations per
+// product beat one FP64 FMA.
+__device__ __forceinline__ void dot2_pair(const float* __restrict__ x, const float* __restrict__ o,
+                                          const float* __restrict__ qt, int DP, int D, int n,
+                                          bool two, double& zn, double& zm) {
+  float S0 = 0.f, C0 = 0.f, S1 = 0.f, C1 = 0.f;
+  const int m = two ? n + 32 : n;
   for (int k = 0; k < D; ++k) {
-    const float q = qt[k * DP + n];
     float sh, sl;
     two_sum(x[k], -o[k], sh, sl);
-    const float p = __fmul_rn(q, sh);
-    const float pe = __fmaf_rn(q, sh, -p);
-    float t, te;
-    two_sum(S, p, t, te);
-    S = t;
-    C = __fmaf_rn(q, sl, __fadd_rn(C, __fadd_rn(te, pe)));
+    const float q0 = qt[k * DP + n], q1 = qt[k * DP + m];
+    const float p0 = __fmul_rn(q0, sh), p1 = __fmul_rn(q1, sh);
+    const float e0 = __fmaf_rn(q0, sh, -p0), e1 = __fmaf_rn(q1, sh, -p1);
+    float t0, te0, t1, te1;
+    two_sum(S0, p0, t0, te0);
+    two_sum(S1, p1, t1, te1);
+    S0 = t0;
+    S1 = t1;
+    C0 = __fmaf_rn(q0, sl, __fadd_rn(C0, __fadd_rn(te0, e0)));
+    C1 = __fmaf_rn(q1, sl, __fadd_rn(C1, __fadd_rn(te1, e1)));
   }
-  return (double)S + (double)C;
+  zn = (double)S0 + (double)C0;
+  zm = (double)S1 + (double)C1;
 }
 
-// Weierstrass re-check: z_n by dot2_rotation, then the exactly reduced terms
-// above (FP32/INT pipes only).
-__device__ double eval_row_weier_precise(const FnConst& fc, const float* __restrict__ x,
-                                         const float* __restrict__ o,
-                                         const float* __restrict__ qt, int DP, double woff64) {
+// The calling warp fills zbuf[0..D) with the FP64-class rotation of row x.
+__device__ __forceinline__ void precise_rotation(const float* __restrict__ x,
+                                                 const float* __restrict__ o,
+                                                 const float* __restrict__ qt, int DP, int D,
+                                                 double* zbuf) {
   const int lane = threadIdx.x & 31;
-  double acc = 0.0;
-  for (int n = lane; n < fc.D; n += 32)
-    acc += (double)weier_gene_precise(dot2_rotation(x, o, qt, DP, fc.D, n));
-  acc = warp_sum64(acc);
-  return acc + woff64;
+  for (int n = lane; n < D; n += 64) {
+    double a, b;
+    const bool two = n + 32 < D;
+    dot2_pair(x, o, qt, DP, D, n, two, a, b);
+    zbuf[n] = a;
+    if (two) zbuf[n + 32] = b;
+  }
+  __syncwarp();
 }
 
-// FP64-class fitness of x (shared memory row), evaluated by the calling warp:
-// z_n = sum_k Q[n][k] (x_k - o_k) by dot2_rotation (qt[k*DP + n] = Q[n][k]),
-// terms in double.  zbuf: DP doubles of per-warp scratch.
-__device__ double eval_row_f64(const FnConst& fc, const float* __restrict__ x,
-                               const float* __restrict__ o, const float* __restrict__ qt,
-                               int DP, double* zbuf) {
-  if (fc.fid == F_WEIERSTRASS) return eval_row_weier_precise(fc, x, o, qt, DP, fc.woff64);
+// sin(pi v) and cos(v) for |pi v|, |v| < 2^-10 by Taylor series (error below
+// 1e-25); the double-precision library calls cost ~10 SM-clocks each here.
+__device__ __forceinline__ double sinpi_small(double v) {
+  const double x = 3.141592653589793 * v, x2 = x * x;
+  return x * fma(x2, fma(x2, 1.0 / 120.0, -1.0 / 6.0), 1.0);
+}
+__device__ __forceinline__ double cos_small(double t) {
+  const double t2 = t * t;
+  return fma(t2, fma(t2, fma(t2, -1.0 / 720.0, 1.0 / 24.0), -0.5), 1.0);
+}
+// 1/sqrt(v) and sqrt(v) for v > 0 in double: FP32 estimate, two Newton steps.
+__device__ __forceinline__ double rsqrt_d(double v) {
+  double r = (double)rsqrtf((float)v);
+  r = r * fma(-0.5 * v * r, r, 1.5);
+  r = r * fma(-0.5 * v * r, r, 1.5);
+  return r;
+}
+
+// Tier 3: f in double precision from the FP64-class rotation zbuf.
+__device__ double eval_tier3(const FnConst& fc, const double* zbuf) {
   const int lane = threadIdx.x & 31;
   const int D = fc.D;
-  for (int n = lane; n < D; n += 32) zbuf[n] = dot2_rotation(x, o, qt, DP, D, n);
-  __syncwarp();
-  double a = 0.0, b = (fc.fid == F_GRIEWANK) ? 1.0 : 0.0;
+  double a = 0.0, b = 0.0, c = 1.0;
   switch (fc.fid) {
     case F_SPHERE:
       for (int j = lane; j < D; j += 32) a = fma(zbuf[j], zbuf[j], a);
       break;
     case F_RASTRIGIN:
       for (int j = lane; j < D; j += 32) {
-        double v = zbuf[j];
-        a += v * v - 10.0 * cospi(2.0 * v) + 10.0;
+        const double v = zbuf[j];
+        const double sp = fabs(v) < 0x1p-12 ? sinpi_small(v) : sinpi(v);
+        a += fma(20.0 * sp, sp, v * v);
       }
       break;
     case F_ACKLEY:
       for (int j = lane; j < D; j += 32) {
-        double v = zbuf[j];
+        const double v = zbuf[j];
+        const double sp = fabs(v) < 0x1p-12 ? sinpi_small(v) : sinpi(v);
         a = fma(v, v, a);
-        b += cospi(2.0 * v);
+        b = fma(sp, sp, b);
       }
       break;
     case F_GRIEWANK:
       for (int j = lane; j < D; j += 32) {
-        double v = zbuf[j];
+        const double v = zbuf[j];
         a = fma(v, v, a);
-        if (!(fc.flags & FLAG_REF_GRIEWANK_NO_PRODUCT)) b *= cos(v / sqrt((double)(j + 1)));
+        if (!(fc.flags & FLAG_REF_GRIEWANK_NO_PRODUCT)) {
+          const double th = v * rsqrt_d((double)(j + 1));
+          c *= fabs(th) < 0x1p-10 ? cos_small(th) : cos(th);
+        }
       }
       break;
     case F_ROSENBROCK:
       for (int j = lane; j + 1 < D; j += 32) {
-        double v = zbuf[j], n = zbuf[j + 1];
-        double t1 = v * v - n, t2 = v - 1.0;
+        const double v = zbuf[j], n = zbuf[j + 1];
+        const double t1 = v * v - n, t2 = v - 1.0;
         a += 100.0 * t1 * t1 + t2 * t2;
       }
       break;
     case F_SCHWEFEL:
       for (int j = lane; j < D; j += 32) {
-        double v = zbuf[j];
-        a += v * sin(sqrt(fabs(v)));
+        const double v = zbuf[j], av = fabs(v);
+        if (av > 0.0) a += v * sin(av * rsqrt_d(av));
       }
       break;
     default:
@@ -427,13 +459,14 @@ __device__ double eval_row_f64(const FnConst& fc, const float* __restrict__ x,
   switch (fc.fid) {
     case F_ACKLEY: {
       b = warp_sum64(b);
-      const double e = (fc.flags & FLAG_REF_ACKLEY_E) ? 2.718282 : 2.718281828459045;
-      f = -20.0 * exp(-0.2 * sqrt(a / D)) - exp(b / D) + 20.0 + e;
+      const double e = 2.718281828459045;
+      const double eref = (fc.flags & FLAG_REF_ACKLEY_E) ? 2.718282 - e : 0.0;
+      f = -20.0 * expm1(-0.2 * sqrt(a / D)) - e * expm1(-2.0 * b / D) + eref;
       break;
     }
     case F_GRIEWANK:
-      b = warp_prod64(b);
-      f = 1.0 + a / 4000.0 - b;
+      c = warp_prod64(c);
+      f = (1.0 - c) + a / 4000.0;
       break;
     case F_SCHWEFEL:
       f = 418.9829 * D - a;
@@ -442,6 +475,134 @@ __device__ double eval_row_f64(const FnConst& fc, const float* __restrict__ x,
       f = a;
       break;
   }
+  return f;
+}
+
+// Tier 2: f from the FP64-class rotation zbuf with FP32 function terms on the
+// rounded z, summed in double, and *err, a first-order bound on |f - f(z)|:
+// per gene |g'(z)| |z - fl(z)| + 8u (|g| + |sub-terms|).  Sphere and
+// Rosenbrock need no transcendental and go straight to tier 3.
+__device__ double eval_tier2(const FnConst& fc, const double* zbuf, double* err) {
+  const int lane = threadIdx.x & 31;
+  const int D = fc.D;
+  const double u = 0x1p-24;
+  double a = 0.0, b = 0.0, e = 0.0, eb = 0.0, lg = 0.0, c = 1.0;
+  int neg = 0;
+  switch (fc.fid) {
+    case F_RASTRIGIN:
+      for (int j = lane; j < D; j += 32) {
+        const double v = zbuf[j];
+        const float zf = (float)v;
+        const double dz = fabs(v - (double)zf);
+        const float sp = sinpif(zf), cp = cospif(zf);
+        const double g = (double)zf * zf + 20.0 * (double)sp * sp;
+        a += g;
+        e += fabs(2.0 * zf + 125.66370614359172 * sp * cp) * dz + 8.0 * u * g;
+      }
+      break;
+    case F_ACKLEY:
+      for (int j = lane; j < D; j += 32) {
+        const double v = zbuf[j];
+        const float zf = (float)v;
+        const double dz = fabs(v - (double)zf);
+        const float sp = sinpif(zf), cp = cospif(zf);
+        a = fma(v, v, a);
+        b += (double)sp * sp;
+        eb += 6.283185307179586 * fabs(sp * cp) * dz + 4.0 * u * (double)sp * sp;
+      }
+      break;
+    case F_GRIEWANK:
+      for (int j = lane; j < D; j += 32) {
+        const double v = zbuf[j];
+        a = fma(v, v, a);
+        if (!(fc.flags & FLAG_REF_GRIEWANK_NO_PRODUCT)) {
+          const double th = v * rsqrt_d((double)(j + 1));
+          const float tf = (float)th;
+          const double dt = fabs(th - (double)tf);
+          const float ct = cosf(tf), st = sinf(tf);
+          c *= (double)ct;
+          if (ct > 0.f) {
+            const float sh = sinf(0.5f * tf);
+            lg += (double)log1pf(-2.f * sh * sh);
+            eb += fabs((double)st / (double)ct) * dt + 8.0 * u;
+          } else {
+            neg = 1;
+            eb += 1.0;  // no relative bound through a non-positive cosine
+          }
+        }
+      }
+      break;
+    case F_SCHWEFEL:
+      for (int j = lane; j < D; j += 32) {
+        const double v = zbuf[j];
+        const float zf = (float)v;
+        const double dz = fabs(v - (double)zf);
+        const float r = sqrtf(fabsf(zf)), sr = sinf(r), cr = cosf(r);
+        const double g = (double)zf * sr;
+        a += g;
+        e += fabs((double)sr + 0.5 * r * cr) * dz + 8.0 * u * fabs((double)zf) * (1.0 + r);
+      }
+      break;
+    default:
+      break;
+  }
+  a = warp_sum64(a);
+  e = warp_sum64(e);
+  double f;
+  switch (fc.fid) {
+    case F_ACKLEY: {
+      b = warp_sum64(b);
+      eb = warp_sum64(eb);
+      const double ee = 2.718281828459045;
+      const double eref = (fc.flags & FLAG_REF_ACKLEY_E) ? 2.718282 - ee : 0.0;
+      const double x2 = exp(-2.0 * b / D);
+      f = -20.0 * expm1(-0.2 * sqrt(a / D)) - ee * expm1(-2.0 * b / D) + eref;
+      e = ee * x2 * (2.0 / D) * eb + 1e-15 * fabs(f);
+      break;
+    }
+    case F_GRIEWANK: {
+      double om;
+      if (fc.flags & FLAG_REF_GRIEWANK_NO_PRODUCT) {
+        om = 0.0;
+        e = 0.0;
+      } else {
+        c = warp_prod64(c);
+        lg = warp_sum64(lg);
+        eb = warp_sum64(eb);
+        neg = __any_sync(0xFFFFFFFFu, neg);
+        om = neg ? 1.0 - c : -expm1(lg);
+        e = neg ? 1e300 : fabs(c) * eb;  // a sign change: leave it to tier 3
+      }
+      f = om + a / 4000.0;
+      break;
+    }
+    case F_SCHWEFEL:
+      f = 418.9829 * D - a;
+      break;
+    default:
+      f = a;
+      break;
+  }
+  *err = 2.0 * e;  // safety factor on the first-order bound
+  return f;
+}
+
+// Weierstrass from the FP64-class rotation: exactly reduced terms (FP32/INT).
+__device__ double eval_weier_precise(const FnConst& fc, const double* zbuf) {
+  const int lane = threadIdx.x & 31;
+  double acc = 0.0;
+  for (int n = lane; n < fc.D; n += 32) acc += (double)weier_gene_precise(zbuf[n]);
+  acc = warp_sum64(acc);
+  return acc + fc.woff64;
+}
+
+// FP64-class fitness of x (shared or global memory row) by the calling warp
+// (qt[k*DP + n] = Q[n][k]); zbuf: DP doubles of per-warp scratch.
+__device__ double eval_row_f64(const FnConst& fc, const float* __restrict__ x,
+                               const float* __restrict__ o, const float* __restrict__ qt,
+                               int DP, double* zbuf) {
+  precise_rotation(x, o, qt, DP, fc.D, zbuf);
+  const double f = fc.fid == F_WEIERSTRASS ? eval_weier_precise(fc, zbuf) : eval_tier3(fc, zbuf);
   __syncwarp();
   return f;
 }

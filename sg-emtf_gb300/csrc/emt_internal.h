@@ -100,7 +100,7 @@ EMT_HD Layout smem_layout(int D, int NP, bool qt_in_smem = true) {
   L.NPP = round4(NP);
   size_t off = 0;
   L.fit64 = off; off = align16(off + sizeof(double) * NP);
-  L.z64 = off;   off = align16(off + sizeof(double) * kWarps * L.DP);
+  L.z64 = off;   off = align16(off + sizeof(double) * kWarps * 2 * L.DP);
   L.X = off;     off = align16(off + sizeof(float) * NP * L.DP);
   L.U = off;     off = align16(off + sizeof(float) * NP * L.DP);
   L.ST = off;    off = align16(off + sizeof(float) * L.DP * L.NPP);
@@ -147,7 +147,7 @@ EMT_HD TcLayout tc_layout(int D, int NP, int Np, int Kp) {
   // FP64 re-check scratch: idle A-region space past Z (the re-checks run
   // after the epilogue has consumed Z and before the next operands are staged)
   const size_t zend = align16(L.A + sizeof(float) * NP * L.DP);
-  const size_t zbuf = sizeof(double) * kWarps * L.DP;
+  const size_t zbuf = sizeof(double) * kWarps * 2 * L.DP;
   if (zend + zbuf <= L.B) {
     L.z64 = zend;
   } else {

@@ -394,21 +394,48 @@ __device__ int select_and_replace(const Smem& s, const EpochArgs& a, const FnCon
   for (int r = warp; r < nre; r += kWarps) {
     const int c = s.list[r];
     const int m = target ? target[c] : c;
-    double* zb = s.z64 + warp * DP;
+    double* zt = s.z64 + warp * 2 * DP;  // trial z, then parent z
+    double* zp = zt + DP;
     // a candidate bit-identical to the member it would replace is a tie in
     // any precision: no re-evaluation needed
     bool same = true;
     for (int j = lane; j < fc.D; j += 32)
       same &= __float_as_uint(s.U[c * DP + j]) == __float_as_uint(s.X[m * DP + j]);
     same = __all_sync(0xFFFFFFFFu, same);
-    double fp = s.fit64[m], ft;
+    double fp = s.fit64[m], ft = 0.0;
+    bool d64;
     if (same) {
       ft = fp;
+      d64 = !strict;
     } else {
-      ft = eval_row_f64(fc, s.U + c * DP, s.o, s.QT, DP, zb);
-      if (isnan(fp)) fp = eval_row_f64(fc, s.X + m * DP, s.o, s.QT, DP, zb);
+      precise_rotation(s.U + c * DP, s.o, s.QT, DP, fc.D, zt);
+      const bool tier2 = fc.fid != F_WEIERSTRASS && fc.fid != F_SPHERE && fc.fid != F_ROSENBROCK;
+      bool decided = false;
+      if (tier2) {
+        // tier 2: FP32 terms on the precise rotation, with error bounds
+        double et, ep = 0.0;
+        const double t2 = eval_tier2(fc, zt, &et);
+        double p2 = fp;
+        if (isnan(fp)) {
+          precise_rotation(s.X + m * DP, s.o, s.QT, DP, fc.D, zp);
+          p2 = eval_tier2(fc, zp, &ep);
+        }
+        if (fabs(t2 - p2) > et + ep) {
+          d64 = strict ? (t2 < p2) : (t2 <= p2);
+          ft = __longlong_as_double(0x7FF8000000000000ll);  // exact values unknown
+          decided = true;
+        }
+      }
+      if (!decided) {
+        // tier 3 (or the exact Weierstrass terms): FP64-class values, cached
+        ft = fc.fid == F_WEIERSTRASS ? eval_weier_precise(fc, zt) : eval_tier3(fc, zt);
+        if (isnan(fp)) {
+          if (!tier2) precise_rotation(s.X + m * DP, s.o, s.QT, DP, fc.D, zp);
+          fp = fc.fid == F_WEIERSTRASS ? eval_weier_precise(fc, zp) : eval_tier3(fc, zp);
+        }
+        d64 = strict ? (ft < fp) : (ft <= fp);
+      }
     }
-    const bool d64 = same ? !strict : (strict ? (ft < fp) : (ft <= fp));
     const bool d32 = strict ? (s.ftr[c] < s.fit[m]) : (s.ftr[c] <= s.fit[m]);
     if (lane == 0) {
       s.flag[c] = d64 ? 3 : 0;

@@ -31,6 +31,7 @@ FLAG_REF_WEIERSTRASS_CONST = 0x2
 FLAG_REF_ACKLEY_E = 0x4
 FLAG_REF_BOXES = 0x8
 FLAG_NO_RECHECK = 0x10
+FLAG_RIGOROUS_WINDOW = 0x20
 MAX_DIM, MAX_POP = 128, 256
 NOALLOC_EXCHANGE_FLOATS = 1 << 19
 

@@ -32,13 +32,14 @@ def test_evaluate_matches_fp64(sgemtf, orc, fid, D, rot):
     for i, x in enumerate(X):
         f64, s, z64 = t.eval64(x)
         assert abs(float(f[i]) - f64) <= tolerance(orc, t, x, s), (i, float(f[i]), f64, s)
-        if t.c.fid != orc.WEIERSTRASS and s > 0:
+        if s > 0:
             worst = max(worst, abs(float(f[i]) - f64) / s)
         # rotation: rigorous FP32 dot-product bound gamma_{D+1} * sum |Q||x - o|
         sa = np.abs(t.Q.astype(np.float64)) @ np.abs(x.astype(np.float64) - t.o)
         g = (D + 1) * 2.0 ** -24 / (1 - (D + 1) * 2.0 ** -24)
         assert np.all(np.abs(z[i] - z64[:D]) <= g * sa + 1e-30)
-    assert worst <= 1e-5
+    # Weierstrass: within its default near-tie half-window, 5e-5 of the scale
+    assert worst <= (5e-5 if fid == orc.WEIERSTRASS else 1e-5)
 
 
 @pytest.mark.parametrize("D", [1, 17, 50])

@@ -33,9 +33,9 @@ def test_tc_fitness_matches_fp64(sgemtf, orc, D, NP):
         for r in range(NP):
             f64, s, _ = t.eval64(X[r])
             assert abs(float(f[r]) - f64) <= tolerance(orc, t, X[r], s), (i, r, float(f[r]), f64)
-            if t.c.fid != orc.WEIERSTRASS and s > 0:
+            if s > 0:
                 worst = max(worst, abs(float(f[r]) - f64) / s)
-        assert worst <= 1e-5
+        assert worst <= (5e-5 if t.c.fid == orc.WEIERSTRASS else 1e-5)
 
 
 @pytest.mark.parametrize("alg", [0, 1, 2])
