@@ -247,6 +247,63 @@ EMT_API int emt_snapshot_size(emt_handle_t* h, size_t* bytes);
 EMT_API int emt_snapshot(emt_handle_t* h, void* buf, size_t bytes);
 EMT_API int emt_restore(emt_handle_t* h, const void* buf, size_t bytes);
 
+/* ---- CVRP multitask engine ------------------------------------------------
+ * One island of giant-tour permutations per instance, decoded into
+ * capacity-feasible routes by the split procedure (Prins 2004; evaluated on
+ * the device in O(n) with Vidal's 2016 deque form); costs are exact int32.  Replaces
+ * the reference's CVRP variant (proposed model/SG-EMTF_cvrp.cu: iter() at
+ * :1487-1607 with per-task params {dimension, cars, customers} at :1496-1500);
+ * that variant is unfinished (its crossover sets every gene to 1, :731-736),
+ * so this engine follows the published methods instead: order crossover,
+ * swap and 2-opt mutation, binary tournaments, elite transfer of whole
+ * permutations between instances with the same customer count. */
+typedef struct emt_cvrp_handle emt_cvrp_handle_t;
+
+#define EMT_CVRP_MAX_CUSTOMERS 255
+
+typedef struct emt_cvrp_config {
+  int32_t pop;               /* island size (2..256)                         */
+  float p_cross;             /* order-crossover probability                  */
+  float p_swap, p_2opt;      /* mutation probabilities                       */
+  int32_t transfer_interval; /* generations between transfers; 0 = off       */
+  float transfer_rate;       /* fraction of the island sent                  */
+  uint64_t seed;
+  int32_t device;
+  int32_t reserved[7];
+} emt_cvrp_config;
+
+typedef struct emt_cvrp_instance {
+  int32_t customers;     /* n, 1..EMT_CVRP_MAX_CUSTOMERS                    */
+  int32_t capacity;
+  const int32_t* x;      /* n + 1 integer coordinates in [0, 40000], node 0 = depot; */
+  const int32_t* y;      /* NULL for all three: uniform on [0, 1000)^2      */
+  const int32_t* demand; /* n + 1 (demand[0] ignored); NULL: uniform 1..10  */
+} emt_cvrp_instance;
+
+EMT_API void emt_cvrp_config_default(emt_cvrp_config* cfg);
+EMT_API int emt_cvrp_create(const emt_cvrp_config* cfg, emt_cvrp_handle_t** out);
+/* Distances are rounded Euclidean, round(sqrt(dx^2 + dy^2)) in integers. */
+EMT_API int emt_cvrp_add_instances(emt_cvrp_handle_t* h, int32_t n, const emt_cvrp_instance* inst);
+EMT_API int emt_cvrp_reset(emt_cvrp_handle_t* h, void* stream);
+EMT_API int emt_cvrp_run(emt_cvrp_handle_t* h, int32_t generations, void* stream);
+EMT_API int emt_cvrp_sync(emt_cvrp_handle_t* h);
+/* Best cost of every instance (n_instances int32). */
+EMT_API int emt_cvrp_get_best_all(emt_cvrp_handle_t* h, int32_t* costs);
+/* One island: pop * customers bytes (customer ids 1..n), pop int32 costs. */
+EMT_API int emt_cvrp_get_population(emt_cvrp_handle_t* h, int32_t inst, uint8_t* perms,
+                                    int32_t* costs);
+/* The instance as the device holds it: n + 1 x, y, demand; (n + 1)^2 distances. */
+EMT_API int emt_cvrp_get_instance(emt_cvrp_handle_t* h, int32_t inst, int32_t* x, int32_t* y,
+                                  int32_t* demand, int32_t* dist);
+/* Cost of `count` caller-given giant tours of instance `inst` (count *
+ * customers bytes, each a permutation of 1..n; anything else is rejected),
+ * decoded on the device by the same split as the engine.  Blocking. */
+EMT_API int emt_cvrp_evaluate(emt_cvrp_handle_t* h, int32_t inst, int32_t count,
+                              const uint8_t* perms, int32_t* costs);
+EMT_API int emt_cvrp_get_stats(emt_cvrp_handle_t* h, emt_stats* out);
+EMT_API const char* emt_cvrp_last_error(const emt_cvrp_handle_t* h);
+EMT_API void emt_cvrp_destroy(emt_cvrp_handle_t* h);
+
 EMT_API const char* emt_last_error(const emt_handle_t* h);
 EMT_API const char* emt_status_string(int status);
 EMT_API void emt_destroy(emt_handle_t* h);

@@ -59,7 +59,15 @@ enum { ORC_DE_RAND1 = 0, ORC_DE_CURRENT1 = 1, ORC_GA = 2 };
 enum {
   ORC_P_POP_INIT = 1, ORC_P_SHIFT = 2, ORC_P_QR_NORMAL = 3, ORC_P_DE_INDEX = 4,
   ORC_P_DE_CR = 5, ORC_P_GA_PARENT = 6, ORC_P_GA_SBX = 7, ORC_P_GA_PM = 8,
-  ORC_P_TRANSFER_PARTNER = 9, ORC_P_TRANSFER_MIX = 10
+  ORC_P_TRANSFER_PARTNER = 9, ORC_P_TRANSFER_MIX = 10,
+  /* CVRP (emt_cvrp_oracle.c) */
+  ORC_P_CVRP_NODE = 16,     /* gen 0, member = node, block 0 -> x, y, demand   */
+  ORC_P_CVRP_POP_INIT = 17, /* gen 0, member i, block b -> Fisher-Yates words  */
+  ORC_P_CVRP_SELECT = 18,   /* gen g, member i -> two binary tournaments       */
+  ORC_P_CVRP_OX = 19,       /* gen g, member i -> (p_cross, cut1, cut2, -)     */
+  ORC_P_CVRP_MUTATE = 20,   /* gen g, member i, block 0 -> (p_swap, s1, s2, p_2opt),
+                               block 1 -> (r1, r2, -, -)                      */
+  ORC_P_CVRP_PARTNER = 21   /* gen g, member 0 -> transfer partner            */
 };
 
 void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
@@ -136,6 +144,29 @@ int orc_transfer_in(const orc_params* p, const orc_task* t, const orc_task* part
 double orc_run_threads(const orc_params* p, const orc_task* tasks, int n, float** X,
                        float** fit32, double** fit64, uint32_t gen0, int gens, int mode,
                        int threads);
+
+/* ---- CVRP (emt_cvrp_oracle.c) ---- */
+typedef struct orc_cvrp_params {
+  uint64_t seed;
+  float p_cross, p_swap, p_2opt;
+} orc_cvrp_params;
+
+uint32_t orc_cvrp_round_sqrt(uint64_t v);
+void orc_cvrp_gen_instance(uint64_t seed, uint32_t inst, int n, int32_t* x, int32_t* y,
+                           int32_t* demand);
+void orc_cvrp_distances(int n, const int32_t* x, const int32_t* y, int32_t* dist);
+int32_t orc_cvrp_split(int n, const int32_t* dist, const int32_t* demand, int32_t capacity,
+                       const uint8_t* perm, int32_t* pred);
+void orc_cvrp_child(const orc_cvrp_params* p, uint32_t inst, int n, int NP, const uint8_t* pop,
+                    const int32_t* cost, uint32_t g, int i, uint8_t* child);
+void orc_cvrp_init_population(uint64_t seed, uint32_t inst, int n, int NP, uint8_t* pop);
+int orc_cvrp_generation(const orc_cvrp_params* p, uint32_t inst, int n, int NP,
+                        const int32_t* dist, const int32_t* demand, int32_t capacity,
+                        uint8_t* pop, int32_t* cost, uint32_t g);
+void orc_cvrp_rank(const int32_t* cost, int NP, int* byrank);
+int orc_cvrp_transfer_in(int n, int NP, const int32_t* dist, const int32_t* demand,
+                         int32_t capacity, const uint8_t* elites, int k, uint8_t* pop,
+                         int32_t* cost);
 
 #ifdef __cplusplus
 }

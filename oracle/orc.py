@@ -26,6 +26,7 @@ FLAG_RIGOROUS_WINDOW = 0x20
 
 P_POP_INIT, P_SHIFT, P_QR_NORMAL, P_DE_INDEX, P_DE_CR = 1, 2, 3, 4, 5
 P_GA_PARENT, P_GA_SBX, P_GA_PM, P_TRANSFER_PARTNER, P_TRANSFER_MIX = 6, 7, 8, 9, 10
+P_CVRP_NODE, P_CVRP_POP_INIT, P_CVRP_SELECT, P_CVRP_OX, P_CVRP_MUTATE, P_CVRP_PARTNER = range(16, 22)
 
 _F32P = ctypes.POINTER(ctypes.c_float)
 _F64P = ctypes.POINTER(ctypes.c_double)
@@ -44,6 +45,11 @@ class Params(ctypes.Structure):
                 ("p_m", ctypes.c_float), ("transfer_mix", ctypes.c_float),
                 ("seed", ctypes.c_uint64), ("recheck_rel", ctypes.c_double),
                 ("flags", ctypes.c_uint32)]
+
+
+class CvrpParams(ctypes.Structure):
+    _fields_ = [("seed", ctypes.c_uint64), ("p_cross", ctypes.c_float), ("p_swap", ctypes.c_float),
+                ("p_2opt", ctypes.c_float)]
 
 
 def build(quiet=True):
@@ -101,6 +107,26 @@ def lib():
                                       ctypes.POINTER(_F64P), ctypes.c_uint32, ctypes.c_int,
                                       ctypes.c_int, ctypes.c_int]
         L.orc_box.argtypes = [ctypes.c_int, ctypes.c_int, _F32P, _F32P]
+        I32P = ctypes.POINTER(ctypes.c_int32)
+        L.orc_cvrp_round_sqrt.restype = ctypes.c_uint32
+        L.orc_cvrp_round_sqrt.argtypes = [ctypes.c_uint64]
+        L.orc_cvrp_gen_instance.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int, I32P,
+                                            I32P, I32P]
+        L.orc_cvrp_distances.argtypes = [ctypes.c_int, I32P, I32P, I32P]
+        L.orc_cvrp_split.restype = ctypes.c_int32
+        L.orc_cvrp_split.argtypes = [ctypes.c_int, I32P, I32P, ctypes.c_int32, _U8P, I32P]
+        L.orc_cvrp_child.argtypes = [ctypes.POINTER(CvrpParams), ctypes.c_uint32, ctypes.c_int,
+                                     ctypes.c_int, _U8P, I32P, ctypes.c_uint32, ctypes.c_int, _U8P]
+        L.orc_cvrp_init_population.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int,
+                                               ctypes.c_int, _U8P]
+        L.orc_cvrp_generation.restype = ctypes.c_int
+        L.orc_cvrp_generation.argtypes = [ctypes.POINTER(CvrpParams), ctypes.c_uint32, ctypes.c_int,
+                                          ctypes.c_int, I32P, I32P, ctypes.c_int32, _U8P, I32P,
+                                          ctypes.c_uint32]
+        L.orc_cvrp_rank.argtypes = [I32P, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+        L.orc_cvrp_transfer_in.restype = ctypes.c_int
+        L.orc_cvrp_transfer_in.argtypes = [ctypes.c_int, ctypes.c_int, I32P, I32P, ctypes.c_int32,
+                                           _U8P, ctypes.c_int, _U8P, I32P]
         _lib = L
     return _lib
 
@@ -228,3 +254,123 @@ def run_threads(p, tasks, X, fit32, fit64, gen0, gens, mode, threads):
     fp = (_F32P * n)(*[_p32(a) for a in fit32])
     dp = (_F64P * n)(*[_p64(a) for a in fit64])
     return lib().orc_run_threads(ctypes.byref(p), arr, n, xp, fp, dp, gen0, gens, mode, threads)
+
+
+# ---- CVRP ----
+def _i32(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+
+
+def _u8(a):
+    return a.ctypes.data_as(_U8P)
+
+
+class CvrpInstance:
+    """One seeded CVRP instance: coordinates, demands, rounded-Euclidean
+    distances, capacity."""
+
+    def __init__(self, seed, inst, n=100, capacity=50, x=None, y=None, demand=None):
+        self.n, self.capacity, self.inst = n, capacity, inst
+        if x is None:
+            self.x = np.zeros(n + 1, np.int32)
+            self.y = np.zeros(n + 1, np.int32)
+            self.demand = np.zeros(n + 1, np.int32)
+            lib().orc_cvrp_gen_instance(seed, inst, n, _i32(self.x), _i32(self.y), _i32(self.demand))
+        else:
+            self.x = np.ascontiguousarray(x, np.int32)
+            self.y = np.ascontiguousarray(y, np.int32)
+            self.demand = np.ascontiguousarray(demand, np.int32)
+        self.dist = np.zeros((n + 1) * (n + 1), np.int32)
+        lib().orc_cvrp_distances(n, _i32(self.x), _i32(self.y), _i32(self.dist))
+
+    def split(self, perm, with_pred=False):
+        perm = np.ascontiguousarray(perm, np.uint8)
+        pred = np.zeros(self.n + 1, np.int32)
+        c = lib().orc_cvrp_split(self.n, _i32(self.dist), _i32(self.demand), self.capacity,
+                                 _u8(perm), _i32(pred))
+        return (c, pred) if with_pred else c
+
+
+def cvrp_params(seed=1, p_cross=0.9, p_swap=0.2, p_2opt=0.2):
+    return CvrpParams(seed, p_cross, p_swap, p_2opt)
+
+
+def cvrp_init_population(seed, inst, n, NP):
+    pop = np.zeros((NP, n), np.uint8)
+    lib().orc_cvrp_init_population(seed, inst, n, NP, _u8(pop))
+    return pop
+
+
+def cvrp_generation(p, ins, pop, cost, g):
+    NP = pop.shape[0]
+    return lib().orc_cvrp_generation(ctypes.byref(p), ins.inst, ins.n, NP, _i32(ins.dist),
+                                     _i32(ins.demand), ins.capacity, _u8(pop), _i32(cost), g)
+
+
+def cvrp_rank(cost):
+    cost = np.ascontiguousarray(cost, np.int32)
+    r = np.zeros(len(cost), np.int32)
+    lib().orc_cvrp_rank(_i32(cost), len(cost), r.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    return r
+
+
+def cvrp_transfer_in(ins, elites, pop, cost):
+    elites = np.ascontiguousarray(elites, np.uint8)
+    return lib().orc_cvrp_transfer_in(ins.n, pop.shape[0], _i32(ins.dist), _i32(ins.demand),
+                                      ins.capacity, _u8(elites), elites.shape[0], _u8(pop),
+                                      _i32(cost))
+
+
+def cvrp_transfer_k(rate, NP):
+    k = int(np.float32(np.float32(rate) * np.float32(NP)) + np.float32(0.5))
+    return max(1, min(NP, k))
+
+
+def cvrp_partner(seed, t, n_inst, gen):
+    """Partner instance of instance t for the transfer at generation gen."""
+    p = int(draw(seed, t, gen, 0, P_CVRP_PARTNER, 0)[0]) % (n_inst - 1)
+    return p + 1 if p >= t else p
+
+
+class CvrpReplay:
+    """Host replay of the CVRP engine's schedule: generations with elite
+    transfer every `interval` generations (exported at the end of the epoch
+    that closes an interval, imported at the start of the next epoch)."""
+
+    def __init__(self, seed, instances, NP, p_cross=0.9, p_swap=0.2, p_2opt=0.2,
+                 interval=0, rate=0.1):
+        self.p = cvrp_params(seed, p_cross, p_swap, p_2opt)
+        self.seed, self.ins, self.NP = seed, instances, NP
+        self.interval = interval if len(instances) > 1 else 0
+        self.rate = rate
+        self.pop = [cvrp_init_population(seed, t, ins.n, NP) for t, ins in enumerate(instances)]
+        self.cost = [np.array([ins.split(r) for r in pop], np.int32)
+                     for ins, pop in zip(instances, self.pop)]
+        self.gen = 0
+        self.elites = None
+        self.accepted = 0
+
+    def _export(self):
+        k = cvrp_transfer_k(self.rate, self.NP)
+        return [pop[cvrp_rank(cost)[:k]].copy() for pop, cost in zip(self.pop, self.cost)]
+
+    def run(self, gens):
+        left = gens
+        T = len(self.ins)
+        while left > 0:
+            g = left
+            if self.interval:
+                if self.gen > 0 and self.gen % self.interval == 0 and self.elites is not None:
+                    for t in range(T):
+                        pt = cvrp_partner(self.seed, t, T, self.gen)
+                        if self.ins[pt].n == self.ins[t].n:
+                            self.accepted += cvrp_transfer_in(self.ins[t], self.elites[pt],
+                                                              self.pop[t], self.cost[t])
+                g = min(left, self.interval - self.gen % self.interval)
+            for t in range(T):
+                for k in range(1, g + 1):
+                    cvrp_generation(self.p, self.ins[t], self.pop[t], self.cost[t], self.gen + k)
+            self.gen += g
+            left -= g
+            if self.interval and self.gen % self.interval == 0:
+                self.elites = self._export()

@@ -3,9 +3,10 @@
 // FP32 power used by the GA operators, and small helpers.
 //
 // Everything here is written so that host and device produce identical bits:
-// every intended fused multiply-add is an explicit fmaf()/__fmaf_rn, and the
-// library is compiled with --fmad=false for host code and explicit intrinsics
-// for device code on the trial path.
+// every intended fused multiply-add is an explicit fmaf()/__fmaf_rn, host code
+// is compiled with -ffp-contract=off, and device code on the trial path uses
+// explicitly rounded intrinsics (__fadd_rn, __fmul_rn, ...), which the
+// compiler never contracts.
 #pragma once
 
 #include <cstdint>
@@ -38,7 +39,9 @@ enum Purpose : uint32_t {
   P_GA_SBX = 7,           // gen g, member i, block b -> (rate, p) for genes 2b, 2b+1
   P_GA_PM = 8,            // gen g, member i, block b -> (r, u) for genes 2b, 2b+1
   P_TRANSFER_PARTNER = 9, // gen g, member 0, block 0 -> partner task
-  P_TRANSFER_MIX = 10     // gen g, member c, block b -> genes 4b..4b+3 of candidate c
+  P_TRANSFER_MIX = 10,    // gen g, member c, block b -> genes 4b..4b+3 of candidate c
+  // CVRP engine (emt_cvrp.cu): node data, Fisher-Yates words, tournaments,
+  // order-crossover cuts, mutation draws, transfer partner (purposes 16..21)
 };
 
 struct U4 {

@@ -41,6 +41,9 @@ EXPORTED = [
     "emt_get_population", "emt_set_population", "emt_get_task_params", "emt_evaluate",
     "emt_get_stats", "emt_snapshot_size", "emt_snapshot", "emt_restore", "emt_last_error",
     "emt_status_string", "emt_destroy",
+    "emt_cvrp_config_default", "emt_cvrp_create", "emt_cvrp_add_instances", "emt_cvrp_reset",
+    "emt_cvrp_run", "emt_cvrp_sync", "emt_cvrp_get_best_all", "emt_cvrp_get_population",
+    "emt_cvrp_get_instance", "emt_cvrp_evaluate", "emt_cvrp_get_stats", "emt_cvrp_last_error", "emt_cvrp_destroy",
 ]
 
 
@@ -97,6 +100,27 @@ class TaskDesc:
                          ptr(self.shift, ctypes.c_float))
 
 
+class CvrpConfig(ctypes.Structure):
+    _fields_ = [("pop", ctypes.c_int32), ("p_cross", ctypes.c_float), ("p_swap", ctypes.c_float),
+                ("p_2opt", ctypes.c_float), ("transfer_interval", ctypes.c_int32),
+                ("transfer_rate", ctypes.c_float), ("seed", ctypes.c_uint64),
+                ("device", ctypes.c_int32), ("reserved", ctypes.c_int32 * 7)]
+
+    def __init__(self, **kw):
+        super().__init__()
+        lib().emt_cvrp_config_default(ctypes.byref(self))
+        for k, v in kw.items():
+            if not hasattr(self, k):
+                raise AttributeError(k)
+            setattr(self, k, v)
+
+
+class CvrpInstanceC(ctypes.Structure):
+    _fields_ = [("customers", ctypes.c_int32), ("capacity", ctypes.c_int32),
+                ("x", ctypes.POINTER(ctypes.c_int32)), ("y", ctypes.POINTER(ctypes.c_int32)),
+                ("demand", ctypes.POINTER(ctypes.c_int32))]
+
+
 class EngineError(RuntimeError):
     def __init__(self, status, message):
         super().__init__("%s (%d): %s" % (status_string(status), status, message))
@@ -145,6 +169,24 @@ def lib():
         L.emt_status_string.restype = ctypes.c_char_p
         L.emt_destroy.argtypes = [vp]
         L.emt_destroy.restype = None
+        i32p = ctypes.POINTER(ctypes.c_int32)
+        u8p = ctypes.POINTER(ctypes.c_uint8)
+        L.emt_cvrp_config_default.argtypes = [ctypes.POINTER(CvrpConfig)]
+        L.emt_cvrp_config_default.restype = None
+        L.emt_cvrp_create.argtypes = [ctypes.POINTER(CvrpConfig), ctypes.POINTER(vp)]
+        L.emt_cvrp_add_instances.argtypes = [vp, i32, ctypes.POINTER(CvrpInstanceC)]
+        L.emt_cvrp_reset.argtypes = [vp, vp]
+        L.emt_cvrp_run.argtypes = [vp, i32, vp]
+        L.emt_cvrp_sync.argtypes = [vp]
+        L.emt_cvrp_get_best_all.argtypes = [vp, i32p]
+        L.emt_cvrp_get_population.argtypes = [vp, i32, u8p, i32p]
+        L.emt_cvrp_get_instance.argtypes = [vp, i32, i32p, i32p, i32p, i32p]
+        L.emt_cvrp_evaluate.argtypes = [vp, i32, i32, u8p, i32p]
+        L.emt_cvrp_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
+        L.emt_cvrp_last_error.argtypes = [vp]
+        L.emt_cvrp_last_error.restype = ctypes.c_char_p
+        L.emt_cvrp_destroy.argtypes = [vp]
+        L.emt_cvrp_destroy.restype = None
         _lib = L
     return _lib
 
@@ -280,3 +322,96 @@ class Engine:
 
     def __exit__(self, *a):
         self.close()
+
+
+class CvrpEngine:
+    """One emt_cvrp_handle: CVRP instances, one island of permutations each."""
+
+    def __init__(self, config=None, **kw):
+        self.config = config if config is not None else CvrpConfig(**kw)
+        self._h = ctypes.c_void_p()
+        rc = lib().emt_cvrp_create(ctypes.byref(self.config), ctypes.byref(self._h))
+        if rc:
+            raise EngineError(rc, "emt_cvrp_create")
+        self.sizes = []
+
+    def _check(self, rc, what):
+        if rc:
+            raise EngineError(rc, "%s: %s" % (what, lib().emt_cvrp_last_error(self._h).decode()))
+
+    def add_instances(self, specs):
+        """specs: (customers, capacity) for seeded instances, or
+        (customers, capacity, x, y, demand) with n + 1 entries each."""
+        keep, arr = [], []
+        for sp in specs:
+            n, cap = int(sp[0]), int(sp[1])
+            if len(sp) > 2:
+                x, y, d = (np.ascontiguousarray(a, np.int32) for a in sp[2:5])
+                keep += [x, y, d]
+                p = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+                arr.append(CvrpInstanceC(n, cap, p(x), p(y), p(d)))
+            else:
+                arr.append(CvrpInstanceC(n, cap, None, None, None))
+        carr = (CvrpInstanceC * len(arr))(*arr)
+        self._check(lib().emt_cvrp_add_instances(self._h, len(arr), carr), "emt_cvrp_add_instances")
+        self.sizes += [int(sp[0]) for sp in specs]
+
+    def reset(self, stream=None):
+        self._check(lib().emt_cvrp_reset(self._h, stream), "emt_cvrp_reset")
+
+    def run(self, generations, stream=None, sync=True):
+        self._check(lib().emt_cvrp_run(self._h, int(generations), stream), "emt_cvrp_run")
+        if sync:
+            self.sync()
+
+    def sync(self):
+        self._check(lib().emt_cvrp_sync(self._h), "emt_cvrp_sync")
+
+    def population(self, inst):
+        n = self.sizes[inst] if 0 <= inst < len(self.sizes) else 1
+        perms = np.zeros((self.config.pop, n), np.uint8)
+        costs = np.zeros(self.config.pop, np.int32)
+        self._check(lib().emt_cvrp_get_population(
+            self._h, inst, perms.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
+            costs.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))), "emt_cvrp_get_population")
+        return perms, costs
+
+    def best_all(self):
+        out = np.zeros(len(self.sizes), np.int32)
+        self._check(lib().emt_cvrp_get_best_all(self._h, out.ctypes.data_as(
+            ctypes.POINTER(ctypes.c_int32))), "emt_cvrp_get_best_all")
+        return out
+
+    def instance(self, inst):
+        n = self.sizes[inst]
+        x, y, d = (np.zeros(n + 1, np.int32) for _ in range(3))
+        dist = np.zeros((n + 1) * (n + 1), np.int32)
+        p = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+        self._check(lib().emt_cvrp_get_instance(self._h, inst, p(x), p(y), p(d), p(dist)),
+                    "emt_cvrp_get_instance")
+        return x, y, d, dist
+
+    def evaluate(self, inst, perms):
+        """Device costs of giant tours (rows of customer ids 1..n)."""
+        perms = np.ascontiguousarray(perms, np.uint8)
+        out = np.zeros(perms.shape[0], np.int32)
+        self._check(lib().emt_cvrp_evaluate(
+            self._h, inst, perms.shape[0], perms.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
+            out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))), "emt_cvrp_evaluate")
+        return out
+
+    def stats(self):
+        st = Stats()
+        self._check(lib().emt_cvrp_get_stats(self._h, ctypes.byref(st)), "emt_cvrp_get_stats")
+        return {k: getattr(st, k) for k, _ in Stats._fields_}
+
+    def close(self):
+        if self._h:
+            lib().emt_cvrp_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
