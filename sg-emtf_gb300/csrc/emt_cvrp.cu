@@ -18,8 +18,10 @@
 // host replay bit for bit.
 //
 // Kernel layout: one CTA per instance, one thread per member; shared memory
-// holds the distance matrix (uint16), demands, the island, the children and
-// each thread's split labels.
+// holds the node table {x, y, distance to depot, demand}, the island and its
+// children, and each thread's split deque.  Distances between customers are
+// recomputed exactly from the integer coordinates where the split needs them
+// (no (n+1)^2 matrix on the device), which keeps three CTAs per SM.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -27,6 +29,7 @@
 #include <cstring>
 #include <new>
 #include <numeric>
+#include <type_traits>
 #include <string>
 #include <vector>
 
@@ -42,8 +45,7 @@ enum : uint32_t {
 
 struct InstDev {
   int32_t n, capacity;
-  int64_t dist_off;  // uint16 entries, (n+1)^2
-  int64_t dem_off;   // int32, n+1
+  int64_t node_off;  // int4 {x, y, d0, demand}, n+1 entries
   int64_t pop_off;   // uint8, NP*n
   int32_t cost_off;  // int32, NP
   int32_t pad;
@@ -53,9 +55,9 @@ struct InstDev {
 struct Args {
   const InstDev* inst;
   int32_t n_inst, NP, gens, mode;  // mode: 0 epoch, 1 init
-  int32_t ring_mask;               // deque slots per thread - 1 (a power of two - 1)
-  const uint16_t* dist;
-  const int32_t* demand;
+  int32_t ring;                    // deque slots per thread (a multiple of 4)
+  int32_t used_words;              // words of the per-thread crossover bitmap
+  const int4* node;
   uint8_t* pop;
   int32_t* cost;
   uint32_t* gen;
@@ -72,44 +74,90 @@ struct Args {
 __host__ __device__ inline size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
 
 // Shared memory of one instance's CTA (P = threads of the block, R = deque
-// slots per thread).  Per-thread arrays are interleaved [slot][thread] so
-// that a warp's accesses fall in 32 distinct banks whatever slot each lane
-// is at.  Member i's tour lives in pool row (cur[i] * P + i); its child is
-// built in the other row and accepted by flipping cur[i].
+// slots per thread, QB = bytes of a stored demand prefix, UW = bitmap words).
+// Per-thread arrays are interleaved [slot][thread] so that a warp's accesses
+// fall in 32 distinct banks whatever slot each lane is at (sub-word demand
+// prefixes: each lane owns one word per 4 / QB slots).  Member i's tour lives
+// in pool row (cur[i] * P + i); its child is built in the other row and
+// accepted by flipping cur[i].  The rank list shares the child-cost array:
+// ranks are only needed outside the generation loop.
 struct Layout {
-  size_t dist, node, pool, cost, kcost, cur, used, rank, ringA, ringQ, total;
+  size_t node, pool, cost, kcost, cur, used, ringA, ringQ, total;
 };
 
-__host__ __device__ inline Layout layout(int n, int P, int R) {
+__host__ __device__ inline Layout layout(int n, int P, int R, int QB, int UW) {
   Layout L;
   size_t off = 0;
-  L.dist = off;  off = align16(off + sizeof(uint16_t) * (n + 1) * (n + 1));
-  L.node = off;  off = align16(off + sizeof(int2) * (n + 1));  // {distance to depot, demand}
+  L.node = off;  off = align16(off + sizeof(int4) * (n + 1));
   L.pool = off;  off = align16(off + (size_t)2 * P * n);
   L.cost = off;  off = align16(off + sizeof(int32_t) * P);
   L.kcost = off; off = align16(off + sizeof(int32_t) * P);
   L.cur = off;   off = align16(off + (size_t)P);
-  L.used = off;  off = align16(off + sizeof(uint32_t) * 8 * P);  // 256-bit set per thread
-  L.rank = off;  off = align16(off + sizeof(int32_t) * P);
+  L.used = off;  off = align16(off + sizeof(uint32_t) * (size_t)UW * P);
   L.ringA = off; off = align16(off + sizeof(int32_t) * (size_t)R * P);
-  L.ringQ = off; off = align16(off + sizeof(int32_t) * (size_t)R * P);
+  L.ringQ = off; off = align16(off + (size_t)QB * R * P);
   L.total = off;
   return L;
 }
 
 // The evaluation kernel's shared memory: the instance and the deque rings only.
-__host__ __device__ inline Layout eval_layout(int n, int P, int R) {
+__host__ __device__ inline Layout eval_layout(int n, int P, int R, int QB) {
   Layout L{};
   size_t off = 0;
-  L.dist = off;  off = align16(off + sizeof(uint16_t) * (n + 1) * (n + 1));
-  L.node = off;  off = align16(off + sizeof(int2) * (n + 1));
+  L.node = off;  off = align16(off + sizeof(int4) * (n + 1));
   L.ringA = off; off = align16(off + sizeof(int32_t) * (size_t)R * P);
-  L.ringQ = off; off = align16(off + sizeof(int32_t) * (size_t)R * P);
+  L.ringQ = off; off = align16(off + (size_t)QB * R * P);
   L.total = off;
   return L;
 }
 
+// Demand prefixes Q_i in the deque, stored in QB bytes.  Every difference
+// the split tests, Q_j - Q_i for i in the deque, lies in [0, 2 * capacity]
+// (the entry was inside the previous window, plus one demand), so storing Q_i
+// modulo 2^(8 QB) and masking the difference is exact when 2 * capacity <
+// 2^(8 QB).  The host picks QB from the largest capacity.
+template <int QB>
+struct QRing {
+  using T = typename std::conditional<QB == 1, uint8_t,
+            typename std::conditional<QB == 2, uint16_t, int32_t>::type>::type;
+  T* base;  // this lane's first element
+  int P;
+  __device__ __forceinline__ QRing(unsigned char* region, int lane, int P_) : P(P_) {
+    base = (T*)region + lane * (4 / QB);
+  }
+  __device__ __forceinline__ int idx(int slot) const {
+    return QB == 4 ? slot * P : (slot / (4 / QB)) * (4 / QB) * P + (slot % (4 / QB));
+  }
+  __device__ __forceinline__ void put(int slot, int32_t q) { base[idx(slot)] = (T)q; }
+  __device__ __forceinline__ int32_t get(int slot) const { return (int32_t)base[idx(slot)]; }
+  // Q - stored, exact under the capacity bound above
+  static __device__ __forceinline__ int32_t gap(int32_t Q, int32_t stored) {
+    return QB == 4 ? Q - stored : (int32_t)((uint32_t)(Q - stored) & ((1u << (8 * QB)) - 1u));
+  }
+};
+
 constexpr int kMaxN = 255;
+
+// Rounded Euclidean distance round(sqrt(dx^2 + dy^2)) of integer points
+// with coordinates in [0, 40000], exact: r0 = trunc(sqrt(v)) from a floating
+// square root (within 1 of floor(sqrt(v)) for v < 2^32: relative error below
+// 2^-21 on values below 2^16), one integer correction each way, then
+// sqrt(v) < r + 1/2 <=> v <= r^2 + r.  Host and device give the same bits.
+EMT_HD uint32_t round_dist(int32_t x0, int32_t y0, int32_t x1, int32_t y1) {
+  const int32_t dx = x0 - x1, dy = y0 - y1;
+  const uint32_t v = (uint32_t)(dx * dx) + (uint32_t)(dy * dy);  // <= 3.2e9
+#if defined(__CUDA_ARCH__)
+  const float f = (float)v;
+  uint32_t r = v ? (uint32_t)(f * rsqrtf(f)) : 0u;
+#else
+  uint32_t r = (uint32_t)std::sqrt((double)v);
+#endif
+  if (r * r > v)
+    --r;
+  else if ((r + 1u) * (r + 1u) <= v)
+    ++r;
+  return v <= r * r + r ? r : r + 1u;
+}
 
 // Split of one giant tour p_0..p_{n-1} into capacity-feasible routes, the
 // shortest-path procedure of Prins (Comput. Oper. Res. 31, 2004) evaluated in
@@ -119,41 +167,47 @@ constexpr int kMaxN = 255;
 //   V_j = S_{j-1} + d0(p_{j-1}) + min { A_i : i < j, Q_j - Q_i <= capacity },
 //   A_i = V_i + d0(p_i) - S_i.
 // The deque holds candidate i in increasing i and increasing A_i; its front
-// is the minimum.  All integer, so V_n equals the O(n L) label-correcting
-// form exactly.  Every window holds at most Lmax + 1 entries (Lmax = most
-// customers one route can serve), which the ring of mask + 1 slots covers;
-// rA/rQ point at this thread's slot 0, slots P apart.
-__device__ __forceinline__ int32_t split_linear(int n, const uint16_t* __restrict__ dist,
-                                                const int2* __restrict__ node, int32_t capacity,
-                                                const uint8_t* __restrict__ perm,
-                                                int32_t* __restrict__ rA, int32_t* __restrict__ rQ,
-                                                int P, int mask) {
-  const int W = n + 1;
-  int head = 0, tail = 0;
+// is the minimum, kept in registers.  All integer, so V_n equals the
+// label-correcting form exactly.  A window holds at most Lmax + 1 entries
+// (Lmax = most customers one route can serve), which the R-slot ring covers;
+// rA points at this thread's slot 0, slots P apart.
+template <int QB>
+__device__ __forceinline__ int32_t split_linear(int n, const int4* __restrict__ node,
+                                                int32_t capacity, const uint8_t* __restrict__ perm,
+                                                int32_t* __restrict__ rA, QRing<QB> rQ, int P,
+                                                int R) {
+  int head = 0, tail = 0, cnt = 0;  // ring positions in [0, R), entries head .. tail - 1
   int32_t V = 0, S = 0, Q = 0, fA = 0, fQ = 0;
-  int prev = 0;
+  int32_t px = 0, py = 0;
   for (int j = 1; j <= n; ++j) {
-    const int c = perm[j - 1];
-    const int2 nd = node[c];
-    if (j > 1) S += (int32_t)dist[prev * W + c];
-    const int32_t A = V + nd.x - S;
-    while (tail > head && rA[((tail - 1) & mask) * P] >= A) --tail;
-    if (tail == head) {
+    const int4 nd = node[perm[j - 1]];  // x, y, d0, demand
+    if (j > 1) S += (int32_t)round_dist(px, py, nd.x, nd.y);
+    px = nd.x;
+    py = nd.y;
+    const int32_t A = V + nd.z - S;
+    while (cnt > 0) {
+      const int b = tail == 0 ? R - 1 : tail - 1;
+      if (rA[b * P] < A) break;
+      tail = b;
+      --cnt;
+    }
+    if (cnt == 0) {
       fA = A;
       fQ = Q;
     }
-    rA[(tail & mask) * P] = A;
-    rQ[(tail & mask) * P] = Q;
-    ++tail;
-    Q += nd.y;
+    rA[tail * P] = A;
+    rQ.put(tail, Q);
+    tail = tail + 1 == R ? 0 : tail + 1;
+    ++cnt;
+    Q += nd.w;
     // the newest candidate (i = j - 1) always fits: q(p_{j-1}) <= capacity
-    while (Q - fQ > capacity && head + 1 < tail) {
-      ++head;
-      fA = rA[(head & mask) * P];
-      fQ = rQ[(head & mask) * P];
+    while (QRing<QB>::gap(Q, fQ) > capacity && cnt > 1) {
+      head = head + 1 == R ? 0 : head + 1;
+      --cnt;
+      fA = rA[head * P];
+      fQ = rQ.get(head);
     }
-    V = S + nd.x + fA;
-    prev = c;
+    V = S + nd.z + fA;
   }
   return V;
 }
@@ -177,15 +231,12 @@ __device__ void rank_members(const int32_t* cost, int NP, int32_t* byrank) {
   __syncthreads();
 }
 
-// Instance data into shared memory: distances and the {d0, demand} node table.
-__device__ void load_instance(const Args& a, const InstDev& d, uint16_t* dist, int2* node) {
-  const int W = d.n + 1;
-  const uint16_t* gd = a.dist + d.dist_off;
-  for (int it = threadIdx.x; it < W * W; it += blockDim.x) dist[it] = gd[it];
-  for (int it = threadIdx.x; it < W; it += blockDim.x)
-    node[it] = make_int2((int32_t)gd[it], a.demand[d.dem_off + it]);
+// The instance's node table into shared memory.
+__device__ void load_instance(const Args& a, const InstDev& d, int4* node) {
+  for (int it = threadIdx.x; it <= d.n; it += blockDim.x) node[it] = a.node[d.node_off + it];
 }
 
+template <int QB>
 __global__ void __launch_bounds__(256) cvrp_epoch_kernel(const Args a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int t = blockIdx.x;
@@ -196,25 +247,24 @@ __global__ void __launch_bounds__(256) cvrp_epoch_kernel(const Args a) {
     if (threadIdx.x == 0) report(a.err, 1);
     return;
   }
-  const Layout L = layout(n, P, a.ring_mask + 1);
-  if (L.total > a.smem_bytes) {
+  const Layout L = layout(n, P, a.ring, QB, a.used_words);
+  if (L.total > a.smem_bytes || n >= 32 * a.used_words) {
     if (threadIdx.x == 0) report(a.err, 2);
     return;
   }
-  uint16_t* dist = (uint16_t*)(smem + L.dist);
-  int2* node = (int2*)(smem + L.node);
+  int4* node = (int4*)(smem + L.node);
   uint8_t* pool = smem + L.pool;
   int32_t* cost = (int32_t*)(smem + L.cost);
   int32_t* kcost = (int32_t*)(smem + L.kcost);
   uint8_t* cur = smem + L.cur;
   uint32_t* used = (uint32_t*)(smem + L.used) + threadIdx.x;
-  int32_t* byrank = (int32_t*)(smem + L.rank);
+  int32_t* byrank = kcost;
   int32_t* rA = (int32_t*)(smem + L.ringA) + threadIdx.x;
-  int32_t* rQ = (int32_t*)(smem + L.ringQ) + threadIdx.x;
-  const int mask = a.ring_mask;
+  const QRing<QB> rQ(smem + L.ringQ, threadIdx.x, P);
+  const int R = a.ring, UW = a.used_words;
   auto row = [&](int m, int s) { return pool + (size_t)(s * P + m) * n; };
 
-  load_instance(a, d, dist, node);
+  load_instance(a, d, node);
   const int i = threadIdx.x;
   uint8_t* gpop = a.pop + d.pop_off;
   if (a.mode == 1) {
@@ -232,7 +282,7 @@ __global__ void __launch_bounds__(256) cvrp_epoch_kernel(const Args a) {
       }
     }
     __syncthreads();
-    if (i < NP) cost[i] = split_linear(n, dist, node, d.capacity, row(i, 0), rA, rQ, P, mask);
+    if (i < NP) cost[i] = split_linear(n, node, d.capacity, row(i, 0), rA, rQ, P, R);
     if (threadIdx.x == 0) {
       a.gen[t] = 0;
       if (a.stats) atomicAdd(a.stats + 0, (unsigned long long)NP);
@@ -265,7 +315,7 @@ __global__ void __launch_bounds__(256) cvrp_epoch_kernel(const Args a) {
         int acc = 0;
         if (i < k) {
           const int m = byrank[NP - k + i];
-          const int32_t cc = split_linear(n, dist, node, d.capacity, row(m, 1), rA, rQ, P, mask);
+          const int32_t cc = split_linear(n, node, d.capacity, row(m, 1), rA, rQ, P, R);
           if (cc < cost[m]) {
             cur[m] = 1;
             cost[m] = cc;
@@ -291,8 +341,7 @@ __global__ void __launch_bounds__(256) cvrp_epoch_kernel(const Args a) {
         if (u01(wo.x) < a.p_cross) {
           const int c1 = (int)(wo.y % (uint32_t)n), c2 = (int)(wo.z % (uint32_t)n);
           const int lo = c1 < c2 ? c1 : c2, hi = c1 < c2 ? c2 : c1;
-#pragma unroll
-          for (int q = 0; q < 8; ++q) used[q * P] = 0u;
+          for (int q = 0; q < UW; ++q) used[q * P] = 0u;
           for (int k = lo; k <= hi; ++k) {
             const uint8_t gene = A[k];
             c[k] = gene;
@@ -303,10 +352,9 @@ __global__ void __launch_bounds__(256) cvrp_epoch_kernel(const Args a) {
           for (int k = 0; k < n; ++k) {
             const uint8_t gene = B[src];
             src = src + 1 == n ? 0 : src + 1;
-            if (!((used[(gene >> 5) * P] >> (gene & 31)) & 1u)) {
-              c[pos] = gene;
-              pos = pos + 1 == n ? 0 : pos + 1;
-            }
+            const bool fresh = !((used[(gene >> 5) * P] >> (gene & 31)) & 1u);
+            if (fresh) c[pos] = gene;
+            pos = fresh ? (pos + 1 == n ? 0 : pos + 1) : pos;
           }
         } else {
           for (int k = 0; k < n; ++k) c[k] = A[k];
@@ -330,7 +378,7 @@ __global__ void __launch_bounds__(256) cvrp_epoch_kernel(const Args a) {
             --hi;
           }
         }
-        kcost[i] = split_linear(n, dist, node, d.capacity, c, rA, rQ, P, mask);
+        kcost[i] = split_linear(n, node, d.capacity, c, rA, rQ, P, R);
       }
       __syncthreads();  // all children built from the old island
       if (i < NP && kcost[i] <= cost[i]) {
@@ -364,25 +412,25 @@ __global__ void __launch_bounds__(256) cvrp_epoch_kernel(const Args a) {
 }
 
 // Costs of caller-given tours of one instance: thread = tour.
+template <int QB>
 __global__ void __launch_bounds__(256) cvrp_eval_kernel(const Args a, int inst, int count,
                                                         const uint8_t* perms, int32_t* costs) {
   extern __shared__ __align__(16) unsigned char smem[];
   const InstDev d = a.inst[inst];
   const int n = d.n, P = blockDim.x;
-  const Layout L = eval_layout(n, P, a.ring_mask + 1);
+  const Layout L = eval_layout(n, P, a.ring, QB);
   if (n < 1 || n > kMaxN || L.total > a.smem_bytes) {
     if (threadIdx.x == 0) report(a.err, 2);
     return;
   }
-  uint16_t* dist = (uint16_t*)(smem + L.dist);
-  int2* node = (int2*)(smem + L.node);
+  int4* node = (int4*)(smem + L.node);
   int32_t* rA = (int32_t*)(smem + L.ringA) + threadIdx.x;
-  int32_t* rQ = (int32_t*)(smem + L.ringQ) + threadIdx.x;
-  load_instance(a, d, dist, node);
+  const QRing<QB> rQ(smem + L.ringQ, threadIdx.x, P);
+  load_instance(a, d, node);
   __syncthreads();
   const int k = blockIdx.x * P + threadIdx.x;
   if (k < count)
-    costs[k] = split_linear(n, dist, node, d.capacity, perms + (size_t)k * n, rA, rQ, P, a.ring_mask);
+    costs[k] = split_linear(n, node, d.capacity, perms + (size_t)k * n, rA, rQ, P, a.ring);
 }
 
 // Best member of every instance.
@@ -422,11 +470,30 @@ int route_bound(const HostInst& hi) {
   return k;
 }
 
-// deque slots per thread: a power of two above the longest route
-int ring_slots(int lmax) {
-  int r = 2;
-  while (r < lmax + 1) r <<= 1;
-  return r;
+// Per-handle kernel shape: deque slots (one more than the longest route,
+// rounded up to a multiple of 4), bytes of a stored demand prefix (the
+// smallest with 2 * capacity below its range), crossover bitmap words.
+struct Shape {
+  int ring = 4, qb = 1, uw = 1;
+};
+
+Shape shape_of(const std::vector<HostInst>& a, const std::vector<HostInst>& b = {}) {
+  int lmax = 0, cap = 0, nmax = 0;
+  for (const std::vector<HostInst>* set : {&a, &b})
+    for (const HostInst& hi : *set) {
+      lmax = std::max(lmax, hi.lmax);
+      cap = std::max(cap, hi.capacity);
+      nmax = std::max(nmax, hi.n);
+    }
+  Shape sh;
+  sh.ring = std::max(4, (lmax + 1 + 3) / 4 * 4);
+  sh.qb = 2 * cap <= 0xFF ? 1 : (2 * cap <= 0xFFFF ? 2 : 4);
+  sh.uw = (nmax >> 5) + 1;
+  return sh;
+}
+
+size_t epoch_smem(int n, int P, const Shape& sh) {
+  return emt::cvrp::layout(n, P, sh.ring, sh.qb, sh.uw).total;
 }
 
 int block_threads(int pop) { return ((pop + 31) / 32) * 32; }
@@ -452,16 +519,6 @@ struct Buf {
   }
 };
 
-// round(sqrt(v)) in integers: r = floor(sqrt(v)); sqrt(v) < r + 1/2 <=> v <= r^2 + r.
-uint32_t round_sqrt(uint64_t v) {
-  uint64_t lo = 0, hi = 1u << 21;
-  while (lo < hi) {
-    const uint64_t mid = (lo + hi + 1) >> 1;
-    if (mid * mid <= v) lo = mid; else hi = mid - 1;
-  }
-  return (v <= lo * lo + lo) ? (uint32_t)lo : (uint32_t)lo + 1u;
-}
-
 }  // namespace
 
 struct emt_cvrp_handle {
@@ -471,14 +528,14 @@ struct emt_cvrp_handle {
   bool uploaded = false, initialized = false;
   uint32_t gdone = 0;
   int parity = 0;
-  int ring = 2;
+  Shape shape;
   int eval_threads = 32;
   size_t smem = 0, eval_smem = 0;
   std::string err;
   cudaStream_t stream = nullptr;
   Buf<emt::cvrp::InstDev> d_inst;
-  Buf<uint16_t> d_dist;
-  Buf<int32_t> d_dem, d_cost, d_err, d_best_idx, d_best_cost;
+  Buf<int4> d_node;
+  Buf<int32_t> d_cost, d_err, d_best_idx, d_best_cost;
   Buf<uint8_t> d_pop, d_elites[2];
   Buf<uint32_t> d_gen;
   Buf<unsigned long long> d_stats;
@@ -501,21 +558,18 @@ int cvrp_upload(emt_cvrp_handle* h) {
   if (!T) return h->fail(EMT_ERR_STATE, "no instances");
   const int NP = h->cfg.pop;
   h->table.resize(T);
-  int64_t dist = 0, dem = 0, pop = 0, el = 0;
+  int64_t nodes = 0, pop = 0, el = 0;
   int32_t cost = 0;
   size_t smem = 0;
-  int ring = 2;
-  for (const HostInst& hi : h->inst) ring = std::max(ring, ring_slots(hi.lmax));
+  const Shape sh = shape_of(h->inst);
   const int P = block_threads(NP);
   for (int t = 0; t < T; ++t) {
     const HostInst& hi = h->inst[t];
     emt::cvrp::InstDev& d = h->table[t];
     d.n = hi.n;
     d.capacity = hi.capacity;
-    d.dist_off = dist;
-    dist += (int64_t)(hi.n + 1) * (hi.n + 1);
-    d.dem_off = dem;
-    dem += hi.n + 1;
+    d.node_off = nodes;
+    nodes += hi.n + 1;
     d.pop_off = pop;
     pop += (int64_t)NP * hi.n;
     d.cost_off = cost;
@@ -523,30 +577,31 @@ int cvrp_upload(emt_cvrp_handle* h) {
     d.pad = 0;
     d.elite_off = el;
     el += (int64_t)NP * hi.n;
-    smem = std::max(smem, emt::cvrp::layout(hi.n, P, ring).total);
+    smem = std::max(smem, epoch_smem(hi.n, P, sh));
   }
   h->smem = smem;
-  h->ring = ring;
+  h->shape = sh;
   // evaluation block: the most threads (128, 64, 32) whose rings fit; 32
   // always does, as the epoch layout of the same rings is larger
   int smax = 0;
   cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->cfg.device);
   for (int pe = 128; pe >= 32; pe >>= 1) {
     size_t es = 0;
-    for (const HostInst& hi : h->inst) es = std::max(es, emt::cvrp::eval_layout(hi.n, pe, ring).total);
+    for (const HostInst& hi : h->inst)
+      es = std::max(es, emt::cvrp::eval_layout(hi.n, pe, sh.ring, sh.qb).total);
     h->eval_threads = pe;
     h->eval_smem = es;
     if (es <= (size_t)smax) break;
   }
-  std::vector<uint16_t> hd((size_t)dist);
-  std::vector<int32_t> hm((size_t)dem);
+  std::vector<int4> hn((size_t)nodes);
   for (int t = 0; t < T; ++t) {
-    std::copy(h->inst[t].dist.begin(), h->inst[t].dist.end(), hd.begin() + h->table[t].dist_off);
-    std::copy(h->inst[t].demand.begin(), h->inst[t].demand.end(), hm.begin() + h->table[t].dem_off);
+    const HostInst& hi = h->inst[t];
+    for (int i = 0; i <= hi.n; ++i)
+      hn[h->table[t].node_off + i] = make_int4(hi.x[i], hi.y[i], (int32_t)hi.dist[i], hi.demand[i]);
   }
   cudaError_t e;
   if ((e = cudaSetDevice(h->cfg.device)) != cudaSuccess) return h->cuda_fail(e, "cudaSetDevice");
-  if ((e = h->d_inst.ensure(T)) || (e = h->d_dist.ensure(hd.size())) || (e = h->d_dem.ensure(hm.size())) ||
+  if ((e = h->d_inst.ensure(T)) || (e = h->d_node.ensure(hn.size())) ||
       (e = h->d_pop.ensure((size_t)pop)) || (e = h->d_cost.ensure((size_t)cost)) ||
       (e = h->d_gen.ensure(T)) || (e = h->d_stats.ensure(2)) || (e = h->d_err.ensure(1)) ||
       (e = h->d_best_idx.ensure(T)) || (e = h->d_best_cost.ensure(T)))
@@ -555,8 +610,7 @@ int cvrp_upload(emt_cvrp_handle* h) {
     for (int b = 0; b < 2; ++b)
       if ((e = h->d_elites[b].ensure((size_t)el))) return h->cuda_fail(e, "cudaMalloc");
   if ((e = cudaMemcpy(h->d_inst.p, h->table.data(), sizeof(emt::cvrp::InstDev) * T, cudaMemcpyHostToDevice)) ||
-      (e = cudaMemcpy(h->d_dist.p, hd.data(), sizeof(uint16_t) * hd.size(), cudaMemcpyHostToDevice)) ||
-      (e = cudaMemcpy(h->d_dem.p, hm.data(), sizeof(int32_t) * hm.size(), cudaMemcpyHostToDevice)) ||
+      (e = cudaMemcpy(h->d_node.p, hn.data(), sizeof(int4) * hn.size(), cudaMemcpyHostToDevice)) ||
       (e = cudaMemset(h->d_gen.p, 0, sizeof(uint32_t) * T)) ||
       (e = cudaMemset(h->d_stats.p, 0, sizeof(unsigned long long) * 2)) ||
       (e = cudaMemset(h->d_err.p, 0, sizeof(int32_t))))
@@ -572,9 +626,9 @@ emt::cvrp::Args cvrp_args(emt_cvrp_handle* h, int mode) {
   a.n_inst = (int32_t)h->inst.size();
   a.NP = h->cfg.pop;
   a.mode = mode;
-  a.ring_mask = h->ring - 1;
-  a.dist = h->d_dist.p;
-  a.demand = h->d_dem.p;
+  a.ring = h->shape.ring;
+  a.used_words = h->shape.uw;
+  a.node = h->d_node.p;
   a.pop = h->d_pop.p;
   a.cost = h->d_cost.p;
   a.gen = h->d_gen.p;
@@ -590,11 +644,11 @@ emt::cvrp::Args cvrp_args(emt_cvrp_handle* h, int mode) {
 }
 
 int cvrp_launch(emt_cvrp_handle* h, const emt::cvrp::Args& a, void* stream) {
-  cudaError_t e = cudaFuncSetAttribute(emt::cvrp::cvrp_epoch_kernel,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->smem);
+  auto kern = h->shape.qb == 1 ? emt::cvrp::cvrp_epoch_kernel<1>
+             : h->shape.qb == 2 ? emt::cvrp::cvrp_epoch_kernel<2> : emt::cvrp::cvrp_epoch_kernel<4>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->smem);
   if (e != cudaSuccess) return h->cuda_fail(e, "cudaFuncSetAttribute");
-  emt::cvrp::cvrp_epoch_kernel<<<(int)h->inst.size(), block_threads(h->cfg.pop), h->smem,
-                                  (cudaStream_t)stream>>>(a);
+  kern<<<(int)h->inst.size(), block_threads(h->cfg.pop), h->smem, (cudaStream_t)stream>>>(a);
   e = cudaGetLastError();
   if (e != cudaSuccess) return h->cuda_fail(e, "cvrp launch");
   return EMT_OK;
@@ -639,8 +693,6 @@ int emt_cvrp_add_instances(emt_cvrp_handle_t* h, int32_t n, const emt_cvrp_insta
   if (n < 0 || (n > 0 && !in)) return h->fail(EMT_ERR_INVALID_ARG, "bad instance array");
   int smax = 0;
   cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->cfg.device);
-  int ring = 2;
-  for (const HostInst& hi : h->inst) ring = std::max(ring, ring_slots(hi.lmax));
   std::vector<HostInst> add;
   for (int k = 0; k < n; ++k) {
     const emt_cvrp_instance& d = in[k];
@@ -677,20 +729,19 @@ int emt_cvrp_add_instances(emt_cvrp_handle_t* h, int32_t n, const emt_cvrp_insta
       if (hi.demand[i] > hi.capacity)
         return h->fail(EMT_ERR_INVALID_ARG, "instance " + std::to_string(k) + ": a demand exceeds the capacity");
     hi.lmax = route_bound(hi);
-    ring = std::max(ring, ring_slots(hi.lmax));
     hi.dist.resize((size_t)W * W);
     for (int i = 0; i < W; ++i)
       for (int j = 0; j < W; ++j) {
-        const int64_t dx = hi.x[i] - hi.x[j], dy = hi.y[i] - hi.y[j];
-        hi.dist[(size_t)i * W + j] = (uint16_t)round_sqrt((uint64_t)(dx * dx + dy * dy));
+        hi.dist[(size_t)i * W + j] = (uint16_t)emt::cvrp::round_dist(hi.x[i], hi.y[i], hi.x[j], hi.y[j]);
       }
     add.push_back(std::move(hi));
   }
   // the deque ring is sized for the handle's longest route, so recheck every island
   const int P = block_threads(h->cfg.pop);
+  const Shape sh = shape_of(h->inst, add);
   for (const std::vector<HostInst>* set : {&h->inst, &add})
     for (const HostInst& hi : *set)
-      if ((size_t)smax < emt::cvrp::layout(hi.n, P, ring).total)
+      if ((size_t)smax < epoch_smem(hi.n, P, sh))
         return h->fail(EMT_ERR_UNSUPPORTED, "an island of " + std::to_string(hi.n) +
                                                 " customers does not fit in shared memory");
   for (auto& a : add) h->inst.push_back(std::move(a));
@@ -838,15 +889,15 @@ int emt_cvrp_evaluate(emt_cvrp_handle_t* h, int32_t inst, int32_t count, const u
   cudaError_t e = cudaMalloc((void**)&dp, (size_t)count * n);
   if (e == cudaSuccess) e = cudaMalloc((void**)&dc, sizeof(int32_t) * count);
   if (e == cudaSuccess) e = cudaMemcpy(dp, perms, (size_t)count * n, cudaMemcpyHostToDevice);
+  auto kern = h->shape.qb == 1 ? emt::cvrp::cvrp_eval_kernel<1>
+             : h->shape.qb == 2 ? emt::cvrp::cvrp_eval_kernel<2> : emt::cvrp::cvrp_eval_kernel<4>;
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(emt::cvrp::cvrp_eval_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)h->eval_smem);
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->eval_smem);
   if (e == cudaSuccess) {
     emt::cvrp::Args a = cvrp_args(h, 0);
     a.smem_bytes = h->eval_smem;
     const int pe = h->eval_threads;
-    emt::cvrp::cvrp_eval_kernel<<<(count + pe - 1) / pe, pe, h->eval_smem, h->stream>>>(a, inst, count,
-                                                                                       dp, dc);
+    kern<<<(count + pe - 1) / pe, pe, h->eval_smem, h->stream>>>(a, inst, count, dp, dc);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(costs, dc, sizeof(int32_t) * count, cudaMemcpyDeviceToHost, h->stream);
@@ -880,8 +931,7 @@ void emt_cvrp_destroy(emt_cvrp_handle_t* h) {
   if (!h) return;
   if (h->stream) cudaStreamSynchronize(h->stream);
   h->d_inst.release();
-  h->d_dist.release();
-  h->d_dem.release();
+  h->d_node.release();
   h->d_cost.release();
   h->d_err.release();
   h->d_best_idx.release();

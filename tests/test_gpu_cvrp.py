@@ -184,3 +184,25 @@ def test_long_routes_run_bit_exact(sgemtf, orc):
     rep.run(15)
     check_islands(e, rep)
     e.close()
+
+
+@pytest.mark.parametrize("cap,dem_hi", [(50, 10), (127, 127), (128, 128), (300, 60),
+                                        (32767, 5000), (32768, 9000), (1 << 23, 1 << 20)])
+def test_demand_prefix_widths(sgemtf, orc, cap, dem_hi):
+    """The deque stores demand prefixes in 1, 2 or 4 bytes depending on the
+    largest capacity (2 * capacity must fit): each width, at and past its
+    limit, replays the host bit for bit."""
+    rng = np.random.default_rng(cap)
+    n = 48
+    x, y = rng.integers(0, 5000, n + 1), rng.integers(0, 5000, n + 1)
+    d = np.r_[0, rng.integers(1, dem_hi + 1, n)]
+    specs = [(n, cap, x, y, d), (n, cap, x, y, d[::-1].copy())]
+    e = engine(sgemtf, specs, seed=9, pop=32, transfer_interval=4)
+    ins = [orc.CvrpInstance(9, t, *sp) for t, sp in enumerate(specs)]
+    rep = orc.CvrpReplay(9, ins, 32, interval=4, rate=0.1)
+    e.run(10)
+    rep.run(10)
+    check_islands(e, rep)
+    tours = np.stack([rng.permutation(n) + 1 for _ in range(200)]).astype(np.uint8)
+    np.testing.assert_array_equal(e.evaluate(0, tours), [ins[0].split(t) for t in tours])
+    e.close()
