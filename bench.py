@@ -312,7 +312,8 @@ def main_cvrp(args, rank, world, local):
         hins = [orc.CvrpInstance(1 + rank, t, CVRP_N, CVRP_CAP) for t in range(n_inst)]
         specs = [(CVRP_N, CVRP_CAP, x.x, x.y, x.demand) for x in hins]
         W = CVRP_N + 1
-        h2d = n_inst * (W * W * 2 + W * 4 + 40)
+        # node table {x, y, d0, demand} and the instance descriptor
+        h2d = n_inst * (W * 16 + 40)
         times = []
         for _ in range(max(1, args.steps)):
             t0 = time.perf_counter()
@@ -332,8 +333,8 @@ def main_cvrp(args, rank, world, local):
     peaks, peak_kind = measured_peaks()
     W = CVRP_N + 1
     # algorithmic HBM bytes of the run: islands and costs in and out once per
-    # epoch launch, the instance (uint16 distances, demands) read once per launch
-    per_launch = n_inst * (2 * CVRP_POP * CVRP_N + 2 * CVRP_POP * 4 + W * W * 2 + W * 4)
+    # epoch launch, the node table {x, y, d0, demand} read once per launch
+    per_launch = n_inst * (2 * CVRP_POP * CVRP_N + 2 * CVRP_POP * 4 + W * 16)
     run_s = float(np.mean(run_ms)) * 1e-3
     gbs = per_launch * (launches - 1) / run_s / 1e9
     line = {

@@ -458,7 +458,7 @@ struct HostInst {
   int n = 0, capacity = 0;
   int lmax = 0;  // most customers one route can serve (smallest demands first)
   std::vector<int32_t> x, y, demand;
-  std::vector<uint16_t> dist;
+  std::vector<int32_t> d0;  // distance of every node to the depot
 };
 
 int route_bound(const HostInst& hi) {
@@ -597,7 +597,7 @@ int cvrp_upload(emt_cvrp_handle* h) {
   for (int t = 0; t < T; ++t) {
     const HostInst& hi = h->inst[t];
     for (int i = 0; i <= hi.n; ++i)
-      hn[h->table[t].node_off + i] = make_int4(hi.x[i], hi.y[i], (int32_t)hi.dist[i], hi.demand[i]);
+      hn[h->table[t].node_off + i] = make_int4(hi.x[i], hi.y[i], hi.d0[i], hi.demand[i]);
   }
   cudaError_t e;
   if ((e = cudaSetDevice(h->cfg.device)) != cudaSuccess) return h->cuda_fail(e, "cudaSetDevice");
@@ -729,11 +729,9 @@ int emt_cvrp_add_instances(emt_cvrp_handle_t* h, int32_t n, const emt_cvrp_insta
       if (hi.demand[i] > hi.capacity)
         return h->fail(EMT_ERR_INVALID_ARG, "instance " + std::to_string(k) + ": a demand exceeds the capacity");
     hi.lmax = route_bound(hi);
-    hi.dist.resize((size_t)W * W);
+    hi.d0.resize(W);
     for (int i = 0; i < W; ++i)
-      for (int j = 0; j < W; ++j) {
-        hi.dist[(size_t)i * W + j] = (uint16_t)emt::cvrp::round_dist(hi.x[i], hi.y[i], hi.x[j], hi.y[j]);
-      }
+      hi.d0[i] = (int32_t)emt::cvrp::round_dist(hi.x[0], hi.y[0], hi.x[i], hi.y[i]);
     add.push_back(std::move(hi));
   }
   // the deque ring is sized for the handle's longest route, so recheck every island
@@ -859,7 +857,9 @@ int emt_cvrp_get_instance(emt_cvrp_handle_t* h, int32_t inst, int32_t* x, int32_
   if (y) std::memcpy(y, hi.y.data(), sizeof(int32_t) * W);
   if (demand) std::memcpy(demand, hi.demand.data(), sizeof(int32_t) * W);
   if (dist)
-    for (size_t k = 0; k < (size_t)W * W; ++k) dist[k] = hi.dist[k];
+    for (int i = 0; i < W; ++i)
+      for (int j = 0; j < W; ++j)
+        dist[(size_t)i * W + j] = (int32_t)emt::cvrp::round_dist(hi.x[i], hi.y[i], hi.x[j], hi.y[j]);
   return EMT_OK;
 }
 
