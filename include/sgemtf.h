@@ -115,6 +115,8 @@ typedef enum emt_rotation {
 #define EMT_FLAG_NO_RECHECK 0x10u             /* select on FP32 fitness only */
 #define EMT_FLAG_RIGOROUS_WINDOW 0x20u        /* Weierstrass near-tie window from the
                                                  rigorous 3^k conditioning bound */
+#define EMT_FLAG_NO_DIFF_RECHECK 0x40u        /* re-check near ties by FP64-class values
+                                                 only, without the differential form */
 
 typedef struct emt_config {
   int32_t algorithm;         /* emt_algorithm                                */
@@ -160,6 +162,10 @@ typedef struct emt_stats {
   double device_ms;           /* device time of the last emt_run            */
   int32_t n_tasks;
   int32_t precision_used;     /* emt_precision actually run                 */
+  uint64_t recheck_differential; /* re-checks decided by the differential form,
+                                    without FP64-class values               */
+  uint64_t anchor_rotations;  /* compensated member rotations computed for it */
+  uint64_t recheck_identical; /* re-checks of a trial bit-identical to its parent */
 } emt_stats;
 
 /* Fills *cfg with DE/rand/1/bin, F = 0.5, CR = 0.9, SBX eta 15 / p_c 0.9,

@@ -78,6 +78,7 @@ struct emt_handle {
   DevBuf<TaskDev> d_tasks;
   DevBuf<int32_t> d_order;
   DevBuf<float> d_pop, d_fit32, d_tol32, d_qt, d_shift, d_elites[2], d_best_f32;
+  DevBuf<float> d_zc, d_zcb;  // per-member compensated rotations and their bounds
   DevBuf<double> d_fit64, d_best_f64;
   DevBuf<uint32_t> d_gen;
   DevBuf<unsigned long long> d_stats;
@@ -318,10 +319,12 @@ int upload(emt_handle* h) {
       (e = h->d_fit32.ensure((size_t)fit)) != cudaSuccess ||
       (e = h->d_tol32.ensure((size_t)fit)) != cudaSuccess ||
       (e = h->d_fit64.ensure((size_t)fit)) != cudaSuccess ||
+      (e = h->d_zc.ensure((size_t)2 * pop)) != cudaSuccess ||
+      (e = h->d_zcb.ensure((size_t)2 * fit)) != cudaSuccess ||
       (e = h->d_qt.ensure((size_t)q)) != cudaSuccess ||
       (e = h->d_shift.ensure((size_t)o)) != cudaSuccess ||
       (e = h->d_gen.ensure(n)) != cudaSuccess ||
-      (e = h->d_stats.ensure(4)) != cudaSuccess || (e = h->d_err.ensure(1)) != cudaSuccess ||
+      (e = h->d_stats.ensure(7)) != cudaSuccess || (e = h->d_err.ensure(1)) != cudaSuccess ||
       (e = h->d_best_idx.ensure(n)) != cudaSuccess ||
       (e = h->d_best_f32.ensure(n)) != cudaSuccess ||
       (e = h->d_best_f64.ensure(n)) != cudaSuccess)
@@ -335,7 +338,8 @@ int upload(emt_handle* h) {
       (e = cudaMemcpy(h->d_shift.p, ho.data(), sizeof(float) * ho.size(), cudaMemcpyHostToDevice)) ||
       (e = cudaMemset(h->d_gen.p, 0, sizeof(uint32_t) * n)) ||
       (e = cudaMemset(h->d_pop.p, 0, sizeof(float) * (size_t)pop)) ||
-      (e = cudaMemset(h->d_stats.p, 0, sizeof(unsigned long long) * 4)) ||
+      (e = cudaMemset(h->d_stats.p, 0, sizeof(unsigned long long) * 7)) ||
+      (e = cudaMemset(h->d_zcb.p, 0xFF, sizeof(float) * 2 * (size_t)fit)) ||
       (e = cudaMemset(h->d_err.p, 0, sizeof(int32_t))))
     return h->cuda_fail(e, "upload");
   if (h->use_tc) {
@@ -375,6 +379,8 @@ emt::EpochArgs base_args(emt_handle* h, int mode) {
   a.fit32 = h->d_fit32.p;
   a.tol32 = h->d_tol32.p;
   a.fit64 = h->d_fit64.p;
+  a.zc = h->d_zc.p;
+  a.zcb = h->d_zcb.p;
   a.qt = h->d_qt.p;
   a.shift = h->d_shift.p;
   a.gen = h->d_gen.p;
@@ -893,9 +899,12 @@ int emt_get_stats(emt_handle_t* h, emt_stats* out) {
   if (h->d_stats.p) {
     int rc = emt_sync(h);
     if (rc) return rc;
-    unsigned long long s[4];
+    unsigned long long s[7];
     cudaError_t e = cudaMemcpy(s, h->d_stats.p, sizeof(s), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return h->cuda_fail(e, "copy stats");
+    out->recheck_differential = s[4];
+    out->anchor_rotations = s[5];
+    out->recheck_identical = s[6];
     out->rechecks = s[0];
     out->recheck_flips = s[1];
     out->transfers_accepted = s[2];
@@ -975,6 +984,9 @@ int emt_restore(emt_handle_t* h, const void* buf, size_t bytes) {
     p += 4;
     if (e != cudaSuccess) return h->cuda_fail(e, "restore");
   }
+  // the cached compensated rotations belong to the replaced islands
+  cudaError_t ez = cudaMemset(h->d_zcb.p, 0xFF, sizeof(float) * h->d_zcb.n);
+  if (ez != cudaSuccess) return h->cuda_fail(ez, "restore");
   h->gdone = (uint32_t)hdr[2];
   h->initialized = true;
   h->elite_parity = 0;
@@ -1012,6 +1024,8 @@ void emt_destroy(emt_handle_t* h) {
   h->d_elites[1].release();
   h->d_best_f32.release();
   h->d_fit64.release();
+  h->d_zc.release();
+  h->d_zcb.release();
   h->d_best_f64.release();
   h->d_gen.release();
   h->d_stats.release();

@@ -298,14 +298,18 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
 
 // One Weierstrass gene from a high-precision argument z (double holding a
 // double-FP32 value): y_k = 2 * 3^k * |z| mod 2 is reduced exactly on the
-// 53-bit significand (r <- 3 r mod 2^(sh+1)), then cos(pi y_k) in FP32;
+// 53-bit significand (r <- 3 r mod 2^(sh+1)), then cos(pi y_k) in FP32
+// (the reduced argument carries 24 bits, so each term is good to ~2^-23);
 // the 21 terms are summed with Kahan compensation.
 __device__ __forceinline__ float weier_gene_precise(double z) {
-  const double az = fabs(z);
-  const unsigned long long b = (unsigned long long)__double_as_longlong(az);
+  // |z| = M 2^-sh with M the 53-bit significand; y_k = 2 3^k |z| mod 2 is
+  // reduced exactly in integers (64-bit for sh < 64, 128-bit up to sh = 127)
+  // and rounded once to FP32 for cospif.  No FP64 arithmetic.
+  const unsigned long long b =
+      (unsigned long long)__double_as_longlong(z) & 0x7FFFFFFFFFFFFFFFull;
   const int E = (int)(b >> 52);
   const unsigned long long M = (b & ((1ull << 52) - 1ull)) | (1ull << 52);
-  const int sh = 1074 - E;  // y_0 = M / 2^sh for normal az
+  const int sh = 1074 - E;  // y_0 = M / 2^sh for normal |z|
   float s = 0.f, comp = 0.f, ak = 1.f;
   auto add = [&](float c) {
     const float v = __fsub_rn(__fmul_rn(-ak, c), comp);
@@ -314,27 +318,38 @@ __device__ __forceinline__ float weier_gene_precise(double z) {
     s = t;
     ak *= 0.5f;
   };
-  if (az == 0.0) {
+  if (b == 0ull || E == 0 || sh > 127) {
+    // |z| < 2^-75: every 2 3^k |z| < 2^-41 and cospif rounds to 1
     for (int k = 0; k <= 20; ++k) add(1.f);
-  } else if (E == 0 || sh > 61) {
-    double p3 = 2.0;
-    for (int k = 0; k <= 20; ++k) {
-      double y = p3 * az;
-      y -= 2.0 * floor(0.5 * y);
-      add(cospif((float)y));
-      p3 *= 3.0;
-    }
   } else if (sh <= 0) {
     const float c = (sh == 0 && (M & 1ull)) ? -1.f : 1.f;
     for (int k = 0; k <= 20; ++k) add(c);
-  } else {
+  } else if (sh < 64) {
     const unsigned long long mask = (2ull << sh) - 1ull;
     unsigned long long r = M & mask;
     const int drop = sh > 24 ? sh - 24 : 0;
     const float scale = __uint_as_float((uint32_t)(127 - (sh - drop)) << 23);
     for (int k = 0; k <= 20; ++k) {
-      add(cospif((float)(r >> drop) * scale));
+      // r >> drop < 2^25: a 32-bit conversion rounds it exactly as a 64-bit
+      // one would, and stays off the FP64 pipe
+      add(cospif(__uint2float_rn((uint32_t)(r >> drop)) * scale));
       r = (r * 3ull) & mask;
+    }
+  } else {
+    // 64 <= sh <= 127: r = (r1 : r0) < 2^(sh+1) <= 2^128, drop = sh - 24 >= 40
+    unsigned long long r0 = M, r1 = 0ull;
+    const unsigned long long mask1 = sh >= 127 ? ~0ull : ((2ull << (sh - 64)) - 1ull);
+    const int drop = sh - 24;
+    const float scale = __uint_as_float((uint32_t)(127 - 24) << 23);
+    for (int k = 0; k <= 20; ++k) {
+      const unsigned long long top =
+          drop >= 64 ? (r1 >> (drop - 64)) : ((r0 >> drop) | (r1 << (64 - drop)));
+      add(cospif(__uint2float_rn((uint32_t)top) * scale));
+      // r <- 3 r mod 2^(sh+1)
+      const unsigned long long lo = r0 * 3ull;
+      const unsigned long long carry = __umul64hi(r0, 3ull);
+      r1 = (r1 * 3ull + carry) & mask1;
+      r0 = lo;
     }
   }
   return s;

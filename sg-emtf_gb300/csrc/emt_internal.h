@@ -64,6 +64,13 @@ struct EpochArgs {
   const float* elites_in;
   float* elites_out;
   unsigned long long* stats;  // [0] rechecks [1] flips [2] transfers [3] evaluations
+                              // [4] re-checks decided by the differential form
+                              // [5] member anchors (compensated rotations) computed
+                              // [6] re-checks of bit-identical trials
+  // per member: compensated rotation z_h, z_l (2 * DP floats, at 2 * pop_off)
+  // and {error bound, refresh limit} (at 2 * fit_off); NaN bound = not cached
+  float* zc;
+  float* zcb;
   int32_t* err;               // first kernel-side check that fired (0 = none)
   size_t smem_bytes;          // dynamic shared memory the launch provides
   int32_t tc_np, tc_kp;       // tensor-core form: padded N and K of the B tiles

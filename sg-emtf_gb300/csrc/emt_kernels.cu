@@ -26,12 +26,14 @@
 #include <cuda_runtime.h>
 
 #include "emt_functions.cuh"
+#include "emt_recheck.cuh"
 #include "emt_tc.cuh"
 
 namespace emt {
 
 struct Smem {
   double *fit64, *z64;
+  float *zc, *zcb;  // this task's anchor cache (global memory)
   float *X, *U, *ST, *Z, *QT, *o, *fit, *tol, *ftr, *ttr;
   int *idx, *flag, *list, *misc;
   // tensor-core form
@@ -52,6 +54,7 @@ __device__ __forceinline__ Smem carve_tc(unsigned char* base, const TcLayout& L)
   s.ST = nullptr;
   s.Z = (float*)(base + L.A);  // rotated rows alias the A operand after the MMAs
   s.QT = nullptr;
+  s.zc = s.zcb = nullptr;
   s.o = (float*)(base + L.o);
   s.fit = (float*)(base + L.fit);
   s.tol = (float*)(base + L.tol);
@@ -80,6 +83,7 @@ __device__ __forceinline__ Smem carve(unsigned char* base, const Layout& L) {
   s.ST = (float*)(base + L.ST);
   s.Z = (float*)(base + L.Z);
   s.QT = (float*)(base + L.QT);
+  s.zc = s.zcb = nullptr;
   s.o = (float*)(base + L.o);
   s.fit = (float*)(base + L.fit);
   s.tol = (float*)(base + L.tol);
@@ -375,8 +379,11 @@ __device__ int select_and_replace(const Smem& s, const EpochArgs& a, const FnCon
                                   int nrows, const int* target, bool strict, int DP,
                                   unsigned long long* rechecks, unsigned long long* flips) {
   const bool recheck = !(a.flags & FLAG_NO_RECHECK);
-  if (threadIdx.x == 0) s.misc[0] = 0;
+  const bool anchors = recheck && s.zcb && !(a.flags & FLAG_NO_DIFF_RECHECK) &&
+                       diff_pays(fc.fid);
+  if (threadIdx.x == 0) s.misc[0] = s.misc[1] = 0;
   __syncthreads();
+  // flag bits: 1 accept, 2 re-checked, 4 anchor carried forward
   for (int c = threadIdx.x; c < nrows; c += kThreads) {
     const int m = target ? target[c] : c;
     const float ft = s.ftr[c], fp = s.fit[m];
@@ -384,12 +391,17 @@ __device__ int select_and_replace(const Smem& s, const EpochArgs& a, const FnCon
     if (recheck && fabsf(ft - fp) <= s.ttr[c] + s.tol[m]) {
       s.flag[c] = 2;
       s.list[atomicAdd(&s.misc[0], 1)] = c;
+    } else if (d32 && anchors && s.zcb[2 * m] <= s.zcb[2 * m + 1]) {
+      // accepted on FP32 fitness with a cached anchor: carry it forward (the
+      // island is converging, so the member is likely re-checked again)
+      s.flag[c] = 5;
+      s.list[nrows - 1 - atomicAdd(&s.misc[1], 1)] = c;
     } else {
       s.flag[c] = d32 ? 1 : 0;
     }
   }
   __syncthreads();
-  const int nre = s.misc[0];
+  const int nre = s.misc[0], nadv = s.misc[1];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int r = warp; r < nre; r += kWarps) {
     const int c = s.list[r];
@@ -404,9 +416,37 @@ __device__ int select_and_replace(const Smem& s, const EpochArgs& a, const FnCon
     same = __all_sync(0xFFFFFFFFu, same);
     double fp = s.fit64[m], ft = 0.0;
     bool d64;
+    // the differential decision: sign of f(u) - f(x) from the parent's cached
+    // compensated rotation and dz = Q (u - x), FP32/INT pipes only; -1 when
+    // its bound cannot separate the two
+    int dd = -1;
+    if (!same && anchors) {
+      float* zh = s.zc + (size_t)m * 2 * DP;
+      float* zl = zh + DP;
+      float* buf = reinterpret_cast<float*>(zt);
+      float ez = s.zcb[2 * m], lim = s.zcb[2 * m + 1];
+      if (!(ez <= lim)) {  // not cached, or its bound has grown: recompute
+        float zmax;
+        ez = anchor_rotation(s.X + m * DP, s.o, s.QT, DP, fc.D, fc.qnorm * (1.f + 0x1p-20f), zh,
+                             zl, &zmax, reinterpret_cast<float2*>(buf + 2 * DP));
+        // carried-forward anchors may drift to 64x the fresh bound, or to
+        // 2^-26 max|z| (below the rounding of the difference forms themselves)
+        lim = fmaxf(64.f * ez, 0x1p-26f * zmax) + 1e-30f;
+        if (lane == 0 && rechecks) atomicAdd(rechecks + 5, 1ull);
+      }
+      dd = diff_decide(fc, zh, zl, ez, s.X + m * DP, s.U + c * DP, s.QT, DP, buf);
+      if (dd == 1) ez = anchor_advance(zh, zl, buf, DP, fc.D, ez);  // the trial replaces x
+      if (lane == 0) {
+        s.zcb[2 * m] = ez;
+        s.zcb[2 * m + 1] = lim;
+      }
+    }
     if (same) {
       ft = fp;
       d64 = !strict;
+    } else if (dd >= 0) {
+      d64 = dd == 1;
+      ft = __longlong_as_double(0x7FF8000000000000ll);  // exact values unknown
     } else {
       precise_rotation(s.U + c * DP, s.o, s.QT, DP, fc.D, zt);
       const bool tier2 = fc.fid != F_WEIERSTRASS && fc.fid != F_SPHERE && fc.fid != F_ROSENBROCK;
@@ -438,6 +478,12 @@ __device__ int select_and_replace(const Smem& s, const EpochArgs& a, const FnCon
     }
     const bool d32 = strict ? (s.ftr[c] < s.fit[m]) : (s.ftr[c] <= s.fit[m]);
     if (lane == 0) {
+      if (rechecks) {
+        if (dd >= 0) atomicAdd(rechecks + 4, 1ull);
+        if (same) atomicAdd(rechecks + 6, 1ull);
+      }
+      // a trial accepted through the FP64-class tiers has no cached anchor
+      if (!same && dd < 0 && d64 && s.zcb) s.zcb[2 * m] = __int_as_float(0x7FC00000);
       s.flag[c] = d64 ? 3 : 0;
       // FP64 value of whichever vector member m holds after this selection,
       // cached for its next re-check.  Targets are distinct, so no race.
@@ -445,6 +491,17 @@ __device__ int select_and_replace(const Smem& s, const EpochArgs& a, const FnCon
       if (rechecks) atomicAdd(rechecks, 1ull);
       if (flips && d64 != d32) atomicAdd(flips, 1ull);
     }
+    __syncwarp();
+  }
+  for (int r = warp; r < nadv; r += kWarps) {
+    const int c = s.list[nrows - 1 - r];
+    const int m = target ? target[c] : c;
+    float* buf = reinterpret_cast<float*>(s.z64 + warp * 2 * DP);
+    float* zh = s.zc + (size_t)m * 2 * DP;
+    row_offset(s.X + m * DP, s.U + c * DP, s.QT, DP, fc.D, fc.qnorm * (1.f + 0x1p-20f), buf,
+               reinterpret_cast<float2*>(buf + 2 * DP));
+    const float ez = anchor_advance(zh, zh + DP, buf, DP, fc.D, s.zcb[2 * m]);
+    if (lane == 0) s.zcb[2 * m] = ez;  // refreshed on its next use if above the limit
     __syncwarp();
   }
   __syncthreads();
@@ -463,7 +520,8 @@ __device__ int select_and_replace(const Smem& s, const EpochArgs& a, const FnCon
       const int m = target ? target[c] : c;
       s.fit[m] = s.ftr[c];
       s.tol[m] = s.ttr[c];
-      if (s.flag[c] == 1) s.fit64[m] = __longlong_as_double(0x7FF8000000000000ll);
+      if (!(s.flag[c] & 2)) s.fit64[m] = __longlong_as_double(0x7FF8000000000000ll);
+      if (s.flag[c] == 1 && s.zcb) s.zcb[2 * m] = __int_as_float(0x7FC00000);
       ++acc;
     }
   }
@@ -571,6 +629,10 @@ __device__ __forceinline__ void epoch_body(const EpochArgs& a, const void* tmap,
   fc.qnorm = td.qnorm;
   fc.rel = a.recheck_rel;
   fc.woff64 = td.woff64;
+  if (a.zc && a.zcb) {
+    s.zc = a.zc + 2 * td.pop_off;
+    s.zcb = a.zcb + 2 * (size_t)td.fit_off;
+  }
   uint32_t phase = 0;
 
   // ---- load the task into shared memory ----
@@ -618,8 +680,10 @@ __device__ __forceinline__ void epoch_body(const EpochArgs& a, const void* tmap,
     stage_differences<TC>(s, s.X, NP, D, DP, NPP);
     __syncthreads();
     evaluate_rows<TC>(s, fc, s.X, NP, DP, NPP, s.fit, s.tol, phase);
-    for (int i = threadIdx.x; i < NP; i += kThreads)
+    for (int i = threadIdx.x; i < NP; i += kThreads) {
       s.fit64[i] = __longlong_as_double(0x7FF8000000000000ll);
+      if (s.zcb) s.zcb[2 * i] = __int_as_float(0x7FC00000);  // anchors not cached
+    }
     if (threadIdx.x == 0) {
       a.gen[task] = a.mode == MODE_INIT ? 0u : a.gen[task];
       if (a.stats) atomicAdd(a.stats + 3, (unsigned long long)NP);

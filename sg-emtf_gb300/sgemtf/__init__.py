@@ -32,6 +32,7 @@ FLAG_REF_ACKLEY_E = 0x4
 FLAG_REF_BOXES = 0x8
 FLAG_NO_RECHECK = 0x10
 FLAG_RIGOROUS_WINDOW = 0x20
+FLAG_NO_DIFF_RECHECK = 0x40
 MAX_DIM, MAX_POP = 128, 256
 NOALLOC_EXCHANGE_FLOATS = 1 << 19
 
@@ -77,7 +78,9 @@ class Stats(ctypes.Structure):
     _fields_ = [("evaluations", ctypes.c_uint64), ("generations", ctypes.c_uint64),
                 ("rechecks", ctypes.c_uint64), ("recheck_flips", ctypes.c_uint64),
                 ("transfers_accepted", ctypes.c_uint64), ("device_ms", ctypes.c_double),
-                ("n_tasks", ctypes.c_int32), ("precision_used", ctypes.c_int32)]
+                ("n_tasks", ctypes.c_int32), ("precision_used", ctypes.c_int32),
+                ("recheck_differential", ctypes.c_uint64), ("anchor_rotations", ctypes.c_uint64),
+                ("recheck_identical", ctypes.c_uint64)]
 
 
 class TaskDesc:

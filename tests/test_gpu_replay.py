@@ -90,3 +90,30 @@ def test_config1_shape_identity_rotation(sgemtf, orc):
     want = replay(orc, oracle_params(orc, eng), tasks, X0, 5)
     for i in range(8):
         assert np.array_equal(eng.population(i)[0], want[i])
+
+
+@pytest.mark.parametrize("precision,flags", [(0, 0), (1, 0), (0, 0x40)])
+def test_replay_converged_islands(sgemtf, orc, precision, flags):
+    """Long runs of small islands converge until trial and parent differ by a
+    few ulps and most selections are near-ties: every re-check path (the
+    differential decision with its cached anchors, the tiered FP64-class
+    values) must still decide as the FP64 replay does."""
+    specs = [(f, 10, 16, 1) for f in range(7)]
+    try:
+        eng, tasks = make_engine(sgemtf, orc, specs, seed=21, precision=precision, flags=flags)
+    except sgemtf.EngineError as e:
+        pytest.skip(str(e))
+    eng.reset()
+    X0 = [eng.population(i)[0] for i in range(len(tasks))]
+    gens = 600
+    eng.run(gens)
+    st = eng.stats()
+    assert st["rechecks"] > 1000
+    if flags & 0x40:
+        assert st["recheck_differential"] == 0
+    else:
+        assert st["recheck_differential"] > 0
+    want = replay(orc, oracle_params(orc, eng), tasks, X0, gens)
+    for i in range(len(tasks)):
+        got = eng.population(i)[0]
+        assert np.array_equal(got, want[i]), (i, np.argwhere(got != want[i])[:5])
