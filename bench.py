@@ -449,7 +449,10 @@ def main():
                          "wall": wall, "stats": st,
                          "clocks": clk.summary(), "precision_used": st["precision_used"]}
         eng.close()
-    head = "tf32x3" if "tf32x3" in results and results["tf32x3"]["precision_used"] == 1 else "fp32"
+    # headline: the faster of the forms that ran (both give identical
+    # populations; both are reported under "forms")
+    ran = [k for k, v in results.items() if k == "fp32" or v["precision_used"] == 1]
+    head = min(ran, key=lambda k: results[k]["dev_ms"])
     r = results[head]
     total_evals = evals_per_step * args.steps * world
     value = total_evals / (r["dev_ms"] * 1e-3)
@@ -501,16 +504,17 @@ def main():
         achieved = FLOPS_PER_EVAL * evals_epoch / epoch_s / 1e12
         roof = {"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"],
                 "unit": "TFLOP/s", "frac": achieved / peaks["bf16_tflops"],
-                # ncu dram read bytes of one epoch launch (31.1 MB for 608 tasks,
+                # ncu dram read bytes of one epoch launch (16.9 MB for 304 tasks,
                 # scaled to the workload's tasks; the state is read once)
-                "traffic": 31.1e6 * n / 608,
+                "traffic": 16.9e6 * n / 304,
                 "peak_kind": peak_kind + " bf16 dense (tf32 nominal is half of it)",
-                "note": "the tensor pipe is ~4% busy; the kernel is bound by CUDA-core "
+                "note": "the tensor pipe is ~5% busy; the kernel is bound by CUDA-core "
                         "issue (function epilogue, trial builder, near-tie re-checks)"}
     else:
         gbs = state_bytes / epoch_s / 1e9
         roof = {"bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": gbs / peaks["hbm_gbs"], "traffic": 23.1e6 * n / 912,
+                # ncu dram read bytes of one epoch launch: 8.12 MB for 304 tasks
+                "frac": gbs / peaks["hbm_gbs"], "traffic": 8.12e6 * n / 304,
                 "peak_kind": peak_kind, "note": "state is resident in shared memory across "
                 "generations; the kernel is bound by CUDA-core issue, not HBM"}
     line = {
