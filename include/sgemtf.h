@@ -136,8 +136,25 @@ typedef struct emt_config {
   double recheck_rel;        /* FP64 re-check window, relative to the fitness
                                 scale; 0 = library default                   */
   int32_t device;            /* CUDA device ordinal                           */
-  int32_t reserved[7];
+  int32_t schedule;          /* emt_schedule: how an epoch's islands are launched */
+  int32_t use_graph;         /* 1: emt_run captures its epoch sequence in a CUDA
+                                graph once and replays it when it recurs        */
+  int32_t reserved[5];
 } emt_config;
+
+/* How emt_run launches an epoch's islands (results are identical).  The
+ * reference launches one kernel per task from one host thread per task on 8
+ * streams (SG-EMTF.cu:1660-1676, 1839-1915); EMT_SCHEDULE_PER_TASK keeps that
+ * shape for comparison. */
+typedef enum emt_schedule {
+  EMT_SCHEDULE_AUTO = 0,     /* tuned by emt_tune, else BUCKETS for mixed shapes */
+  EMT_SCHEDULE_SINGLE = 1,   /* one launch over every island, shared memory sized
+                                for the largest, longest islands first         */
+  EMT_SCHEDULE_BUCKETS = 2,  /* islands grouped by resident CTAs per SM, one
+                                launch per group with its own shared-memory size,
+                                groups concurrent on side streams               */
+  EMT_SCHEDULE_PER_TASK = 3  /* one single-CTA launch per island, 8 streams     */
+} emt_schedule;
 
 typedef struct emt_task_desc {
   int32_t function;              /* emt_function                             */
@@ -166,6 +183,8 @@ typedef struct emt_stats {
                                     without FP64-class values               */
   uint64_t anchor_rotations;  /* compensated member rotations computed for it */
   uint64_t recheck_identical; /* re-checks of a trial bit-identical to its parent */
+  int32_t epoch_launches;     /* kernel launches per epoch under the schedule in use */
+  int32_t schedule_used;      /* emt_schedule in use | 0x100 when graphs replay  */
 } emt_stats;
 
 /* Fills *cfg with DE/rand/1/bin, F = 0.5, CR = 0.9, SBX eta 15 / p_c 0.9,
@@ -218,6 +237,16 @@ EMT_API int emt_run(emt_handle_t* h, int32_t generations, void* stream);
  * its handle carries.  Results are bit-identical to emt_run. */
 #define EMT_NOALLOC_EXCHANGE_FLOATS (1 << 19)
 EMT_API int emt_run_noalloc(emt_handle_t* h, int32_t generations, void* stream);
+
+/* Autotuner for EMT_SCHEDULE_AUTO: runs `generations` generations with each
+ * candidate schedule in turn (single launch; occupancy buckets; each with and
+ * without graph replay), times them with events on `stream`, and keeps the
+ * fastest for later emt_run calls on this handle.  The generations are real
+ * work (the run continues; results do not depend on the schedule).  Blocking.
+ * *chosen (may be NULL) receives schedule | (graph ? 0x100 : 0).  Replaces
+ * the reference's fixed 8-stream, one-launch-per-task shape
+ * (SG-EMTF.cu:1660-1676). */
+EMT_API int emt_tune(emt_handle_t* h, int32_t generations, void* stream, int32_t* chosen);
 
 /* Waits for the handle's work and reports a kernel's error word. */
 EMT_API int emt_sync(emt_handle_t* h);

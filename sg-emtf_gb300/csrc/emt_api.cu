@@ -75,6 +75,23 @@ struct emt_handle {
   double device_ms = 0.0;
   unsigned long long stats_base[4] = {0, 0, 0, 0};
 
+  // launch schedules: islands grouped by resident CTAs per SM (each group a
+  // contiguous range of the bucketed order, d_order[n ..]), per-island shared
+  // memory, side streams and fork/join events, the cached epoch-loop graph
+  struct Bucket {
+    int first = 0, count = 0;
+    size_t smem = 0;
+  };
+  std::vector<Bucket> buckets;
+  std::vector<size_t> task_smem;
+  int tuned = 0;  // schedule | 0x100 (graph) chosen by emt_tune; 0 = not tuned
+  static constexpr int kSide = 8;
+  cudaStream_t side[kSide] = {};
+  cudaStream_t cap = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev[kSide] = {};
+  cudaGraphExec_t gexec = nullptr;
+  std::vector<int64_t> gkey;
+
   DevBuf<TaskDev> d_tasks;
   DevBuf<int32_t> d_order;
   DevBuf<float> d_pop, d_fit32, d_tol32, d_qt, d_shift, d_elites[2], d_best_f32;
@@ -302,6 +319,39 @@ int upload(emt_handle* h) {
   }
   std::stable_sort(h->order.begin(), h->order.end(),
                    [&](int a, int b) { return cost[a] > cost[b]; });
+  // occupancy buckets: islands with the same resident CTAs per SM share a
+  // launch whose shared memory is the largest of the group; in LPT order
+  cudaError_t e0 = cudaSetDevice(h->device);
+  if (e0 != cudaSuccess) return h->cuda_fail(e0, "cudaSetDevice");
+  h->task_smem.assign(n, 0);
+  std::vector<int> occ(n, 0);
+  for (int t = 0; t < n; ++t) {
+    const HostTask& ht = h->tasks[t];
+    h->task_smem[t] = h->use_tc ? emt::tc_layout(ht.D, ht.NP, h->tc_np, h->tc_kp).total
+                                : emt::smem_layout(ht.D, ht.NP, h->table[t].qt_in_smem != 0).total;
+    occ[t] = emt_epoch_occupancy(h->use_tc, h->task_smem[t]);
+    if (occ[t] <= 0) return h->fail(EMT_ERR_UNSUPPORTED, "an island does not fit on an SM");
+  }
+  std::vector<int32_t> border(h->order);
+  std::stable_sort(border.begin(), border.end(), [&](int a, int b) { return occ[a] < occ[b]; });
+  h->buckets.clear();
+  for (int i = 0; i < n; ++i) {
+    const int t = border[i];
+    if (h->buckets.empty() || occ[border[h->buckets.back().first]] != occ[t]) {
+      emt_handle::Bucket b;
+      b.first = i;
+      h->buckets.push_back(b);
+    }
+    h->buckets.back().count++;
+    h->buckets.back().smem = std::max(h->buckets.back().smem, h->task_smem[t]);
+  }
+  h->order.insert(h->order.end(), border.begin(), border.end());
+  if (h->gexec) {
+    cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+    h->gkey.clear();
+  }
+  h->tuned = 0;
 
   std::vector<float> hq((size_t)q, 0.f), ho((size_t)o, 0.f);
   for (int t = 0; t < n; ++t) {
@@ -314,7 +364,7 @@ int upload(emt_handle* h) {
   cudaError_t e;
   if ((e = cudaSetDevice(h->device)) != cudaSuccess) return h->cuda_fail(e, "cudaSetDevice");
   if ((e = h->d_tasks.ensure(n)) != cudaSuccess ||
-      (e = h->d_order.ensure(n)) != cudaSuccess ||
+      (e = h->d_order.ensure(2 * (size_t)n)) != cudaSuccess ||
       (e = h->d_pop.ensure((size_t)pop)) != cudaSuccess ||
       (e = h->d_fit32.ensure((size_t)fit)) != cudaSuccess ||
       (e = h->d_tol32.ensure((size_t)fit)) != cudaSuccess ||
@@ -333,7 +383,7 @@ int upload(emt_handle* h) {
     for (int b = 0; b < 2; ++b)
       if ((e = h->d_elites[b].ensure((size_t)el)) != cudaSuccess) return h->cuda_fail(e, "cudaMalloc");
   if ((e = cudaMemcpy(h->d_tasks.p, h->table.data(), sizeof(TaskDev) * n, cudaMemcpyHostToDevice)) ||
-      (e = cudaMemcpy(h->d_order.p, h->order.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice)) ||
+      (e = cudaMemcpy(h->d_order.p, h->order.data(), sizeof(int32_t) * 2 * n, cudaMemcpyHostToDevice)) ||
       (e = cudaMemcpy(h->d_qt.p, hq.data(), sizeof(float) * hq.size(), cudaMemcpyHostToDevice)) ||
       (e = cudaMemcpy(h->d_shift.p, ho.data(), sizeof(float) * ho.size(), cudaMemcpyHostToDevice)) ||
       (e = cudaMemset(h->d_gen.p, 0, sizeof(uint32_t) * n)) ||
@@ -411,6 +461,166 @@ int launch_epoch(emt_handle* h, const emt::EpochArgs& a, int grid, void* stream)
   return emt_launch_epoch(a, grid, stream, h->use_tc ? (const void*)&h->tmap : nullptr);
 }
 
+// ---- epoch plans, launch schedules, graph replay ----
+
+struct EpochStep {
+  int gens, imp, exp, parity;
+};
+
+int transfer_interval_of(const emt_handle* h) {
+  return (h->cfg.transfer_interval > 0 && h->tasks.size() > 1) ? h->cfg.transfer_interval : 0;
+}
+
+// The epochs emt_run(generations) launches from the handle's current state:
+// an epoch ends at every transfer boundary.
+std::vector<EpochStep> plan_epochs(const emt_handle* h, int generations) {
+  std::vector<EpochStep> plan;
+  const int interval = transfer_interval_of(h);
+  uint32_t gdone = h->gdone;
+  int parity = h->elite_parity, left = generations;
+  while (left > 0) {
+    EpochStep s{left, 0, 0, parity};
+    if (interval) {
+      s.imp = (gdone > 0 && gdone % (uint32_t)interval == 0) ? 1 : 0;
+      s.gens = std::min(left, interval - (int)(gdone % (uint32_t)interval));
+      s.exp = ((gdone + (uint32_t)s.gens) % (uint32_t)interval == 0) ? 1 : 0;
+    }
+    plan.push_back(s);
+    if (s.exp) parity ^= 1;
+    gdone += (uint32_t)s.gens;
+    left -= s.gens;
+  }
+  return plan;
+}
+
+void apply_plan(emt_handle* h, const std::vector<EpochStep>& plan) {
+  for (const EpochStep& s : plan) {
+    if (s.exp) h->elite_parity ^= 1;
+    h->gdone += (uint32_t)s.gens;
+  }
+}
+
+int effective_schedule(const emt_handle* h) {
+  if (h->cfg.schedule != EMT_SCHEDULE_AUTO) return h->cfg.schedule;
+  if (h->tuned) return h->tuned & 0xFF;
+  return h->buckets.size() > 1 ? EMT_SCHEDULE_BUCKETS : EMT_SCHEDULE_SINGLE;
+}
+
+bool effective_graph(const emt_handle* h) {
+  if (h->cfg.schedule == EMT_SCHEDULE_AUTO && h->tuned) return (h->tuned & 0x100) != 0;
+  return h->cfg.use_graph != 0;
+}
+
+int ensure_side(emt_handle* h) {
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < emt_handle::kSide && e == cudaSuccess; ++i) {
+    if (!h->side[i]) e = cudaStreamCreateWithFlags(&h->side[i], cudaStreamNonBlocking);
+    if (e == cudaSuccess && !h->join_ev[i])
+      e = cudaEventCreateWithFlags(&h->join_ev[i], cudaEventDisableTiming);
+  }
+  if (e == cudaSuccess && !h->fork_ev) e = cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming);
+  if (e == cudaSuccess && !h->cap) e = cudaStreamCreateWithFlags(&h->cap, cudaStreamNonBlocking);
+  return e == cudaSuccess ? EMT_OK : h->cuda_fail(e, "side streams");
+}
+
+// One epoch's islands under a schedule; stream receives every launch or
+// waits for them (fork/join through events), so the next epoch's transfer
+// sees all of this epoch's exports.
+int launch_sched(emt_handle* h, emt::EpochArgs a, int sched, cudaStream_t stream) {
+  const void* tm = h->use_tc ? (const void*)&h->tmap : nullptr;
+  const int n = (int)h->tasks.size();
+  if (sched == EMT_SCHEDULE_SINGLE || (sched == EMT_SCHEDULE_BUCKETS && h->buckets.size() == 1))
+    return emt_launch_epoch_noattr(a, n, stream, tm);
+  int e = (int)cudaEventRecord(h->fork_ev, stream);
+  const int nside = sched == EMT_SCHEDULE_BUCKETS ? (int)h->buckets.size() : emt_handle::kSide;
+  for (int i = 0; i < nside && !e; ++i) e = (int)cudaStreamWaitEvent(h->side[i], h->fork_ev, 0);
+  if (sched == EMT_SCHEDULE_BUCKETS) {
+    for (int i = 0; i < nside && !e; ++i) {
+      const emt_handle::Bucket& b = h->buckets[i];
+      emt::EpochArgs ab = a;
+      ab.order = h->d_order.p + n + b.first;
+      ab.smem_bytes = b.smem;
+      e = emt_launch_epoch_noattr(ab, b.count, h->side[i], tm);
+    }
+  } else {
+    for (int k = 0; k < n && !e; ++k) {
+      const int t = h->order[k];
+      emt::EpochArgs at = a;
+      at.single_task = t;
+      at.smem_bytes = h->task_smem[t];
+      e = emt_launch_epoch_noattr(at, 1, h->side[k % emt_handle::kSide], tm);
+    }
+  }
+  for (int i = 0; i < nside && !e; ++i) {
+    e = (int)cudaEventRecord(h->join_ev[i], h->side[i]);
+    if (!e) e = (int)cudaStreamWaitEvent(stream, h->join_ev[i], 0);
+  }
+  return e;
+}
+
+int enqueue_plan(emt_handle* h, const std::vector<EpochStep>& plan, int sched, cudaStream_t stream) {
+  const int interval = transfer_interval_of(h);
+  for (const EpochStep& s : plan) {
+    emt::EpochArgs a = base_args(h, emt::MODE_EPOCH);
+    a.gens = s.gens;
+    if (interval) {
+      a.transfer_import = s.imp;
+      a.transfer_export = s.exp;
+      a.elites_in = h->d_elites[s.parity ^ 1].p;
+      a.elites_out = h->d_elites[s.parity].p;
+    }
+    const int e = launch_sched(h, a, sched, stream);
+    if (e) return e;
+  }
+  return 0;
+}
+
+// Launches a plan on `stream` (directly, or as a CUDA graph captured once
+// per distinct plan and replayed), between the handle's timing events.
+int run_plan(emt_handle* h, const std::vector<EpochStep>& plan, int sched, bool graph,
+             cudaStream_t stream) {
+  if (sched != EMT_SCHEDULE_SINGLE || graph) {
+    const int rc = ensure_side(h);
+    if (rc) return rc;
+  }
+  int e = emt_epoch_smem_attr(h->use_tc, h->smem_bytes);
+  if (e) return h->cuda_fail((cudaError_t)e, "shared-memory attribute");
+  cudaEventRecord(h->ev0, stream);
+  if (graph && !plan.empty()) {
+    std::vector<int64_t> key{sched};
+    for (const EpochStep& s : plan) {
+      key.push_back(s.gens);
+      key.push_back(s.imp | (s.exp << 1) | (s.parity << 2));
+    }
+    if (!h->gexec || key != h->gkey) {
+      if (h->gexec) cudaGraphExecDestroy(h->gexec);
+      h->gexec = nullptr;
+      h->gkey.clear();
+      cudaGraph_t g = nullptr;
+      e = (int)cudaStreamBeginCapture(h->cap, cudaStreamCaptureModeThreadLocal);
+      if (!e) {
+        const int le = enqueue_plan(h, plan, sched, h->cap);
+        e = (int)cudaStreamEndCapture(h->cap, &g);
+        if (le) e = le;
+      }
+      if (!e) e = (int)cudaGraphInstantiate(&h->gexec, g, 0);
+      if (g) cudaGraphDestroy(g);
+      if (e) {
+        h->gexec = nullptr;
+        return h->cuda_fail((cudaError_t)e, "epoch graph capture");
+      }
+      h->gkey = key;
+    }
+    e = (int)cudaGraphLaunch(h->gexec, stream);
+  } else {
+    e = enqueue_plan(h, plan, sched, stream);
+  }
+  if (e) return h->cuda_fail((cudaError_t)e, "epoch launch");
+  cudaEventRecord(h->ev1, stream);
+  h->timing_pending = true;
+  return EMT_OK;
+}
+
 int check_task(const emt_handle* h, int32_t task) {
   return (task >= 0 && task < (int32_t)h->tasks.size()) ? EMT_OK : EMT_ERR_INVALID_ARG;
 }
@@ -484,6 +694,9 @@ int emt_create(const emt_config* cfg, emt_handle_t** out) {
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return EMT_ERR_CUDA;
   if (cfg->device < 0 || cfg->device >= ndev) return EMT_ERR_INVALID_ARG;
+  if (cfg->schedule < EMT_SCHEDULE_AUTO || cfg->schedule > EMT_SCHEDULE_PER_TASK ||
+      (cfg->use_graph != 0 && cfg->use_graph != 1))
+    return EMT_ERR_INVALID_ARG;
   emt_handle* h = new (std::nothrow) emt_handle();
   if (!h) return EMT_ERR_OUT_OF_MEMORY;
   h->cfg = *cfg;
@@ -603,36 +816,46 @@ int emt_run(emt_handle_t* h, int32_t generations, void* stream) {
     if (rc) return rc;
   }
   h->stream = (cudaStream_t)stream;
-  const int n = (int)h->tasks.size();
-  const int interval = (h->cfg.transfer_interval > 0 && n > 1) ? h->cfg.transfer_interval : 0;
-  cudaEventRecord(h->ev0, h->stream);
-  int left = generations;
-  while (left > 0) {
-    int g = left;
-    bool do_import = false, do_export = false;
-    if (interval) {
-      do_import = h->gdone > 0 && (h->gdone % (uint32_t)interval) == 0;
-      int to_boundary = interval - (int)(h->gdone % (uint32_t)interval);
-      g = std::min(left, to_boundary);
-      do_export = ((h->gdone + (uint32_t)g) % (uint32_t)interval) == 0;
-    }
-    emt::EpochArgs a = base_args(h, emt::MODE_EPOCH);
-    a.gens = g;
-    if (interval) {
-      a.transfer_import = do_import ? 1 : 0;
-      a.transfer_export = do_export ? 1 : 0;
-      a.elites_in = h->d_elites[h->elite_parity ^ 1].p;
-      a.elites_out = h->d_elites[h->elite_parity].p;
-    }
-    int e = launch_epoch(h, a, n, stream);
-    if (e) return h->cuda_fail((cudaError_t)e, "epoch launch");
-    if (interval && do_export) h->elite_parity ^= 1;
-    h->gdone += (uint32_t)g;
-    left -= g;
-  }
-  cudaEventRecord(h->ev1, h->stream);
-  h->timing_pending = true;
+  const std::vector<EpochStep> plan = plan_epochs(h, generations);
+  const int rc = run_plan(h, plan, effective_schedule(h), effective_graph(h), h->stream);
+  if (rc) return rc;
+  apply_plan(h, plan);
   return EMT_OK;
+}
+
+int emt_tune(emt_handle_t* h, int32_t generations, void* stream, int32_t* chosen) {
+  if (!h) return EMT_ERR_INVALID_ARG;
+  if (generations <= 0) return h->fail(EMT_ERR_INVALID_ARG, "tuning needs generations > 0");
+  if (!h->initialized) {
+    int rc = emt_reset(h, stream);
+    if (rc) return rc;
+  }
+  h->stream = (cudaStream_t)stream;
+  std::vector<int> cands{EMT_SCHEDULE_SINGLE, EMT_SCHEDULE_SINGLE | 0x100};
+  if (h->buckets.size() > 1) {
+    cands.push_back(EMT_SCHEDULE_BUCKETS);
+    cands.push_back(EMT_SCHEDULE_BUCKETS | 0x100);
+  }
+  int best = 0;
+  float best_ms = 0.f;
+  for (int c : cands) {
+    const std::vector<EpochStep> plan = plan_epochs(h, generations);
+    int rc = run_plan(h, plan, c & 0xFF, (c & 0x100) != 0, h->stream);
+    if (rc) return rc;
+    apply_plan(h, plan);
+    cudaError_t e = cudaEventSynchronize(h->ev1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    if (e != cudaSuccess) return h->cuda_fail(e, "tuning");
+    h->timing_pending = false;
+    if (!best || ms < best_ms) {
+      best = c;
+      best_ms = ms;
+    }
+  }
+  h->tuned = best;
+  if (chosen) *chosen = best;
+  return emt_sync(h);
 }
 
 // ---------------------------------------------------------------------------
@@ -912,6 +1135,13 @@ int emt_get_stats(emt_handle_t* h, emt_stats* out) {
     out->generations = h->initialized ? (uint64_t)h->gdone * h->tasks.size() : 0;
   }
   out->device_ms = h->device_ms;
+  if (h->uploaded) {
+    const int sched = effective_schedule(h);
+    out->schedule_used = sched | (effective_graph(h) ? 0x100 : 0);
+    out->epoch_launches = sched == EMT_SCHEDULE_SINGLE ? 1
+                          : sched == EMT_SCHEDULE_BUCKETS ? (int32_t)h->buckets.size()
+                                                          : (int32_t)h->tasks.size();
+  }
   return EMT_OK;
 }
 
@@ -1032,6 +1262,13 @@ void emt_destroy(emt_handle_t* h) {
   h->d_err.release();
   h->d_best_idx.release();
   h->d_qtc.release();
+  if (h->gexec) cudaGraphExecDestroy(h->gexec);
+  for (int i = 0; i < emt_handle::kSide; ++i) {
+    if (h->side[i]) cudaStreamDestroy(h->side[i]);
+    if (h->join_ev[i]) cudaEventDestroy(h->join_ev[i]);
+  }
+  if (h->fork_ev) cudaEventDestroy(h->fork_ev);
+  if (h->cap) cudaStreamDestroy(h->cap);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   delete h;

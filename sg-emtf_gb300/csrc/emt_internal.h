@@ -211,5 +211,8 @@ struct BestArgs {
 // Kernel launchers (emt_kernels.cu).  tmap: the CUtensorMap of the B
 // operand tiles (tensor-core form), or null for the FP32 form.
 int emt_launch_epoch(const emt::EpochArgs& a, int grid, void* stream, const void* tmap = nullptr);
+int emt_launch_epoch_noattr(const emt::EpochArgs& a, int grid, void* stream, const void* tmap);
+int emt_epoch_smem_attr(bool tc, size_t bytes);
+int emt_epoch_occupancy(bool tc, size_t bytes);
 int emt_launch_eval(const emt::EvalArgs& a, void* stream);
 int emt_launch_best(const emt::BestArgs& a, void* stream);

@@ -900,6 +900,39 @@ int emt_launch_epoch(const emt::EpochArgs& a, int grid, void* stream, const void
   return (int)cudaGetLastError();
 }
 
+// Epoch launch without touching the function's shared-memory attribute (the
+// caller has raised it to cover a.smem_bytes); usable inside stream capture.
+int emt_launch_epoch_noattr(const emt::EpochArgs& a, int grid, void* stream, const void* tmap) {
+  if (grid <= 0) return 0;
+  if (tmap)
+    emt::epoch_kernel_tc<<<grid, emt::kThreads, a.smem_bytes, (cudaStream_t)stream>>>(
+        a, *reinterpret_cast<const CUtensorMap*>(tmap));
+  else
+    emt::epoch_kernel<<<grid, emt::kThreads, a.smem_bytes, (cudaStream_t)stream>>>(a);
+  return (int)cudaGetLastError();
+}
+
+// Raises the epoch kernel's dynamic shared-memory limit to bytes.
+int emt_epoch_smem_attr(bool tc, size_t bytes) {
+  const cudaError_t e =
+      tc ? cudaFuncSetAttribute(emt::epoch_kernel_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)bytes)
+         : cudaFuncSetAttribute(emt::epoch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)bytes);
+  return (int)e;
+}
+
+// Resident CTAs per SM of the epoch kernel with `bytes` of dynamic shared
+// memory (0 if it cannot launch).
+int emt_epoch_occupancy(bool tc, size_t bytes) {
+  int n = 0;
+  if (emt_epoch_smem_attr(tc, bytes) != 0) return 0;
+  const cudaError_t e =
+      tc ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, emt::epoch_kernel_tc, emt::kThreads, bytes)
+         : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, emt::epoch_kernel, emt::kThreads, bytes);
+  return e == cudaSuccess ? n : 0;
+}
+
 int emt_launch_eval(const emt::EvalArgs& a, void* stream) {
   const int grid = (a.n + 63) / 64;
   if (grid <= 0) return 0;

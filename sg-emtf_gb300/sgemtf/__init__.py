@@ -33,12 +33,13 @@ FLAG_REF_BOXES = 0x8
 FLAG_NO_RECHECK = 0x10
 FLAG_RIGOROUS_WINDOW = 0x20
 FLAG_NO_DIFF_RECHECK = 0x40
+SCHEDULE_AUTO, SCHEDULE_SINGLE, SCHEDULE_BUCKETS, SCHEDULE_PER_TASK = 0, 1, 2, 3
 MAX_DIM, MAX_POP = 128, 256
 NOALLOC_EXCHANGE_FLOATS = 1 << 19
 
 EXPORTED = [
     "emt_config_default", "emt_function_from_reference", "emt_function_box", "emt_create",
-    "emt_add_tasks", "emt_reset", "emt_run", "emt_run_noalloc", "emt_sync", "emt_get_best", "emt_get_best_all",
+    "emt_add_tasks", "emt_reset", "emt_run", "emt_run_noalloc", "emt_tune", "emt_sync", "emt_get_best", "emt_get_best_all",
     "emt_get_population", "emt_set_population", "emt_get_task_params", "emt_evaluate",
     "emt_get_stats", "emt_snapshot_size", "emt_snapshot", "emt_restore", "emt_last_error",
     "emt_status_string", "emt_destroy",
@@ -55,7 +56,8 @@ class Config(ctypes.Structure):
                 ("transfer_interval", ctypes.c_int32), ("transfer_rate", ctypes.c_float),
                 ("transfer_mix", ctypes.c_float), ("flags", ctypes.c_uint32),
                 ("seed", ctypes.c_uint64), ("recheck_rel", ctypes.c_double),
-                ("device", ctypes.c_int32), ("reserved", ctypes.c_int32 * 7)]
+                ("device", ctypes.c_int32), ("schedule", ctypes.c_int32),
+                ("use_graph", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5)]
 
     def __init__(self, **kw):
         super().__init__()
@@ -80,7 +82,8 @@ class Stats(ctypes.Structure):
                 ("transfers_accepted", ctypes.c_uint64), ("device_ms", ctypes.c_double),
                 ("n_tasks", ctypes.c_int32), ("precision_used", ctypes.c_int32),
                 ("recheck_differential", ctypes.c_uint64), ("anchor_rotations", ctypes.c_uint64),
-                ("recheck_identical", ctypes.c_uint64)]
+                ("recheck_identical", ctypes.c_uint64), ("epoch_launches", ctypes.c_int32),
+                ("schedule_used", ctypes.c_int32)]
 
 
 class TaskDesc:
@@ -155,6 +158,7 @@ def lib():
         L.emt_reset.argtypes = [vp, vp]
         L.emt_run.argtypes = [vp, i32, vp]
         L.emt_run_noalloc.argtypes = [vp, i32, vp]
+        L.emt_tune.argtypes = [vp, i32, vp, ctypes.POINTER(ctypes.c_int32)]
         L.emt_sync.argtypes = [vp]
         L.emt_get_best.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_double), f32p]
         L.emt_get_best_all.argtypes = [vp, f32p]
@@ -238,6 +242,13 @@ class Engine:
         self._check(lib().emt_run(self._h, int(generations), stream), "emt_run")
         if sync:
             self.sync()
+
+    def tune(self, generations, stream=None):
+        """emt_tune: time the launch schedules on real generations, keep the
+        fastest; returns schedule | 0x100 when graph replay won."""
+        out = ctypes.c_int32(0)
+        self._check(lib().emt_tune(self._h, int(generations), stream, ctypes.byref(out)), "emt_tune")
+        return out.value
 
     def run_noalloc(self, generations, stream=None, sync=True):
         """emt_run_noalloc: allocates nothing (needs a prior reset())."""
