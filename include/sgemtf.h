@@ -167,7 +167,14 @@ typedef struct emt_task_desc {
   const float* shift;            /* D floats; NULL draws o ~ U(0.8 * box)   */
 } emt_task_desc;
 
-#define EMT_MAX_DIM 128
+/* Islands with D <= EMT_MAX_FUSED_DIM run in the fused kernel (one CTA per
+ * island, state in shared memory).  A handle holding any task with a larger
+ * D (up to EMT_MAX_DIM, e.g. 256 tasks of D = 1000) runs every island as an
+ * HBM-resident pipeline instead: trial kernel, rotation GEMM (tcgen05
+ * tensor cores or FP32 CUDA cores), evaluation, selection; emt_evaluate and
+ * emt_run_noalloc return EMT_ERR_UNSUPPORTED for such a handle. */
+#define EMT_MAX_DIM 1024
+#define EMT_MAX_FUSED_DIM 128
 #define EMT_MAX_POP 256
 
 typedef struct emt_stats {

@@ -17,6 +17,7 @@
 #include <new>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/sgemtf.h"
@@ -32,6 +33,7 @@ struct HostTask {
   std::vector<float> Q;  // D*D row-major, the operator the device applies
   std::vector<float> o;  // D
   float woff = 0.f, qnorm = 1.f;
+  uint32_t qr_id = 0;  // task id whose seeded rotation is still to be generated
   double woff64 = 0.0;
 };
 
@@ -105,6 +107,15 @@ struct emt_handle {
   int tc_np = 0, tc_kp = 0;
   DevBuf<float> d_qtc;
   CUtensorMap tmap;
+  // large islands (any D > 128): HBM-resident pipeline (emt_large.cuh)
+  bool large = false, large_tc = false;
+  int lKp = 0, lNq = 0;
+  int64_t lrows = 0;
+  size_t lsel_smem = 0;
+  DevBuf<float> d_U, d_ftr, d_ttr, d_S, d_Z, d_qbig;
+  DevBuf<int64_t> d_srow, d_qrow;
+  DevBuf<int32_t> d_rank;
+  CUtensorMap smap, qmap;
 
   int fail(int code, const std::string& msg) {
     err = msg;
@@ -147,7 +158,9 @@ float weierstrass_reference_offset() {
 // matrix (Box-Muller on Philox words, purpose P_QR_NORMAL), column signs
 // fixed so that R has a positive diagonal.
 void seeded_rotation(uint64_t seed, uint32_t task, int D, std::vector<double>& Q) {
-  std::vector<double> A((size_t)D * D), v(D);
+  // A is held column-major (At[c][i] = A[i][c]) so the Householder column
+  // updates run over contiguous memory; every sum keeps its order.
+  std::vector<double> At((size_t)D * D), v(D);
   for (int r = 0; r < D; ++r)
     for (int c = 0; c < D; c += 4) {
       emt::U4 w = emt::draw(seed, task, 0, (uint32_t)r, emt::P_QR_NORMAL, (uint32_t)(c >> 2));
@@ -157,29 +170,31 @@ void seeded_rotation(uint64_t seed, uint32_t task, int D, std::vector<double>& Q
         double u2 = (double)ww[2 * h + 1] * 0x1p-32;
         double rad = std::sqrt(-2.0 * std::log(u1));
         double th = 6.283185307179586 * u2;
-        if (c + 2 * h < D) A[(size_t)r * D + c + 2 * h] = rad * std::cos(th);
-        if (c + 2 * h + 1 < D) A[(size_t)r * D + c + 2 * h + 1] = rad * std::sin(th);
+        if (c + 2 * h < D) At[(size_t)(c + 2 * h) * D + r] = rad * std::cos(th);
+        if (c + 2 * h + 1 < D) At[(size_t)(c + 2 * h + 1) * D + r] = rad * std::sin(th);
       }
     }
   Q.assign((size_t)D * D, 0.0);
   for (int i = 0; i < D; ++i) Q[(size_t)i * D + i] = 1.0;
   for (int k = 0; k < D - 1; ++k) {
     double nrm = 0.0;
-    for (int i = k; i < D; ++i) nrm += A[(size_t)i * D + k] * A[(size_t)i * D + k];
+    const double* ak = At.data() + (size_t)k * D;
+    for (int i = k; i < D; ++i) nrm += ak[i] * ak[i];
     nrm = std::sqrt(nrm);
     if (nrm == 0.0) continue;
-    double alpha = A[(size_t)k * D + k] > 0 ? -nrm : nrm;
+    double alpha = ak[k] > 0 ? -nrm : nrm;
     std::fill(v.begin(), v.end(), 0.0);
-    for (int i = k; i < D; ++i) v[i] = A[(size_t)i * D + k];
+    for (int i = k; i < D; ++i) v[i] = ak[i];
     v[k] -= alpha;
     double vn = 0.0;
     for (int i = k; i < D; ++i) vn += v[i] * v[i];
     if (vn == 0.0) continue;
     for (int c = k; c < D; ++c) {
+      double* ac = At.data() + (size_t)c * D;
       double s = 0.0;
-      for (int i = k; i < D; ++i) s += v[i] * A[(size_t)i * D + c];
+      for (int i = k; i < D; ++i) s += v[i] * ac[i];
       s = 2.0 * s / vn;
-      for (int i = k; i < D; ++i) A[(size_t)i * D + c] -= s * v[i];
+      for (int i = k; i < D; ++i) ac[i] -= s * v[i];
     }
     for (int r = 0; r < D; ++r) {
       double s = 0.0;
@@ -189,7 +204,7 @@ void seeded_rotation(uint64_t seed, uint32_t task, int D, std::vector<double>& Q
     }
   }
   for (int c = 0; c < D; ++c)
-    if (A[(size_t)c * D + c] < 0)
+    if (At[(size_t)c * D + c] < 0)
       for (int r = 0; r < D; ++r) Q[(size_t)r * D + c] = -Q[(size_t)r * D + c];
 }
 
@@ -257,6 +272,85 @@ int encode_qtc_map(emt_handle* h) {
   return EMT_OK;
 }
 
+// 3-D FP32 tensor map (K, rows, 2 planes), box (32, brows, 1), 128B swizzle.
+int encode_planes(emt_handle* h, CUtensorMap* map, float* base, int K, int64_t rows, int brows) {
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                                   cudaEnableDefault, &q);
+  if (e != cudaSuccess || !fn || q != cudaDriverEntryPointSuccess)
+    return h->fail(EMT_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  const cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, 2};
+  const cuuint64_t strides[2] = {(cuuint64_t)K * 4, (cuuint64_t)K * (cuuint64_t)rows * 4};
+  const cuuint32_t box[3] = {32, (cuuint32_t)brows, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = ((EncodeTiledFn)fn)(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box,
+                                   estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS)
+    return h->fail(EMT_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+  return EMT_OK;
+}
+
+// Buffers of the large-island pipeline: trials, trial fitness, ranks, the
+// rotation operands S (rows of a task padded to 128, Kp columns; FP32, or
+// TF32 hi and lo planes) and results Z (Nq columns), and for the tensor-core
+// form Q's TF32 hi/lo planes, Nq rows per task, with their TMA maps.
+int large_upload(emt_handle* h, int64_t pop, int32_t fit) {
+  const int n = (int)h->tasks.size();
+  int dmax = 1, dpmax = 4;
+  for (const auto& t : h->tasks) dmax = std::max(dmax, t.D);
+  dpmax = emt::round4(dmax);
+  h->lKp = emt::round32(dmax);
+  h->lNq = (dmax + emt::kLargeBN - 1) / emt::kLargeBN * emt::kLargeBN;
+  std::vector<int64_t> srow(n), qrow(n);
+  int64_t rows = 0;
+  for (int t = 0; t < n; ++t) {
+    srow[t] = rows;
+    rows += (h->tasks[t].NP + emt::kLargeBM - 1) / emt::kLargeBM * emt::kLargeBM;
+    qrow[t] = (int64_t)t * h->lNq;
+  }
+  h->lrows = rows;
+  h->lsel_smem = emt::large_select_smem(dpmax);
+  const int planes = h->large_tc ? 2 : 1;
+  cudaError_t e;
+  if ((e = h->d_U.ensure((size_t)pop)) || (e = h->d_ftr.ensure((size_t)fit)) ||
+      (e = h->d_ttr.ensure((size_t)fit)) || (e = h->d_rank.ensure((size_t)fit)) ||
+      (e = h->d_srow.ensure(n)) || (e = h->d_qrow.ensure(n)) ||
+      (e = h->d_S.ensure((size_t)planes * rows * h->lKp)) ||
+      (e = h->d_Z.ensure((size_t)rows * h->lNq)))
+    return h->cuda_fail(e, "cudaMalloc");
+  if ((e = cudaMemcpy(h->d_srow.p, srow.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice)) ||
+      (e = cudaMemcpy(h->d_qrow.p, qrow.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice)) ||
+      (e = cudaMemset(h->d_S.p, 0, sizeof(float) * h->d_S.n)) ||
+      (e = cudaMemset(h->d_Z.p, 0, sizeof(float) * h->d_Z.n)) ||
+      (e = cudaMemset(h->d_U.p, 0, sizeof(float) * (size_t)pop)))
+    return h->cuda_fail(e, "upload");
+  if (!h->large_tc) return EMT_OK;
+  const size_t plane = (size_t)n * h->lNq * h->lKp, per = (size_t)h->lNq * h->lKp;
+  if ((e = h->d_qbig.ensure(2 * plane))) return h->cuda_fail(e, "cudaMalloc");
+  std::vector<float> hi(per), lo(per);
+  for (int t = 0; t < n; ++t) {
+    const HostTask& ht = h->tasks[t];
+    std::fill(hi.begin(), hi.end(), 0.f);
+    std::fill(lo.begin(), lo.end(), 0.f);
+    for (int r = 0; r < ht.D; ++r)
+      for (int c = 0; c < ht.D; ++c) {
+        const float v = ht.Q[(size_t)r * ht.D + c];
+        const float vh = tf32_hi(v);
+        hi[(size_t)r * h->lKp + c] = vh;
+        lo[(size_t)r * h->lKp + c] = v - vh;
+      }
+    if ((e = cudaMemcpy(h->d_qbig.p + (size_t)t * per, hi.data(), sizeof(float) * per, cudaMemcpyHostToDevice)) ||
+        (e = cudaMemcpy(h->d_qbig.p + plane + (size_t)t * per, lo.data(), sizeof(float) * per, cudaMemcpyHostToDevice)))
+      return h->cuda_fail(e, "upload");
+  }
+  int rc = encode_planes(h, &h->smap, h->d_S.p, h->lKp, rows, emt::kLargeBM);
+  if (!rc) rc = encode_planes(h, &h->qmap, h->d_qbig.p, h->lKp, (int64_t)n * h->lNq, emt::kLargeBN);
+  return rc;
+}
+
 int upload(emt_handle* h) {
   if (h->uploaded) return EMT_OK;
   const int n = (int)h->tasks.size();
@@ -293,7 +387,14 @@ int upload(emt_handle* h) {
     smem = std::max(smem, emt::smem_layout(ht.D, ht.NP, d.qt_in_smem != 0).total);
   }
   h->use_tc = false;
-  if (h->cfg.precision != EMT_ROT_FP32) {
+  h->large = false;
+  for (const auto& t : h->tasks) h->large |= t.D > emt::kMaxDim;
+  if (h->large) {
+    h->large_tc = h->cfg.precision != EMT_ROT_FP32 && device_has_tcgen05(h->device);
+    if (!h->large_tc && h->cfg.precision == EMT_ROT_TF32X3)
+      return h->fail(EMT_ERR_UNSUPPORTED, "tensor-core form needs an sm_10x device");
+    smem = 0;
+  } else if (h->cfg.precision != EMT_ROT_FP32) {
     int np = 0, kp = 0;
     const bool ok = device_has_tcgen05(h->device) && tc_fits(h->tasks, np, kp);
     if (!ok && h->cfg.precision == EMT_ROT_TF32X3)
@@ -324,8 +425,8 @@ int upload(emt_handle* h) {
   cudaError_t e0 = cudaSetDevice(h->device);
   if (e0 != cudaSuccess) return h->cuda_fail(e0, "cudaSetDevice");
   h->task_smem.assign(n, 0);
-  std::vector<int> occ(n, 0);
-  for (int t = 0; t < n; ++t) {
+  std::vector<int> occ(n, 1);
+  for (int t = 0; t < n && !h->large; ++t) {
     const HostTask& ht = h->tasks[t];
     h->task_smem[t] = h->use_tc ? emt::tc_layout(ht.D, ht.NP, h->tc_np, h->tc_kp).total
                                 : emt::smem_layout(ht.D, ht.NP, h->table[t].qt_in_smem != 0).total;
@@ -335,7 +436,7 @@ int upload(emt_handle* h) {
   std::vector<int32_t> border(h->order);
   std::stable_sort(border.begin(), border.end(), [&](int a, int b) { return occ[a] < occ[b]; });
   h->buckets.clear();
-  for (int i = 0; i < n; ++i) {
+  for (int i = 0; i < n && !h->large; ++i) {
     const int t = border[i];
     if (h->buckets.empty() || occ[border[h->buckets.back().first]] != occ[t]) {
       emt_handle::Bucket b;
@@ -411,6 +512,10 @@ int upload(emt_handle* h) {
     if ((e = cudaMemcpy(h->d_qtc.p, hqc.data(), sizeof(float) * hqc.size(), cudaMemcpyHostToDevice)))
       return h->cuda_fail(e, "upload");
     int rc = encode_qtc_map(h);
+    if (rc) return rc;
+  }
+  if (h->large) {
+    int rc = large_upload(h, pop, fit);
     if (rc) return rc;
   }
   h->uploaded = true;
@@ -523,6 +628,86 @@ int ensure_side(emt_handle* h) {
   return e == cudaSuccess ? EMT_OK : h->cuda_fail(e, "side streams");
 }
 
+// ---- large islands: argument block and launch sequences ----
+
+emt::LargeArgs large_args(emt_handle* h) {
+  emt::LargeArgs a{};
+  a.tasks = h->d_tasks.p;
+  a.n_tasks = (int32_t)h->tasks.size();
+  a.Kp = h->lKp;
+  a.Nq = h->lNq;
+  a.tc = h->large_tc ? 1 : 0;
+  a.srow = h->d_srow.p;
+  a.qrow = h->d_qrow.p;
+  a.split = (int64_t)h->lrows * h->lKp;
+  a.pop = h->d_pop.p;
+  a.U = h->d_U.p;
+  a.fit32 = h->d_fit32.p;
+  a.tol32 = h->d_tol32.p;
+  a.fit64 = h->d_fit64.p;
+  a.ftr = h->d_ftr.p;
+  a.ttr = h->d_ttr.p;
+  a.qt = h->d_qt.p;
+  a.shift = h->d_shift.p;
+  a.S = h->d_S.p;
+  a.Z = h->d_Z.p;
+  a.gen = h->d_gen.p;
+  a.rank = h->d_rank.p;
+  a.algorithm = h->cfg.algorithm;
+  a.F = h->cfg.F;
+  a.CR = h->cfg.CR;
+  a.eta_c = h->cfg.eta_c;
+  a.p_c = h->cfg.p_c;
+  a.eta_m = h->cfg.eta_m;
+  a.p_m = h->cfg.p_m;
+  a.seed = h->cfg.seed;
+  a.recheck_rel = (float)(h->cfg.recheck_rel > 0 ? h->cfg.recheck_rel : 1e-5);
+  a.flags = h->cfg.flags;
+  a.transfer_rate = h->cfg.transfer_rate;
+  a.transfer_mix = h->cfg.transfer_mix;
+  a.stats = h->d_stats.p;
+  a.err = h->d_err.p;
+  a.select_smem = h->lsel_smem;
+  return a;
+}
+
+// fitness of every member: operands from the islands, rotation, evaluation
+int large_eval_members(emt_handle* h, cudaStream_t stream) {
+  const emt::LargeArgs a = large_args(h);
+  int e = emt_large_build(a, emt::large::BUILD_X, stream);
+  if (!e) e = emt_large_gemm(a, &h->smap, &h->qmap, stream);
+  if (!e) e = emt_large_eval(a, 0, emt::kMaxPop, stream);
+  return e;
+}
+
+// One generation: trials, rotation, evaluation, selection (4 launches).
+int large_generation(emt_handle* h, const emt::LargeArgs& a, cudaStream_t stream) {
+  int e = emt_large_build(a, emt::large::BUILD_TRIALS, stream);
+  if (!e) e = emt_large_gemm(a, &h->smap, &h->qmap, stream);
+  if (!e) e = emt_large_eval(a, 1, emt::kMaxPop, stream);
+  if (!e) e = emt_large_select(a, emt::large::SEL_GENERATION, stream);
+  return e;
+}
+
+int large_epoch(emt_handle* h, int gens, int imp, int exp, int parity, cudaStream_t stream) {
+  emt::LargeArgs a = large_args(h);
+  if (transfer_interval_of(h)) {
+    a.elites_in = h->d_elites[parity ^ 1].p;
+    a.elites_out = h->d_elites[parity].p;
+  }
+  int e = 0;
+  if (imp) {  // elite transfer in: rank, candidates, their fitness, strict selection
+    e = emt_large_select(a, emt::large::SEL_RANK, stream);
+    if (!e) e = emt_large_build(a, emt::large::BUILD_CANDIDATES, stream);
+    if (!e) e = emt_large_gemm(a, &h->smap, &h->qmap, stream);
+    if (!e) e = emt_large_eval(a, 1, emt::kMaxPop, stream);
+    if (!e) e = emt_large_select(a, emt::large::SEL_IMPORT, stream);
+  }
+  for (int g = 0; g < gens && !e; ++g) e = large_generation(h, a, stream);
+  if (!e && exp) e = emt_large_select(a, emt::large::SEL_EXPORT, stream);
+  return e;
+}
+
 // One epoch's islands under a schedule; stream receives every launch or
 // waits for them (fork/join through events), so the next epoch's transfer
 // sees all of this epoch's exports.
@@ -560,6 +745,13 @@ int launch_sched(emt_handle* h, emt::EpochArgs a, int sched, cudaStream_t stream
 
 int enqueue_plan(emt_handle* h, const std::vector<EpochStep>& plan, int sched, cudaStream_t stream) {
   const int interval = transfer_interval_of(h);
+  if (h->large) {
+    for (const EpochStep& s : plan) {
+      const int e = large_epoch(h, s.gens, s.imp, s.exp, s.parity, stream);
+      if (e) return e;
+    }
+    return 0;
+  }
   for (const EpochStep& s : plan) {
     emt::EpochArgs a = base_args(h, emt::MODE_EPOCH);
     a.gens = s.gens;
@@ -715,6 +907,7 @@ int emt_add_tasks(emt_handle_t* h, int32_t n, const emt_task_desc* td) {
   if (n < 0 || (n > 0 && !td)) return h->fail(EMT_ERR_INVALID_ARG, "bad task array");
   const int smem_cap = max_smem_optin(h->device);
   std::vector<HostTask> add;
+  std::vector<int> qr_pending;
   add.reserve(n);
   for (int i = 0; i < n; ++i) {
     const emt_task_desc& d = td[i];
@@ -725,7 +918,7 @@ int emt_add_tasks(emt_handle_t* h, int32_t n, const emt_task_desc* td) {
       return h->fail(EMT_ERR_INVALID_ARG, "task " + std::to_string(i) + ": dim out of range");
     if (d.pop < 4 || d.pop > EMT_MAX_POP)
       return h->fail(EMT_ERR_INVALID_ARG, "task " + std::to_string(i) + ": pop out of range");
-    if ((size_t)smem_cap < emt::smem_layout(d.dim, d.pop, false).total)
+    if (d.dim <= emt::kMaxDim && (size_t)smem_cap < emt::smem_layout(d.dim, d.pop, false).total)
       return h->fail(EMT_ERR_UNSUPPORTED, "task " + std::to_string(i) +
                                               ": island does not fit in shared memory");
     HostTask ht;
@@ -744,12 +937,10 @@ int emt_add_tasks(emt_handle_t* h, int32_t n, const emt_task_desc* td) {
       case EMT_ROTATION_IDENTITY:
         for (int k = 0; k < D; ++k) ht.Q[(size_t)k * D + k] = 1.f;
         break;
-      case EMT_ROTATION_SEEDED_QR: {
-        std::vector<double> Q;
-        seeded_rotation(h->cfg.seed, id, D, Q);
-        for (size_t k = 0; k < Q.size(); ++k) ht.Q[k] = (float)Q[k];
+      case EMT_ROTATION_SEEDED_QR:
+        qr_pending.push_back((int)add.size());  // generated below, in parallel
+        ht.qr_id = id;
         break;
-      }
       case EMT_ROTATION_DENSE:
         if (!d.rotation_matrix) return h->fail(EMT_ERR_INVALID_ARG, "dense rotation without matrix");
         for (size_t k = 0; k < (size_t)D * D; ++k) {
@@ -774,6 +965,30 @@ int emt_add_tasks(emt_handle_t* h, int32_t n, const emt_task_desc* td) {
         for (int qd = 0; qd < 4 && k + qd < D; ++qd) ht.o[k + qd] = emt::ffma(emt::u01(emt::word(w, qd)), r, a);
       }
     }
+    if (h->cfg.flags & EMT_FLAG_REF_WEIERSTRASS_CONST)
+      ht.woff64 = -(double)D * (double)weierstrass_reference_offset();
+    else
+      ht.woff64 = (double)D * (2.0 - 0x1p-20);
+    ht.woff = (float)ht.woff64;
+    add.push_back(std::move(ht));
+  }
+  // seeded rotations (an O(D^3) FP64 QR each) on all host cores
+  if (!qr_pending.empty()) {
+    const int nth = (int)std::min<size_t>(qr_pending.size(), std::max(1u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> pool;
+    for (int w = 0; w < nth; ++w)
+      pool.emplace_back([&, w] {
+        std::vector<double> Q;
+        for (size_t k = w; k < qr_pending.size(); k += nth) {
+          HostTask& ht = add[qr_pending[k]];
+          seeded_rotation(h->cfg.seed, ht.qr_id, ht.D, Q);
+          for (size_t e = 0; e < Q.size(); ++e) ht.Q[e] = (float)Q[e];
+        }
+      });
+    for (auto& th : pool) th.join();
+  }
+  for (auto& ht : add) {
+    const int D = ht.D;
     double qn = 0.0;
     for (int r = 0; r < D; ++r) {
       double s = 0.0;
@@ -781,12 +996,6 @@ int emt_add_tasks(emt_handle_t* h, int32_t n, const emt_task_desc* td) {
       qn = std::max(qn, std::sqrt(s));
     }
     ht.qnorm = (float)qn;
-    if (h->cfg.flags & EMT_FLAG_REF_WEIERSTRASS_CONST)
-      ht.woff64 = -(double)D * (double)weierstrass_reference_offset();
-    else
-      ht.woff64 = (double)D * (2.0 - 0x1p-20);
-    ht.woff = (float)ht.woff64;
-    add.push_back(std::move(ht));
   }
   for (auto& t : add) h->tasks.push_back(std::move(t));
   h->uploaded = false;
@@ -799,8 +1008,14 @@ int emt_reset(emt_handle_t* h, void* stream) {
   int rc = upload(h);
   if (rc) return rc;
   h->stream = (cudaStream_t)stream;
-  emt::EpochArgs a = base_args(h, emt::MODE_INIT);
-  int e = launch_epoch(h, a, (int)h->tasks.size(), stream);
+  int e;
+  if (h->large) {
+    e = emt_large_init(large_args(h), stream);
+    if (!e) e = large_eval_members(h, h->stream);
+  } else {
+    emt::EpochArgs a = base_args(h, emt::MODE_INIT);
+    e = launch_epoch(h, a, (int)h->tasks.size(), stream);
+  }
   if (e) return h->cuda_fail((cudaError_t)e, "init launch");
   h->initialized = true;
   h->gdone = 0;
@@ -890,6 +1105,8 @@ int emt_run_noalloc(emt_handle_t* h, int32_t generations, void* stream) {
   if (generations < 0) return h->fail(EMT_ERR_INVALID_ARG, "negative generation count");
   if (!h->initialized || !h->uploaded)
     return h->fail(EMT_ERR_STATE, "emt_run_noalloc needs a handle prepared by emt_reset");
+  if (h->large)
+    return h->fail(EMT_ERR_UNSUPPORTED, "emt_run_noalloc serves islands of D <= 128 only");
   const int n = (int)h->tasks.size();
   const int interval = (h->cfg.transfer_interval > 0 && n > 1) ? h->cfg.transfer_interval : 0;
   float* buf[2] = {nullptr, nullptr};
@@ -999,7 +1216,7 @@ int emt_get_best(emt_handle_t* h, int32_t task, double* fitness, float* x) {
   if (rc) return rc;
   emt::BestArgs b{h->d_tasks.p, (int32_t)h->tasks.size(), h->d_pop.p, h->d_fit32.p, h->d_fit64.p,
                   h->d_qt.p, h->d_shift.p, h->d_best_idx.p, h->d_best_f32.p, h->d_best_f64.p};
-  int e = emt_launch_best(b, h->stream);
+  int e = h->large ? emt_large_best(b, h->lKp, h->stream) : emt_launch_best(b, h->stream);
   if (e) return h->cuda_fail((cudaError_t)e, "best launch");
   if ((rc = emt_sync(h))) return rc;
   int32_t idx = 0;
@@ -1022,7 +1239,7 @@ int emt_get_best_all(emt_handle_t* h, float* fitness) {
   if (rc) return rc;
   emt::BestArgs b{h->d_tasks.p, (int32_t)h->tasks.size(), h->d_pop.p, h->d_fit32.p, h->d_fit64.p,
                   h->d_qt.p, h->d_shift.p, h->d_best_idx.p, h->d_best_f32.p, h->d_best_f64.p};
-  int e = emt_launch_best(b, h->stream);
+  int e = h->large ? emt_large_best(b, h->lKp, h->stream) : emt_launch_best(b, h->stream);
   if (e) return h->cuda_fail((cudaError_t)e, "best launch");
   cudaError_t ce = cudaMemcpyAsync(fitness, h->d_best_f32.p, sizeof(float) * h->tasks.size(),
                                    cudaMemcpyDeviceToHost, h->stream);
@@ -1057,9 +1274,16 @@ int emt_set_population(emt_handle_t* h, int32_t task, const float* x) {
   cudaError_t e = cudaMemcpy2D(h->d_pop.p + d.pop_off, sizeof(float) * d.DP, x, sizeof(float) * d.D,
                                sizeof(float) * d.D, d.NP, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return h->cuda_fail(e, "copy population");
-  emt::EpochArgs a = base_args(h, emt::MODE_EVAL);
-  a.single_task = task;
-  int le = launch_epoch(h, a, 1, h->stream);
+  int le;
+  if (h->large) {  // re-evaluates every island (unchanged ones get the same values)
+    e = cudaMemset(h->d_fit64.p + d.fit_off, 0xFF, sizeof(double) * d.NP);
+    if (e != cudaSuccess) return h->cuda_fail(e, "reset cache");
+    le = large_eval_members(h, h->stream);
+  } else {
+    emt::EpochArgs a = base_args(h, emt::MODE_EVAL);
+    a.single_task = task;
+    le = launch_epoch(h, a, 1, h->stream);
+  }
   if (le) return h->cuda_fail((cudaError_t)le, "evaluate launch");
   return emt_sync(h);
 }
@@ -1080,6 +1304,9 @@ int emt_evaluate(emt_handle_t* h, int32_t task, int32_t n, const float* x, float
   int rc = upload(h);
   if (rc) return rc;
   if (n == 0) return EMT_OK;
+  if (h->large)
+    return h->fail(EMT_ERR_UNSUPPORTED, "emt_evaluate serves islands of D <= 128; read a large "
+                                        "island's fitness with emt_get_population");
   const HostTask& t = h->tasks[task];
   float *dx = nullptr, *df = nullptr, *dz = nullptr;
   cudaError_t e;
@@ -1225,11 +1452,18 @@ int emt_restore(emt_handle_t* h, const void* buf, size_t bytes) {
   // rank by the same restored FP32 fitness, so the rows are identical).
   const int interval = (h->cfg.transfer_interval > 0 && h->tasks.size() > 1) ? h->cfg.transfer_interval : 0;
   if (interval && h->gdone > 0 && h->gdone % (uint32_t)interval == 0) {
-    emt::EpochArgs a = base_args(h, emt::MODE_EPOCH);
-    a.gens = 0;
-    a.transfer_export = 1;
-    a.elites_out = h->d_elites[0].p;
-    int e = launch_epoch(h, a, (int)h->tasks.size(), h->stream);
+    int e;
+    if (h->large) {
+      emt::LargeArgs la = large_args(h);
+      la.elites_out = h->d_elites[0].p;
+      e = emt_large_select(la, emt::large::SEL_EXPORT, h->stream);
+    } else {
+      emt::EpochArgs a = base_args(h, emt::MODE_EPOCH);
+      a.gens = 0;
+      a.transfer_export = 1;
+      a.elites_out = h->d_elites[0].p;
+      e = launch_epoch(h, a, (int)h->tasks.size(), h->stream);
+    }
     if (e) return h->cuda_fail((cudaError_t)e, "elite export");
     h->elite_parity = 1;
     return emt_sync(h);

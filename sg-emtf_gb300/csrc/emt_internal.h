@@ -76,6 +76,60 @@ struct EpochArgs {
   int32_t tc_np, tc_kp;       // tensor-core form: padded N and K of the B tiles
 };
 
+// Islands too large for one CTA's shared memory (D > kMaxDim, up to
+// kMaxDimLarge): each generation runs as a pipeline of kernels over
+// HBM-resident islands (emt_large.cuh).  Rotation operands: S holds one row
+// per member (rows of a task padded to a multiple of 128, Kp columns, zero
+// beyond D); Z receives Q (s) per row, Nq columns.
+constexpr int kMaxDimLarge = 1024;
+constexpr int kLargeBM = 128;  // GEMM tile rows (members)
+constexpr int kLargeBN = 256;  // GEMM tile columns (rotated genes), tensor-core form
+
+struct LargeArgs {
+  const TaskDev* tasks;
+  int32_t n_tasks;
+  int32_t Kp, Nq;        // padded GEMM K (multiple of 32) and N (multiple of 256)
+  int32_t tc;            // 1: S holds the TF32 hi part, S + split the lo part
+  const int64_t* srow;   // per task: first row of its block in S and Z
+  const int64_t* qrow;   // per task: first row of its Q tiles (tensor-core form)
+  int64_t split;         // floats between the hi and lo planes of S
+  float* pop;            // members, stride DP (TaskDev::pop_off)
+  float* U;              // trials, same layout
+  float* fit32;
+  float* tol32;
+  double* fit64;
+  float* ftr;            // trial fitness and window, same offsets as fit32
+  float* ttr;
+  const float* qt;       // FP32 Q^T per task (TaskDev::q_off)
+  const float* shift;
+  float* S;
+  float* Z;
+  uint32_t* gen;
+  int32_t* rank;         // per member: rank order of the task (byrank)
+  int32_t algorithm;
+  float F, CR, eta_c, p_c, eta_m, p_m;
+  uint64_t seed;
+  float recheck_rel;
+  uint32_t flags;
+  float transfer_rate, transfer_mix;
+  const float* elites_in;
+  float* elites_out;
+  unsigned long long* stats;
+  int32_t* err;
+  size_t select_smem;    // dynamic shared memory of the selection kernel
+};
+
+namespace large {
+enum BuildMode : int { BUILD_X = 0, BUILD_TRIALS = 1, BUILD_CANDIDATES = 2 };
+enum SelectMode : int { SEL_GENERATION = 0, SEL_IMPORT = 1, SEL_EXPORT = 2, SEL_RANK = 3 };
+}  // namespace large
+
+// Dynamic shared memory of the large-island selection kernel: per-warp
+// re-check scratch (2 DP doubles) and the flag/list/target/misc arrays.
+EMT_HD size_t large_select_smem(int DP) {
+  return sizeof(double) * kWarps * 2 * (size_t)DP + sizeof(int) * (4 * kMaxPop + 16);
+}
+
 // Arguments of the standalone evaluation kernel (emt_evaluate).
 struct EvalArgs {
   const TaskDev* tasks;
@@ -215,4 +269,11 @@ int emt_launch_epoch_noattr(const emt::EpochArgs& a, int grid, void* stream, con
 int emt_epoch_smem_attr(bool tc, size_t bytes);
 int emt_epoch_occupancy(bool tc, size_t bytes);
 int emt_launch_eval(const emt::EvalArgs& a, void* stream);
+// large islands (emt_large.cuh)
+int emt_large_init(const emt::LargeArgs& a, void* stream);
+int emt_large_build(const emt::LargeArgs& a, int mode, void* stream);
+int emt_large_gemm(const emt::LargeArgs& a, const void* smap, const void* qmap, void* stream);
+int emt_large_eval(const emt::LargeArgs& a, int which, int rows, void* stream);
+int emt_large_select(const emt::LargeArgs& a, int mode, void* stream);
+int emt_large_best(const emt::BestArgs& a, int maxD, void* stream);
 int emt_launch_best(const emt::BestArgs& a, void* stream);

@@ -942,3 +942,5 @@ int emt_launch_eval(const emt::EvalArgs& a, void* stream) {
   emt::eval_kernel<<<grid, emt::kThreads, a.smem_bytes, (cudaStream_t)stream>>>(a);
   return (int)cudaGetLastError();
 }
+
+#include "emt_large.cuh"

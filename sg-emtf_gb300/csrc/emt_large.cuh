@@ -1,0 +1,718 @@
+// emt_large.cuh -- islands too large for one CTA's shared memory (D up to
+// 1024; config 4: D = 1000, NP = 256, GA).  Included at the end of
+// emt_kernels.cu, whose selection and ranking code it reuses.
+//
+// A generation is a pipeline of kernels over HBM-resident islands:
+//   build   trial genes (DE or GA, the same arithmetic and Philox stream as
+//           the fused kernel) and the rotation operand s = u - o, split into
+//           TF32 hi/lo planes for the tensor-core form;
+//   gemm    Z = S Q^T for every task: tcgen05.mma kind::tf32 (3 products,
+//           hi*hi + hi*lo + lo*hi, FP32 accumulation in tensor memory), 128 x
+//           256 tiles fed by TMA (128B swizzle) through a 2-stage mbarrier
+//           pipeline; or FP32 CUDA-core tiles (128 x 128, 8 x 8 per thread);
+//   eval    one warp per row: f and its rounding window from the Z row;
+//   select  one CTA per task: the fused kernel's selection with its near-tie
+//           re-check (global-memory operands, shared-memory scratch).
+// Elite transfer reuses rank/select with the candidates in the trial rows.
+#pragma once
+
+namespace emt {
+namespace large {
+
+__device__ __forceinline__ bool large_ok(const TaskDev& t) {
+  return t.D >= 1 && t.D <= kMaxDimLarge && t.NP >= 4 && t.NP <= kMaxPop && t.DP == round4(t.D);
+}
+
+__device__ __forceinline__ FnConst fn_const(const TaskDev& td, float rel) {
+  FnConst fc;
+  fc.fid = td.fid;
+  fc.D = td.D;
+  fc.flags = td.flags;
+  fc.woff = td.woff;
+  fc.qnorm = td.qnorm;
+  fc.rel = rel;
+  fc.woff64 = td.woff64;
+  return fc;
+}
+
+// Transfer partner and candidate count of task t at generation gen0 (the
+// fused kernel's rule); -1 when there is none.
+__device__ __forceinline__ int transfer_partner(const LargeArgs& a, int t, uint32_t gen0, int& k) {
+  if (a.n_tasks < 2) return -1;
+  const U4 w = draw(a.seed, (uint32_t)t, gen0, 0u, P_TRANSFER_PARTNER, 0);
+  uint32_t p = w.x % (uint32_t)(a.n_tasks - 1);
+  if (p >= (uint32_t)t) ++p;
+  const TaskDev pd = a.tasks[p];
+  if (!large_ok(pd)) return -1;
+  const int kt = transfer_k(a.transfer_rate, a.tasks[t].NP), kp = transfer_k(a.transfer_rate, pd.NP);
+  k = kt < kp ? kt : kp;
+  return (int)p;
+}
+
+// Operand row of s = v - o: FP32 (FP32 form) or TF32 hi/lo planes.
+__device__ __forceinline__ void put_s(const LargeArgs& a, int64_t row, int j, float v) {
+  float* p = a.S + row * a.Kp + j;
+  if (a.tc) {
+    const float hi = tc::tf32_round(v);
+    p[0] = hi;
+    p[a.split] = v - hi;
+  } else {
+    p[0] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// initial islands (the fused kernel's MODE_INIT draw)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) init_kernel(const LargeArgs a) {
+  const int task = blockIdx.y;
+  const TaskDev td = a.tasks[task];
+  if (!large_ok(td)) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) atomicCAS(a.err, 0, CHECK_BAD_DESCRIPTOR);
+    return;
+  }
+  const int D = td.D, NP = td.NP, DP = td.DP, nb = (D + 3) >> 2;
+  const float r = fsub(td.hi, td.lo);
+  float* X = a.pop + td.pop_off;
+  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < NP * nb; it += gridDim.x * blockDim.x) {
+    const int i = it / nb, b = it - i * nb;
+    const U4 w = draw(a.seed, (uint32_t)task, 0u, (uint32_t)i, P_POP_INIT, (uint32_t)b);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int j = 4 * b + q;
+      if (j < D) X[(size_t)i * DP + j] = fminf(ffma(u01(word(w, q)), r, td.lo), td.hi);
+    }
+    if (4 * b + 4 >= DP)
+      for (int j = D; j < DP; ++j) X[(size_t)i * DP + j] = 0.f;
+    if (b == 0) a.fit64[td.fit_off + i] = __longlong_as_double(0x7FF8000000000000ll);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.gen[task] = 0u;
+    if (a.stats) atomicAdd(a.stats + 3, (unsigned long long)NP);  // the initial evaluation
+  }
+}
+
+// ---------------------------------------------------------------------------
+// trial rows and rotation operands; one CTA per (task, 8 members)
+// ---------------------------------------------------------------------------
+constexpr int kBuildRows = 8;
+
+__global__ void __launch_bounds__(256) build_kernel(const LargeArgs a, int mode) {
+  __shared__ int sidx[kBuildRows][4];
+  __shared__ int spart[kBuildRows];
+  const int task = blockIdx.y;
+  const TaskDev td = a.tasks[task];
+  if (!large_ok(td)) return;
+  const int D = td.D, NP = td.NP, DP = td.DP;
+  const int i0 = blockIdx.x * kBuildRows;
+  if (i0 >= NP) return;
+  const int nrow = min(kBuildRows, NP - i0);
+  const float* X = a.pop + td.pop_off;
+  float* U = a.U + td.pop_off;
+  const float* o = a.shift + td.o_off;
+  const int64_t srow = a.srow[task];
+  const float lo = td.lo, hi = td.hi;
+
+  if (mode == BUILD_X) {  // operands of the members themselves
+    for (int it = threadIdx.x; it < nrow * D; it += blockDim.x) {
+      const int r = it / D, j = it - r * D, i = i0 + r;
+      put_s(a, srow + i, j, fsub(X[(size_t)i * DP + j], o[j]));
+    }
+    return;
+  }
+  const uint32_t gen0 = a.gen[task];
+  if (mode == BUILD_CANDIDATES) {
+    int k = 0;
+    const int p = transfer_partner(a, task, gen0, k);
+    if (p < 0 || i0 >= k) return;
+    const TaskDev pd = a.tasks[p];
+    const float* el = a.elites_in + pd.elite_off;
+    const int* byrank = a.rank + td.fit_off;
+    const float rp = fsub(pd.hi, pd.lo), rt = fsub(td.hi, td.lo);
+    const int nc = min(nrow, k - i0);
+    for (int it = threadIdx.x; it < nc * D; it += blockDim.x) {
+      const int r = it / D, j = it - r * D, c = i0 + r;
+      const U4 wm = draw(a.seed, (uint32_t)task, gen0, (uint32_t)c, P_TRANSFER_MIX, (uint32_t)(j >> 2));
+      float v = X[(size_t)byrank[c] * DP + j];
+      if (j < pd.D && u01(word(wm, j & 3)) < a.transfer_mix) {
+        const float q = fdiv(fsub(el[(size_t)c * pd.DP + j], pd.lo), rp);
+        v = clamp_box(ffma(q, rt, td.lo), td.lo, td.hi);
+      }
+      U[(size_t)c * DP + j] = v;
+      put_s(a, srow + c, j, fsub(v, o[j]));
+    }
+    return;
+  }
+  // ---- trials of generation G ----
+  const uint32_t G = gen0 + 1u;
+  if (a.algorithm == 0 || a.algorithm == 1) {
+    if (threadIdx.x < nrow) {
+      const int i = i0 + threadIdx.x;
+      const U4 w = draw(a.seed, (uint32_t)task, G, (uint32_t)i, P_DE_INDEX, 0);
+      int r1, r2, r3, jr;
+      de_indices(w, i, NP, D, r1, r2, r3, jr);
+      sidx[threadIdx.x][0] = a.algorithm == 0 ? r1 : i;
+      sidx[threadIdx.x][1] = r2;
+      sidx[threadIdx.x][2] = r3;
+      sidx[threadIdx.x][3] = jr;
+    }
+    __syncthreads();
+    const int nb = (D + 3) >> 2;
+    for (int it = threadIdx.x; it < nrow * nb; it += blockDim.x) {
+      const int r = it / nb, b = it - r * nb, i = i0 + r;
+      const U4 w = draw(a.seed, (uint32_t)task, G, (uint32_t)i, P_DE_CR, (uint32_t)b);
+      const float* xb = X + (size_t)sidx[r][0] * DP;
+      const float* x2 = X + (size_t)sidx[r][1] * DP;
+      const float* x3 = X + (size_t)sidx[r][2] * DP;
+      const float* xi = X + (size_t)i * DP;
+      const int jr = sidx[r][3];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int j = 4 * b + q;
+        if (j < D) {
+          const float m = clamp_box(ffma(a.F, fsub(x2[j], x3[j]), xb[j]), lo, hi);
+          const float t = (u01(word(w, q)) < a.CR || j == jr) ? m : xi[j];
+          U[(size_t)i * DP + j] = t;
+          put_s(a, srow + i, j, fsub(t, o[j]));
+        }
+      }
+    }
+    return;
+  }
+  // GA: parent per member (CrossPrep), SBX on the pair (i, i^1), polynomial
+  // mutation -- the fused kernel's build_trials, gene for gene
+  if (threadIdx.x < nrow) {
+    const int i = i0 + threadIdx.x;
+    sidx[threadIdx.x][0] =
+        (int)(draw(a.seed, (uint32_t)task, G, (uint32_t)i, P_GA_PARENT, 0).x % (uint32_t)NP);
+    const int pi = i ^ 1;
+    spart[threadIdx.x] = pi < NP ? (int)(draw(a.seed, (uint32_t)task, G, (uint32_t)pi, P_GA_PARENT, 0).x %
+                                         (uint32_t)NP)
+                                 : sidx[threadIdx.x][0];
+  }
+  __syncthreads();
+  const float ec = fdiv(1.f, fadd(a.eta_c, 1.f));
+  const float em1 = fadd(a.eta_m, 1.f), em = fdiv(1.f, em1);
+  const float pm = a.p_m < 0.f ? fdiv(1.f, (float)D) : a.p_m;
+  const float range = fsub(hi, lo);
+  const int nb = (D + 1) >> 1;
+  for (int it = threadIdx.x; it < nrow * nb; it += blockDim.x) {
+    const int r = it / nb, b = it - r * nb, i = i0 + r;
+    const int r0 = sidx[r][0], partner = spart[r];
+    const U4 ws = draw(a.seed, (uint32_t)task, G, (uint32_t)i, P_GA_SBX, (uint32_t)b);
+    const U4 wm = draw(a.seed, (uint32_t)task, G, (uint32_t)i, P_GA_PM, (uint32_t)b);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int j = 2 * b + h;
+      if (j >= D) break;
+      const float x0 = X[(size_t)r0 * DP + j], x1 = X[(size_t)partner * DP + j];
+      float c;
+      if (u01(word(ws, 2 * h)) < a.p_c) {
+        const float pu = u01(word(ws, 2 * h + 1));
+        const float tv = pu <= 0.5f ? fmul(2.f, pu) : fdiv(0.5f, fsub(1.f, pu));
+        float beta = det_powf(tv, ec);
+        if (i & 1) beta = -beta;
+        c = fmul(0.5f, ffma(fadd(1.f, beta), x0, fmul(fsub(1.f, beta), x1)));
+        c = clamp_box(c, lo, hi);
+      } else {
+        c = x0;
+      }
+      if (u01(word(wm, 2 * h)) < pm) {
+        const float um = u01(word(wm, 2 * h + 1));
+        float dq;
+        if (um <= 0.5f) {
+          const float d1 = fdiv(fsub(c, lo), range);
+          const float v = ffma(fsub(1.f, fmul(2.f, um)), det_powf(fsub(1.f, d1), em1), fmul(2.f, um));
+          dq = fsub(det_powf(v, em), 1.f);
+        } else {
+          const float d2 = fdiv(fsub(hi, c), range);
+          const float v = ffma(fmul(2.f, fsub(um, 0.5f)), det_powf(fsub(1.f, d2), em1),
+                               fmul(2.f, fsub(1.f, um)));
+          dq = fsub(1.f, det_powf(v, em));
+        }
+        c = clamp_box(ffma(dq, range, c), lo, hi);
+      }
+      U[(size_t)i * DP + j] = c;
+      put_s(a, srow + i, j, fsub(c, o[j]));
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Z = S Q^T, FP32 form: 128 x 128 tiles, K step 16, 8 x 8 outputs per thread
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) gemm_f32_kernel(const LargeArgs a) {
+  constexpr int BM = 128, BN = 128, BK = 16;
+  __shared__ __align__(16) float As[BK][BM + 4];
+  __shared__ __align__(16) float Bs[BK][BN + 4];
+  const int task = blockIdx.z;
+  const TaskDev td = a.tasks[task];
+  if (!large_ok(td)) return;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  if (m0 >= td.NP || n0 >= td.D) return;
+  const int D = td.D, DP = td.DP;
+  const float* S = a.S + (a.srow[task] + m0) * (int64_t)a.Kp;
+  const float* QT = a.qt + td.q_off;  // QT[k * DP + n] = Q[n][k]
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  float acc[8][8];
+#pragma unroll
+  for (int r = 0; r < 8; ++r)
+#pragma unroll
+    for (int c = 0; c < 8; ++c) acc[r][c] = 0.f;
+  for (int k0 = 0; k0 < D; k0 += BK) {
+    // A tile: 128 rows x 16 k, transposed into As[k][row]
+    for (int it = threadIdx.x; it < BM * BK / 4; it += 256) {
+      const int r = it >> 2, kq = (it & 3) * 4;
+      const float4 v = *reinterpret_cast<const float4*>(S + (int64_t)r * a.Kp + k0 + kq);
+      As[kq + 0][r] = v.x;
+      As[kq + 1][r] = v.y;
+      As[kq + 2][r] = v.z;
+      As[kq + 3][r] = v.w;
+    }
+    // B tile: Q^T rows k0..k0+15, columns n0..n0+127 (zero beyond D)
+    for (int it = threadIdx.x; it < BK * BN; it += 256) {
+      const int kk = it / BN, n = it - kk * BN;
+      const int k = k0 + kk, col = n0 + n;
+      Bs[kk][n] = (k < D && col < D) ? QT[(int64_t)k * DP + col] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      float av[8], bv[8];
+      const float4 a0 = *reinterpret_cast<const float4*>(&As[kk][ty * 4]);
+      const float4 a1 = *reinterpret_cast<const float4*>(&As[kk][64 + ty * 4]);
+      const float4 b0 = *reinterpret_cast<const float4*>(&Bs[kk][tx * 4]);
+      const float4 b1 = *reinterpret_cast<const float4*>(&Bs[kk][64 + tx * 4]);
+      av[0] = a0.x; av[1] = a0.y; av[2] = a0.z; av[3] = a0.w;
+      av[4] = a1.x; av[5] = a1.y; av[6] = a1.z; av[7] = a1.w;
+      bv[0] = b0.x; bv[1] = b0.y; bv[2] = b0.z; bv[3] = b0.w;
+      bv[4] = b1.x; bv[5] = b1.y; bv[6] = b1.z; bv[7] = b1.w;
+#pragma unroll
+      for (int r = 0; r < 8; ++r)
+#pragma unroll
+        for (int c = 0; c < 8; ++c) acc[r][c] = fmaf(av[r], bv[c], acc[r][c]);
+    }
+    __syncthreads();
+  }
+  float* Z = a.Z + (a.srow[task] + m0) * (int64_t)a.Nq + n0;
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    const int row = (r < 4 ? ty * 4 + r : 64 + ty * 4 + r - 4);
+    if (m0 + row >= td.NP) continue;
+    float* zr = Z + (int64_t)row * a.Nq;
+    *reinterpret_cast<float4*>(zr + tx * 4) = make_float4(acc[r][0], acc[r][1], acc[r][2], acc[r][3]);
+    *reinterpret_cast<float4*>(zr + 64 + tx * 4) =
+        make_float4(acc[r][4], acc[r][5], acc[r][6], acc[r][7]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Z = S Q^T, tensor-core form: one CTA per (task, 128-row, 256-column) tile.
+// warp 0: TMA producer; warp 1: TMEM owner and MMA issuer; warps 2-5: epilogue
+// (tcgen05.ld lane quadrant = warp mod 4).  Every wait gives up after 2 s.
+// ---------------------------------------------------------------------------
+constexpr int kTcStages = 2;
+constexpr uint32_t kTileA = kLargeBM * 128;  // bytes of one 128-row x 32-float plane
+constexpr uint32_t kTileB = kLargeBN * 128;
+constexpr uint32_t kStageBytes = 2 * kTileA + 2 * kTileB;  // hi + lo of A and B
+constexpr size_t kGemmTcSmem = kTcStages * kStageBytes + 1024 + 128;
+
+__global__ void __launch_bounds__(192, 1)
+    gemm_tc_kernel(const LargeArgs a, const __grid_constant__ CUtensorMap smap,
+                   const __grid_constant__ CUtensorMap qmap) {
+  extern __shared__ __align__(16) unsigned char raw[];
+  unsigned char* base = (unsigned char*)(((uintptr_t)raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(base + kTcStages * kStageBytes);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 8);
+  int* ctl = reinterpret_cast<int*>(tslot + 1);  // [0] failed, [1] issued, [2] consumed
+  const int task = blockIdx.z;
+  const TaskDev td = a.tasks[task];
+  if (!large_ok(td)) return;
+  const int m0 = blockIdx.y * kLargeBM, n0 = blockIdx.x * kLargeBN;
+  if (m0 >= td.NP || n0 >= td.D) return;  // uniform: before any barrier
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t sbase = tc::smem_addr(base);
+  const uint32_t full0 = tc::smem_addr(bars), empty0 = tc::smem_addr(bars + 2),
+                 done = tc::smem_addr(bars + 4);
+  const int nkb = (td.D + 31) >> 5;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kTcStages; ++s) {
+      tc::mbar_init(full0 + 8 * s, 1);
+      tc::mbar_init(empty0 + 8 * s, 1);
+    }
+    tc::mbar_init(done, 1);
+    ctl[0] = ctl[1] = ctl[2] = 0;
+  }
+  if (warp == 1) tc::tmem_alloc(tslot, kLargeBN);
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = *tslot;
+  const int64_t srow = a.srow[task] + m0, qrow = a.qrow[task] + n0;
+
+  if (warp == 0 && lane == 0) {  // producer
+    for (int kb = 0; kb < nkb; ++kb) {
+      const int s = kb % kTcStages;
+      if (kb >= kTcStages && !tc::mbar_wait(empty0 + 8 * s, ((kb / kTcStages) - 1) & 1)) {
+        atomicExch(&ctl[0], 1);
+        break;
+      }
+      if (ctl[0]) break;
+      const uint32_t st = sbase + s * kStageBytes;
+      tc::mbar_expect_tx(full0 + 8 * s, kStageBytes);
+      tc::tma_load_3d(st, &smap, kb * 32, (int)srow, 0, full0 + 8 * s);
+      tc::tma_load_3d(st + kTileA, &smap, kb * 32, (int)srow, 1, full0 + 8 * s);
+      tc::tma_load_3d(st + 2 * kTileA, &qmap, kb * 32, (int)qrow, 0, full0 + 8 * s);
+      tc::tma_load_3d(st + 2 * kTileA + kTileB, &qmap, kb * 32, (int)qrow, 1, full0 + 8 * s);
+      ctl[1] = kb + 1;
+    }
+  } else if (warp == 1 && lane == 0) {  // MMA issuer
+    const uint32_t idesc = tc::idesc_tf32(kLargeBM, kLargeBN);
+    int kb = 0;
+    for (; kb < nkb; ++kb) {
+      const int s = kb % kTcStages;
+      if (!tc::mbar_wait(full0 + 8 * s, (kb / kTcStages) & 1)) {
+        atomicExch(&ctl[0], 1);
+        break;
+      }
+      tc::fence_after();
+      const uint32_t st = sbase + s * kStageBytes;
+      const uint32_t pa[3] = {0u, 0u, kTileA}, pb[3] = {0u, kTileB, 0u};
+      for (int p = 0; p < 3; ++p)
+        for (int ks = 0; ks < 4; ++ks) {
+          const uint64_t ad = tc::sdesc_sw128(st + pa[p] + 32u * ks);
+          const uint64_t bd = tc::sdesc_sw128(st + 2 * kTileA + pb[p] + 32u * ks);
+          tc::mma_tf32(tmem, ad, bd, idesc, (kb | p | ks) ? 1u : 0u);
+        }
+      tc::mma_commit(empty0 + 8 * s);
+      ctl[2] = kb + 1;
+    }
+    if (kb == nkb) tc::mma_commit(done);
+  } else if (warp >= 2) {  // epilogue
+    const bool ok = tc::mbar_wait(done, 0);
+    if (!ok && lane == 0) atomicExch(&ctl[0], 1);
+    tc::fence_after();
+    const int q = warp & 3;
+    const int row = m0 + 32 * q + lane;
+    if (ok) {
+      float* zr = a.Z + (a.srow[task] + row) * (int64_t)a.Nq + n0;
+      for (int c0 = 0; c0 < kLargeBN; c0 += 16) {
+        float v[16];
+        tc::tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, v);
+        if (row < td.NP)
+#pragma unroll
+          for (int g = 0; g < 4; ++g)
+            reinterpret_cast<float4*>(zr + c0)[g] = make_float4(v[4 * g], v[4 * g + 1], v[4 * g + 2], v[4 * g + 3]);
+      }
+    }
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (ctl[0]) {
+    if (threadIdx.x == 0) {
+      atomicCAS(a.err, 0, CHECK_TIMEOUT);
+      // let copies still in flight land before the CTA's shared memory goes
+      for (int kb = ctl[2]; kb < ctl[1]; ++kb)
+        tc::mbar_wait(full0 + 8 * (kb % kTcStages), (kb / kTcStages) & 1);
+    }
+    __syncthreads();
+  }
+  if (warp == 1) {
+    tc::fence_after();
+    tc::tmem_dealloc(tmem, kLargeBN);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// f and its window for one Z row, by the calling warp (lanes over genes; the
+// fused kernel's FP32 forms and scale)
+// ---------------------------------------------------------------------------
+__device__ void eval_row_lanes(const FnConst& fc, const float* __restrict__ z,
+                               const float* __restrict__ x, const float* __restrict__ o,
+                               float* fout, float* tout) {
+  const int lane = threadIdx.x & 31, D = fc.D;
+  const bool griewank_prod = !(fc.flags & FLAG_REF_GRIEWANK_NO_PRODUCT);
+  float a = 0.f, b = 0.f, c = 1.f, sa = 0.f, ss = 0.f;
+  int neg = 0;
+  switch (fc.fid) {
+    case F_SPHERE:
+      for (int j = lane; j < D; j += 32) a = fmaf(z[j], z[j], a);
+      sa = a;
+      break;
+    case F_RASTRIGIN:
+      for (int j = lane; j < D; j += 32) {
+        const float v = z[j], sp = sinpif(v);
+        a += fmaf(20.f * sp, sp, v * v);
+      }
+      sa = a;
+      break;
+    case F_ACKLEY:
+      for (int j = lane; j < D; j += 32) {
+        const float v = z[j], sp = sinpif(v);
+        a = fmaf(v, v, a);
+        b = fmaf(sp, sp, b);
+      }
+      break;
+    case F_GRIEWANK:
+      for (int j = lane; j < D; j += 32) {
+        const float v = z[j];
+        a = fmaf(v, v, a);
+        if (griewank_prod) {
+          const float th = __fdiv_rn(v, sqrtf((float)(j + 1)));
+          const float ct = cosf(th);
+          c *= ct;
+          if (ct > 0.f) {
+            const float sh = sinf(0.5f * th);
+            b += log1pf(-2.f * sh * sh);
+          } else {
+            neg = 1;
+          }
+        }
+      }
+      break;
+    case F_ROSENBROCK:
+      for (int j = lane; j + 1 < D; j += 32) {
+        const float v = z[j], n = z[j + 1];
+        const float t1 = fmaf(v, v, -n), t2 = v - 1.f;
+        const float t = fmaf(100.f * t1, t1, t2 * t2);
+        a += t;
+        sa += t + 200.f * fabsf(t1) * fmaf(v, v, fabsf(n)) + 2.f * fabsf(t2) * (fabsf(v) + 1.f);
+      }
+      break;
+    case F_SCHWEFEL:
+      for (int j = lane; j < D; j += 32) {
+        const float v = z[j], t = v * sinf(sqrtf(fabsf(v)));
+        a += t;
+        sa += fabsf(t);
+      }
+      break;
+    case F_WEIERSTRASS:
+      for (int j = lane; j < D; j += 32) {
+        a += weier_gene_f32(z[j]);
+        const float d = x[j] - o[j];
+        ss = fmaf(d, d, ss);
+      }
+      break;
+    default:
+      break;
+  }
+  a = warp_sum(a);
+  b = warp_sum(b);
+  c = warp_prod(c);
+  sa = warp_sum(sa);
+  ss = warp_sum(ss);
+  neg = __any_sync(0xFFFFFFFFu, neg);
+  float f, scale;
+  switch (fc.fid) {
+    case F_ACKLEY: {
+      const float e = 2.71828183f;
+      const float eref = (fc.flags & FLAG_REF_ACKLEY_E) ? 2.718282f - e : 0.f;
+      const float t1 = -20.f * expm1f(-0.2f * sqrtf(a / (float)D));
+      const float t2 = -e * expm1f(-2.f * b / (float)D);
+      f = t1 + t2 + eref;
+      scale = t1 + t2 + fabsf(eref);
+      break;
+    }
+    case F_GRIEWANK: {
+      const float om = !griewank_prod ? 0.f : (neg ? 1.f - c : -expm1f(b));
+      f = om + a / 4000.f;
+      scale = a / 4000.f + fabsf(om) + ((griewank_prod && neg) ? fabsf(c) + 1.f : 0.f);
+      break;
+    }
+    case F_SCHWEFEL:
+      f = 418.9829f * (float)D - a;
+      scale = 418.9829f * (float)D + sa;
+      break;
+    case F_WEIERSTRASS:
+      f = a + fc.woff;
+      scale = 2.f * (float)D + fabsf(fc.woff);
+      break;
+    default:
+      f = a;
+      scale = sa;
+      break;
+  }
+  float t = fc.rel * scale;
+  if (fc.fid == F_WEIERSTRASS)
+    t = (fc.flags & FLAG_RIGOROUS_WINDOW) ? t + weier_rotation_bound(D, fc.qnorm, sqrtf(ss))
+                                          : 5.f * t;
+  *fout = f;
+  *tout = t;
+}
+
+// which = 0: members (fit32/tol32); 1: trials (ftr/ttr); rows < limit
+__global__ void __launch_bounds__(256) eval_kernel(const LargeArgs a, int which, int limit) {
+  const int task = blockIdx.y;
+  const TaskDev td = a.tasks[task];
+  if (!large_ok(td)) return;
+  const int row = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (row >= td.NP || row >= limit) return;  // warp-uniform
+  const FnConst fc = fn_const(td, a.recheck_rel);
+  const float* z = a.Z + (a.srow[task] + row) * (int64_t)a.Nq;
+  const float* x = (which ? a.U : a.pop) + td.pop_off + (size_t)row * td.DP;
+  float f, t;
+  eval_row_lanes(fc, z, x, a.shift + td.o_off, &f, &t);
+  if ((threadIdx.x & 31) == 0) {
+    (which ? a.ftr : a.fit32)[td.fit_off + row] = f;
+    (which ? a.ttr : a.tol32)[td.fit_off + row] = t;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// selection, ranking and elite exchange: one CTA (256 threads) per task,
+// the fused kernel's select_and_replace over global-memory rows
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) select_kernel(const LargeArgs a, int mode) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int task = blockIdx.x;
+  const TaskDev td = a.tasks[task];
+  if (!large_ok(td)) return;
+  if (large_select_smem(td.DP) > a.select_smem) {
+    if (threadIdx.x == 0) atomicCAS(a.err, 0, CHECK_SMEM_TOO_SMALL);
+    return;
+  }
+  const int NP = td.NP, DP = td.DP;
+  Smem s{};
+  s.z64 = reinterpret_cast<double*>(smraw);
+  int* ip = reinterpret_cast<int*>(s.z64 + (size_t)kWarps * 2 * DP);
+  s.flag = ip;
+  s.list = ip + kMaxPop;
+  s.idx = ip + 2 * kMaxPop;  // targets (transfer)
+  s.misc = ip + 4 * kMaxPop;
+  s.X = a.pop + td.pop_off;
+  s.U = a.U + td.pop_off;
+  s.fit = a.fit32 + td.fit_off;
+  s.tol = a.tol32 + td.fit_off;
+  s.ftr = a.ftr + td.fit_off;
+  s.ttr = a.ttr + td.fit_off;
+  s.fit64 = a.fit64 + td.fit_off;
+  s.o = const_cast<float*>(a.shift + td.o_off);
+  s.QT = const_cast<float*>(a.qt + td.q_off);
+  s.zc = s.zcb = nullptr;
+  EpochArgs ea{};
+  ea.flags = a.flags;
+  const FnConst fc = fn_const(td, a.recheck_rel);
+  unsigned long long* st_re = a.stats ? a.stats + 0 : nullptr;
+  unsigned long long* st_fl = a.stats ? a.stats + 1 : nullptr;
+  int* byrank = a.rank + td.fit_off;
+  if (mode == SEL_GENERATION) {
+    select_and_replace(s, ea, fc, NP, nullptr, false, DP, st_re, st_fl);
+    if (threadIdx.x == 0) {
+      a.gen[task] += 1u;
+      if (a.stats) atomicAdd(a.stats + 3, (unsigned long long)NP);
+    }
+  } else if (mode == SEL_RANK || mode == SEL_EXPORT) {
+    rank_members(s, NP, s.idx);
+    if (mode == SEL_RANK) {
+      for (int i = threadIdx.x; i < NP; i += kThreads) byrank[i] = s.idx[i];
+    } else {
+      const int k = transfer_k(a.transfer_rate, NP);
+      float* el = a.elites_out + td.elite_off;
+      for (int it = threadIdx.x; it < k * DP; it += kThreads) {
+        const int c = it / DP, j = it - c * DP;
+        el[(size_t)c * DP + j] = s.X[(size_t)s.idx[c] * DP + j];
+      }
+    }
+  } else {  // SEL_IMPORT: candidates in trial rows [0, k) against ranks NP - k + c
+    int k = 0;
+    if (transfer_partner(a, task, a.gen[task], k) < 0) return;
+    for (int c = threadIdx.x; c < k; c += kThreads) s.idx[c] = byrank[NP - k + c];
+    __syncthreads();
+    // each thread returns the replacements among its own rows
+    const int acc = select_and_replace(s, ea, fc, k, s.idx, true, DP, st_re, st_fl);
+    if (acc && a.stats) atomicAdd(a.stats + 2, (unsigned long long)acc);
+    if (threadIdx.x == 0 && a.stats) atomicAdd(a.stats + 3, (unsigned long long)k);
+  }
+}
+
+// best member per task and its FP64-class fitness; zbuf in dynamic smem
+__global__ void __launch_bounds__(32) best_kernel(const BestArgs a) {
+  extern __shared__ double zb[];
+  const int task = blockIdx.x;
+  if (task >= a.n_tasks) return;
+  const TaskDev td = a.tasks[task];
+  if (!large_ok(td)) return;
+  const int lane = threadIdx.x;
+  float bf = __int_as_float(0x7F800000);
+  int bi = 0x7FFFFFFF;
+  for (int i = lane; i < td.NP; i += 32) {
+    const float f = a.fit32[td.fit_off + i];
+    if (f < bf || (f == bf && i < bi)) {
+      bf = f;
+      bi = i;
+    }
+  }
+#pragma unroll
+  for (int m = 16; m > 0; m >>= 1) {
+    const float of = __shfl_xor_sync(0xFFFFFFFFu, bf, m);
+    const int oi = __shfl_xor_sync(0xFFFFFFFFu, bi, m);
+    if (of < bf || (of == bf && oi < bi)) {
+      bf = of;
+      bi = oi;
+    }
+  }
+  if (bi < 0 || bi >= td.NP) bi = 0;
+  double f64 = a.fit64[td.fit_off + bi];
+  if (isnan(f64))
+    f64 = eval_row_f64(fn_const(td, 0.f), a.pop + td.pop_off + (size_t)bi * td.DP,
+                       a.shift + td.o_off, a.qt + td.q_off, td.DP, zb);
+  if (lane == 0) {
+    a.best_idx[task] = bi;
+    a.best_f32[task] = bf;
+    a.best_f64[task] = f64;
+  }
+}
+
+}  // namespace large
+}  // namespace emt
+
+// ---- host launchers ----
+int emt_large_init(const emt::LargeArgs& a, void* stream) {
+  emt::large::init_kernel<<<dim3(16, a.n_tasks), 256, 0, (cudaStream_t)stream>>>(a);
+  return (int)cudaGetLastError();
+}
+
+int emt_large_build(const emt::LargeArgs& a, int mode, void* stream) {
+  const int gx = (emt::kMaxPop + emt::large::kBuildRows - 1) / emt::large::kBuildRows;
+  emt::large::build_kernel<<<dim3(gx, a.n_tasks), 256, 0, (cudaStream_t)stream>>>(a, mode);
+  return (int)cudaGetLastError();
+}
+
+int emt_large_gemm(const emt::LargeArgs& a, const void* smap, const void* qmap, void* stream) {
+  const int gy = emt::kMaxPop / emt::kLargeBM;
+  if (a.tc) {
+    static_assert(emt::large::kGemmTcSmem <= 227 * 1024, "tile pipeline");
+    cudaError_t e = cudaFuncSetAttribute(emt::large::gemm_tc_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)emt::large::kGemmTcSmem);
+    if (e != cudaSuccess) return (int)e;
+    emt::large::gemm_tc_kernel<<<dim3(a.Nq / emt::kLargeBN, gy, a.n_tasks), 192,
+                                 emt::large::kGemmTcSmem, (cudaStream_t)stream>>>(
+        a, *reinterpret_cast<const CUtensorMap*>(smap), *reinterpret_cast<const CUtensorMap*>(qmap));
+  } else {
+    emt::large::gemm_f32_kernel<<<dim3((a.Nq + 127) / 128, gy, a.n_tasks), 256, 0,
+                                  (cudaStream_t)stream>>>(a);
+  }
+  return (int)cudaGetLastError();
+}
+
+int emt_large_eval(const emt::LargeArgs& a, int which, int rows, void* stream) {
+  const int gx = (emt::kMaxPop + 7) / 8;
+  emt::large::eval_kernel<<<dim3(gx, a.n_tasks), 256, 0, (cudaStream_t)stream>>>(a, which, rows);
+  return (int)cudaGetLastError();
+}
+
+int emt_large_select(const emt::LargeArgs& a, int mode, void* stream) {
+  cudaError_t e = cudaFuncSetAttribute(emt::large::select_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)a.select_smem);
+  if (e != cudaSuccess) return (int)e;
+  emt::large::select_kernel<<<a.n_tasks, emt::kThreads, a.select_smem, (cudaStream_t)stream>>>(a, mode);
+  return (int)cudaGetLastError();
+}
+
+int emt_large_best(const emt::BestArgs& a, int maxD, void* stream) {
+  if (a.n_tasks <= 0) return 0;
+  emt::large::best_kernel<<<a.n_tasks, 32, sizeof(double) * (size_t)(maxD + 4), (cudaStream_t)stream>>>(a);
+  return (int)cudaGetLastError();
+}

@@ -88,7 +88,7 @@ def test_invalid_arguments(sgemtf):
         eng.run(1)
     assert e.value.status == sgemtf.ERR_STATE
     for bad in [dict(function=9, dim=4, pop=8), dict(function=0, dim=0, pop=8),
-                dict(function=0, dim=129, pop=8), dict(function=0, dim=4, pop=3),
+                dict(function=0, dim=1025, pop=8), dict(function=0, dim=4, pop=3),
                 dict(function=0, dim=4, pop=257)]:
         with pytest.raises(sgemtf.EngineError) as e:
             eng.add_tasks([sgemtf.TaskDesc(**bad)])

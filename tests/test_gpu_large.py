@@ -1,0 +1,115 @@
+"""Large islands (D > 128, up to 1024): the HBM-resident pipeline -- trial
+kernel, rotation GEMM (tcgen05 TF32x3 or FP32 CUDA cores), evaluation,
+selection with the near-tie re-check -- against the oracle replaying the
+same Philox stream with every selection decided in FP64.  Same operators
+as the fused kernel (SG-EMTF.cu:548-831, SG-EMTF_DE.cu:474-706)."""
+import numpy as np
+import pytest
+
+from gpu_util import make_engine, oracle_params, tolerance
+from test_gpu_replay import replay
+
+pytestmark = pytest.mark.gpu
+
+# a mixed handle: any D > 128 sends every island (the D = 10 one too) through
+# the large-island pipeline; D = 257 and 300 leave ragged GEMM tiles
+SPECS = [(0, 200, 16, 1), (1, 130, 32, 1), (2, 257, 8, 1), (3, 300, 20, 1), (4, 160, 16, 1),
+         (5, 140, 12, 1), (6, 129, 16, 1), (0, 10, 16, 1)]
+
+
+def engine(sgemtf, orc, precision, **kw):
+    try:
+        return make_engine(sgemtf, orc, SPECS, seed=17, precision=precision, **kw)
+    except sgemtf.EngineError as e:
+        pytest.skip(str(e))
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("alg", [0, 2])
+def test_large_replay_bit_exact(sgemtf, orc, precision, alg):
+    kw = dict(algorithm=alg)
+    if alg == 2:
+        kw.update(eta_c=15.0, p_c=0.9, eta_m=15.0, p_m=-1.0)
+    eng, tasks = engine(sgemtf, orc, precision, **kw)
+    eng.reset()
+    X0 = [eng.population(i)[0] for i in range(len(tasks))]
+    gens = 6
+    eng.run(gens)
+    want = replay(orc, oracle_params(orc, eng), tasks, X0, gens)
+    for i in range(len(tasks)):
+        got = eng.population(i)[0]
+        assert np.array_equal(got, want[i]), (precision, alg, i, np.argwhere(got != want[i])[:5])
+    st = eng.stats()
+    assert st["evaluations"] == sum(t.NP for t in tasks) * (gens + 1)
+    eng.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_large_fitness_within_window(sgemtf, orc, precision):
+    eng, tasks = engine(sgemtf, orc, precision)
+    eng.reset()
+    for i, t in enumerate(tasks):
+        X, f = eng.population(i)
+        for r in range(t.NP):
+            f64, scale, _ = t.eval64(X[r])
+            assert abs(float(f[r]) - f64) <= tolerance(orc, t, X[r], scale), (i, r)
+    eng.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_large_transfer_epochs(sgemtf, orc, precision):
+    specs = [(0, 150, 16, 1), (1, 150, 16, 1), (6, 140, 12, 1), (2, 200, 20, 1)]
+    interval = 3
+    try:
+        eng, tasks = make_engine(sgemtf, orc, specs, seed=5, precision=precision, algorithm=2,
+                                 transfer_interval=interval, transfer_rate=0.25, transfer_mix=0.5)
+    except sgemtf.EngineError as e:
+        pytest.skip(str(e))
+    p = oracle_params(orc, eng)
+    eng.reset()
+    n = len(tasks)
+    state = [eng.population(i) for i in range(n)]
+    gen, replaced = 0, 0
+    for epoch in range(3):
+        eng.run(interval)
+        X = [s[0].copy() for s in state]
+        f32 = [s[1].copy() for s in state]
+        f64 = [np.full(t.NP, np.nan) for t in tasks]
+        if gen > 0:
+            elites = [state[i][0][np.argsort(orc.rank(state[i][1]))] for i in range(n)]
+            for i, t in enumerate(tasks):
+                q = orc.transfer_partner(p, i, n, gen)
+                k = min(max(1, int(0.25 * t.NP + 0.5)), max(1, int(0.25 * tasks[q].NP + 0.5)))
+                replaced += orc.transfer_in(p, t, tasks[q], elites[q][:k], X[i], f32[i], f64[i], gen, 0)
+        for i, t in enumerate(tasks):
+            for g in range(gen + 1, gen + interval + 1):
+                orc.generation(p, t, X[i], f32[i], f64[i], g, 0)
+        gen += interval
+        state = [eng.population(i) for i in range(n)]
+        for i in range(n):
+            assert np.array_equal(state[i][0], X[i]), (epoch, i)
+    assert eng.stats()["transfers_accepted"] == replaced
+    eng.close()
+
+
+def test_large_best_snapshot_and_limits(sgemtf, orc):
+    eng, tasks = engine(sgemtf, orc, 0, transfer_interval=2)
+    eng.reset()
+    eng.run(4)
+    best = eng.best_all()
+    for i in range(len(tasks)):
+        assert best[i] == eng.population(i)[1].min()
+    f64, x = eng.best(2)
+    assert np.isfinite(f64) and x.shape == (tasks[2].D,)
+    snap = eng.snapshot()
+    eng.run(3)
+    after = [eng.population(i)[0] for i in range(len(tasks))]
+    eng.restore(snap)
+    eng.run(3)
+    for i in range(len(tasks)):
+        assert np.array_equal(eng.population(i)[0], after[i])
+    with pytest.raises(sgemtf.EngineError):
+        eng.evaluate(0, np.zeros((1, tasks[0].D), np.float32))
+    with pytest.raises(sgemtf.EngineError):
+        eng.run_noalloc(1)
+    eng.close()
