@@ -255,6 +255,14 @@ EMT_API int emt_run_noalloc(emt_handle_t* h, int32_t generations, void* stream);
  * (SG-EMTF.cu:1660-1676). */
 EMT_API int emt_tune(emt_handle_t* h, int32_t generations, void* stream, int32_t* chosen);
 
+/* Measurement hook for roofline reports: times `reps` launches of the
+ * rotation GEMM (Z = S Q^T for every island) of a large-island handle on its
+ * current operands, with CUDA events on `stream`; *ms receives the mean
+ * duration of one launch.  Blocking.  EMT_ERR_UNSUPPORTED for fused-kernel
+ * handles, whose rotation runs inside the epoch kernel.  No counterpart in
+ * the reference. */
+EMT_API int emt_time_rotation(emt_handle_t* h, int32_t reps, void* stream, float* ms);
+
 /* Waits for the handle's work and reports a kernel's error word. */
 EMT_API int emt_sync(emt_handle_t* h);
 

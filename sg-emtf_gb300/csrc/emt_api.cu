@@ -109,12 +109,12 @@ struct emt_handle {
   CUtensorMap tmap;
   // large islands (any D > 128): HBM-resident pipeline (emt_large.cuh)
   bool large = false, large_tc = false;
-  int lKp = 0, lNq = 0;
+  int lKp = 0, lNq = 0, ldp = 4, lgrid = 0;
   int64_t lrows = 0;
   size_t lsel_smem = 0;
   DevBuf<float> d_U, d_ftr, d_ttr, d_S, d_Z, d_qbig;
   DevBuf<int64_t> d_srow, d_qrow;
-  DevBuf<int32_t> d_rank;
+  DevBuf<int32_t> d_rank, d_flag, d_rlist, d_rcount;
   CUtensorMap smap, qmap;
 
   int fail(int code, const std::string& msg) {
@@ -312,11 +312,17 @@ int large_upload(emt_handle* h, int64_t pop, int32_t fit) {
     qrow[t] = (int64_t)t * h->lNq;
   }
   h->lrows = rows;
+  h->ldp = dpmax;
   h->lsel_smem = emt::large_select_smem(dpmax);
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+  h->lgrid = std::max(1, 2 * sms);  // re-check CTAs: two per SM, persistent
   const int planes = h->large_tc ? 2 : 1;
   cudaError_t e;
   if ((e = h->d_U.ensure((size_t)pop)) || (e = h->d_ftr.ensure((size_t)fit)) ||
       (e = h->d_ttr.ensure((size_t)fit)) || (e = h->d_rank.ensure((size_t)fit)) ||
+      (e = h->d_flag.ensure((size_t)fit)) || (e = h->d_rlist.ensure((size_t)2 * fit)) ||
+      (e = h->d_rcount.ensure(1)) ||
       (e = h->d_srow.ensure(n)) || (e = h->d_qrow.ensure(n)) ||
       (e = h->d_S.ensure((size_t)planes * rows * h->lKp)) ||
       (e = h->d_Z.ensure((size_t)rows * h->lNq)))
@@ -653,6 +659,9 @@ emt::LargeArgs large_args(emt_handle* h) {
   a.Z = h->d_Z.p;
   a.gen = h->d_gen.p;
   a.rank = h->d_rank.p;
+  a.flag = h->d_flag.p;
+  a.rlist = h->d_rlist.p;
+  a.rcount = h->d_rcount.p;
   a.algorithm = h->cfg.algorithm;
   a.F = h->cfg.F;
   a.CR = h->cfg.CR;
@@ -685,7 +694,7 @@ int large_generation(emt_handle* h, const emt::LargeArgs& a, cudaStream_t stream
   int e = emt_large_build(a, emt::large::BUILD_TRIALS, stream);
   if (!e) e = emt_large_gemm(a, &h->smap, &h->qmap, stream);
   if (!e) e = emt_large_eval(a, 1, emt::kMaxPop, stream);
-  if (!e) e = emt_large_select(a, emt::large::SEL_GENERATION, stream);
+  if (!e) e = emt_large_selection(a, emt::large::SEL_GENERATION, h->ldp, h->lgrid, stream);
   return e;
 }
 
@@ -701,7 +710,7 @@ int large_epoch(emt_handle* h, int gens, int imp, int exp, int parity, cudaStrea
     if (!e) e = emt_large_build(a, emt::large::BUILD_CANDIDATES, stream);
     if (!e) e = emt_large_gemm(a, &h->smap, &h->qmap, stream);
     if (!e) e = emt_large_eval(a, 1, emt::kMaxPop, stream);
-    if (!e) e = emt_large_select(a, emt::large::SEL_IMPORT, stream);
+    if (!e) e = emt_large_selection(a, emt::large::SEL_IMPORT, h->ldp, h->lgrid, stream);
   }
   for (int g = 0; g < gens && !e; ++g) e = large_generation(h, a, stream);
   if (!e && exp) e = emt_large_select(a, emt::large::SEL_EXPORT, stream);
@@ -1036,6 +1045,29 @@ int emt_run(emt_handle_t* h, int32_t generations, void* stream) {
   if (rc) return rc;
   apply_plan(h, plan);
   return EMT_OK;
+}
+
+int emt_time_rotation(emt_handle_t* h, int32_t reps, void* stream, float* ms) {
+  if (!h || !ms || reps < 1) return EMT_ERR_INVALID_ARG;
+  if (!h->initialized) {
+    int rc = emt_reset(h, stream);
+    if (rc) return rc;
+  }
+  if (!h->large) return h->fail(EMT_ERR_UNSUPPORTED, "the rotation of fused islands runs inside the epoch kernel");
+  h->stream = (cudaStream_t)stream;
+  const emt::LargeArgs a = large_args(h);
+  cudaEventRecord(h->ev0, h->stream);
+  int e = 0;
+  for (int r = 0; r < reps && !e; ++r) e = emt_large_gemm(a, &h->smap, &h->qmap, h->stream);
+  if (e) return h->cuda_fail((cudaError_t)e, "rotation launch");
+  cudaEventRecord(h->ev1, h->stream);
+  cudaError_t ce = cudaEventSynchronize(h->ev1);
+  float t = 0.f;
+  if (ce == cudaSuccess) ce = cudaEventElapsedTime(&t, h->ev0, h->ev1);
+  if (ce != cudaSuccess) return h->cuda_fail(ce, "rotation timing");
+  h->timing_pending = false;
+  *ms = t / (float)reps;
+  return emt_sync(h);
 }
 
 int emt_tune(emt_handle_t* h, int32_t generations, void* stream, int32_t* chosen) {

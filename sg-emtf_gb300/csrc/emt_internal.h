@@ -106,6 +106,9 @@ struct LargeArgs {
   float* Z;
   uint32_t* gen;
   int32_t* rank;         // per member: rank order of the task (byrank)
+  int32_t* flag;         // per trial row: 0 keep, 1 replace (FP32), 2 near tie, 3 replace (re-checked)
+  int32_t* rlist;        // near ties of the step: (task, row) pairs
+  int32_t* rcount;       // their number
   int32_t algorithm;
   float F, CR, eta_c, p_c, eta_m, p_m;
   uint64_t seed;
@@ -276,4 +279,7 @@ int emt_large_gemm(const emt::LargeArgs& a, const void* smap, const void* qmap, 
 int emt_large_eval(const emt::LargeArgs& a, int which, int rows, void* stream);
 int emt_large_select(const emt::LargeArgs& a, int mode, void* stream);
 int emt_large_best(const emt::BestArgs& a, int maxD, void* stream);
+// selection of a generation (mode SEL_GENERATION) or a transfer import
+// (SEL_IMPORT): classify, re-check near ties on the whole GPU, apply
+int emt_large_selection(const emt::LargeArgs& a, int mode, int maxDP, int grid, void* stream);
 int emt_launch_best(const emt::BestArgs& a, void* stream);

@@ -625,6 +625,207 @@ __global__ void __launch_bounds__(256) select_kernel(const LargeArgs a, int mode
   }
 }
 
+// ---------------------------------------------------------------------------
+// selection split for parallelism.  The per-task CTA above would re-check a
+// task's near ties with its 8 warps while most SMs idle; at D = 1000 each
+// re-check rotates 10^6 compensated products.  Instead:
+//   classify (CTA per task): FP32 decisions; near ties to a global list;
+//   recheck  (persistent grid): one CTA per near tie, the compensated
+//            rotation spread over its 256 threads (the same per-output
+//            arithmetic as precise_rotation, so the same bits), then warp 0
+//            evaluates the FP64-class terms (tiers 2/3, exact Weierstrass);
+//   apply    (CTA per task): accepted rows into the island, counters.
+// ---------------------------------------------------------------------------
+
+// rows of the step and the member each one competes with
+__device__ __forceinline__ int sel_rows(const LargeArgs& a, int task, int mode, int& k) {
+  const TaskDev td = a.tasks[task];
+  if (mode == SEL_IMPORT) {
+    k = 0;
+    if (transfer_partner(a, task, a.gen[task], k) < 0) return 0;
+    return k;
+  }
+  return td.NP;
+}
+__device__ __forceinline__ int sel_target(const LargeArgs& a, const TaskDev& td, int mode, int k, int c) {
+  return mode == SEL_IMPORT ? a.rank[td.fit_off + td.NP - k + c] : c;
+}
+
+__global__ void __launch_bounds__(256) classify_kernel(const LargeArgs a, int mode) {
+  const int task = blockIdx.x;
+  const TaskDev td = a.tasks[task];
+  if (!large_ok(td)) return;
+  int k = 0;
+  const int nrows = sel_rows(a, task, mode, k);
+  const bool strict = mode == SEL_IMPORT;
+  const bool recheck = !(a.flags & FLAG_NO_RECHECK);
+  for (int c = threadIdx.x; c < nrows; c += blockDim.x) {
+    const int m = sel_target(a, td, mode, k, c);
+    const float ft = a.ftr[td.fit_off + c], fp = a.fit32[td.fit_off + m];
+    const bool d32 = strict ? (ft < fp) : (ft <= fp);
+    int f = d32 ? 1 : 0;
+    if (recheck && fabsf(ft - fp) <= a.ttr[td.fit_off + c] + a.tol32[td.fit_off + m]) {
+      f = 2;
+      const int r = atomicAdd(a.rcount, 1);
+      a.rlist[2 * r] = task;
+      a.rlist[2 * r + 1] = c;
+    }
+    a.flag[td.fit_off + c] = f;
+  }
+}
+
+// z = Q (x - o) of one row by the whole CTA: pr holds the exact split of
+// x - o; output n is the compensated dot product of dot2_pair, in the same
+// order, so the values equal precise_rotation's.
+__device__ void cta_precise_rotation(const float* __restrict__ x, const float* __restrict__ o,
+                                     const float* __restrict__ qt, int DP, int D, float2* pr,
+                                     double* zbuf) {
+  for (int k = threadIdx.x; k < D; k += blockDim.x) {
+    float sh, sl;
+    two_sum(x[k], -o[k], sh, sl);
+    pr[k] = make_float2(sh, sl);
+  }
+  __syncthreads();
+  for (int n = threadIdx.x; n < D; n += blockDim.x) {
+    float S = 0.f, C = 0.f;
+    for (int k = 0; k < D; ++k) {
+      const float2 hl = pr[k];
+      const float q = qt[(size_t)k * DP + n];
+      const float p = __fmul_rn(q, hl.x);
+      const float e = __fmaf_rn(q, hl.x, -p);
+      float t, te;
+      two_sum(S, p, t, te);
+      S = t;
+      C = __fmaf_rn(q, hl.y, __fadd_rn(C, __fadd_rn(te, e)));
+    }
+    zbuf[n] = (double)S + (double)C;
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(256) recheck_kernel(const LargeArgs a, int mode) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ int sh_same, sh_dec;
+  __shared__ double sh_ft, sh_fp;
+  const int count = *a.rcount;
+  const int warp = threadIdx.x >> 5;
+  for (int r = blockIdx.x; r < count; r += gridDim.x) {
+    const int task = a.rlist[2 * r], c = a.rlist[2 * r + 1];
+    const TaskDev td = a.tasks[task];
+    const int D = td.D, DP = td.DP;
+    double* zt = reinterpret_cast<double*>(smraw);
+    double* zp = zt + DP;
+    float2* pr = reinterpret_cast<float2*>(zp + DP);
+    int k = 0;
+    sel_rows(a, task, mode, k);
+    const int m = sel_target(a, td, mode, k, c);
+    const bool strict = mode == SEL_IMPORT;
+    const float* u = a.U + td.pop_off + (size_t)c * DP;
+    const float* x = a.pop + td.pop_off + (size_t)m * DP;
+    const float* o = a.shift + td.o_off;
+    const float* qt = a.qt + td.q_off;
+    const FnConst fc = fn_const(td, a.recheck_rel);
+    if (threadIdx.x == 0) sh_same = 1;
+    __syncthreads();
+    for (int j = threadIdx.x; j < D; j += blockDim.x)
+      if (__float_as_uint(u[j]) != __float_as_uint(x[j])) sh_same = 0;
+    __syncthreads();
+    double fp = a.fit64[td.fit_off + m];
+    if (sh_same) {
+      if (threadIdx.x == 0) {
+        sh_dec = strict ? 0 : 1;
+        sh_ft = fp;
+        sh_fp = fp;
+      }
+    } else {
+      cta_precise_rotation(u, o, qt, DP, D, pr, zt);
+      const bool need_p = isnan(fp);
+      if (need_p) cta_precise_rotation(x, o, qt, DP, D, pr, zp);
+      if (warp == 0) {
+        const bool tier2 = fc.fid != F_WEIERSTRASS && fc.fid != F_SPHERE && fc.fid != F_ROSENBROCK;
+        bool decided = false;
+        int dec = 0;
+        double ft = __longlong_as_double(0x7FF8000000000000ll), fpv = fp;
+        if (tier2) {
+          double et, ep = 0.0;
+          const double t2 = eval_tier2(fc, zt, &et);
+          double p2 = fp;
+          if (need_p) p2 = eval_tier2(fc, zp, &ep);
+          if (fabs(t2 - p2) > et + ep) {
+            dec = strict ? (t2 < p2) : (t2 <= p2);
+            decided = true;
+          }
+        }
+        if (!decided) {
+          ft = fc.fid == F_WEIERSTRASS ? eval_weier_precise(fc, zt) : eval_tier3(fc, zt);
+          if (need_p) fpv = fc.fid == F_WEIERSTRASS ? eval_weier_precise(fc, zp) : eval_tier3(fc, zp);
+          dec = strict ? (ft < fpv) : (ft <= fpv);
+        }
+        if ((threadIdx.x & 31) == 0) {
+          sh_dec = dec;
+          sh_ft = ft;
+          sh_fp = fpv;
+        }
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const bool d64 = sh_dec != 0;
+      const float f32t = a.ftr[td.fit_off + c], f32p = a.fit32[td.fit_off + m];
+      const bool d32 = strict ? (f32t < f32p) : (f32t <= f32p);
+      a.flag[td.fit_off + c] = d64 ? 3 : 0;
+      // FP64 value of whichever vector member m holds afterwards
+      a.fit64[td.fit_off + m] = d64 ? sh_ft : sh_fp;
+      if (a.stats) {
+        atomicAdd(a.stats + 0, 1ull);
+        if (d64 != d32) atomicAdd(a.stats + 1, 1ull);
+        if (sh_same) atomicAdd(a.stats + 6, 1ull);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(256) apply_kernel(const LargeArgs a, int mode) {
+  const int task = blockIdx.x;
+  const TaskDev td = a.tasks[task];
+  if (!large_ok(td)) return;
+  int k = 0;
+  const int nrows = sel_rows(a, task, mode, k);
+  const int DP = td.DP, nq = DP >> 2;
+  __shared__ int acc;
+  if (threadIdx.x == 0) acc = 0;
+  __syncthreads();
+  for (int it = threadIdx.x; it < nrows * nq; it += blockDim.x) {
+    const int c = it / nq, q = it - c * nq;
+    if (a.flag[td.fit_off + c] & 1) {
+      const int m = sel_target(a, td, mode, k, c);
+      reinterpret_cast<float4*>(a.pop + td.pop_off + (size_t)m * DP)[q] =
+          reinterpret_cast<const float4*>(a.U + td.pop_off + (size_t)c * DP)[q];
+    }
+  }
+  for (int c = threadIdx.x; c < nrows; c += blockDim.x) {
+    const int f = a.flag[td.fit_off + c];
+    if (f & 1) {
+      const int m = sel_target(a, td, mode, k, c);
+      a.fit32[td.fit_off + m] = a.ftr[td.fit_off + c];
+      a.tol32[td.fit_off + m] = a.ttr[td.fit_off + c];
+      if (f == 1) a.fit64[td.fit_off + m] = __longlong_as_double(0x7FF8000000000000ll);
+      atomicAdd(&acc, 1);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (mode == SEL_GENERATION) {
+      a.gen[task] += 1u;
+      if (a.stats) atomicAdd(a.stats + 3, (unsigned long long)td.NP);
+    } else if (a.stats) {
+      if (acc) atomicAdd(a.stats + 2, (unsigned long long)acc);
+      atomicAdd(a.stats + 3, (unsigned long long)k);
+    }
+  }
+}
+
 // best member per task and its FP64-class fitness; zbuf in dynamic smem
 __global__ void __launch_bounds__(32) best_kernel(const BestArgs a) {
   extern __shared__ double zb[];
@@ -708,6 +909,16 @@ int emt_large_select(const emt::LargeArgs& a, int mode, void* stream) {
                                        (int)a.select_smem);
   if (e != cudaSuccess) return (int)e;
   emt::large::select_kernel<<<a.n_tasks, emt::kThreads, a.select_smem, (cudaStream_t)stream>>>(a, mode);
+  return (int)cudaGetLastError();
+}
+
+int emt_large_selection(const emt::LargeArgs& a, int mode, int maxDP, int grid, void* stream) {
+  cudaError_t e = cudaMemsetAsync(a.rcount, 0, sizeof(int32_t), (cudaStream_t)stream);
+  if (e != cudaSuccess) return (int)e;
+  emt::large::classify_kernel<<<a.n_tasks, 256, 0, (cudaStream_t)stream>>>(a, mode);
+  const size_t sm = sizeof(double) * 2 * (size_t)maxDP + sizeof(float2) * (size_t)maxDP;
+  emt::large::recheck_kernel<<<grid, 256, sm, (cudaStream_t)stream>>>(a, mode);
+  emt::large::apply_kernel<<<a.n_tasks, 256, 0, (cudaStream_t)stream>>>(a, mode);
   return (int)cudaGetLastError();
 }
 

@@ -39,7 +39,7 @@ NOALLOC_EXCHANGE_FLOATS = 1 << 19
 
 EXPORTED = [
     "emt_config_default", "emt_function_from_reference", "emt_function_box", "emt_create",
-    "emt_add_tasks", "emt_reset", "emt_run", "emt_run_noalloc", "emt_tune", "emt_sync", "emt_get_best", "emt_get_best_all",
+    "emt_add_tasks", "emt_reset", "emt_run", "emt_run_noalloc", "emt_tune", "emt_time_rotation", "emt_sync", "emt_get_best", "emt_get_best_all",
     "emt_get_population", "emt_set_population", "emt_get_task_params", "emt_evaluate",
     "emt_get_stats", "emt_snapshot_size", "emt_snapshot", "emt_restore", "emt_last_error",
     "emt_status_string", "emt_destroy",
@@ -159,6 +159,7 @@ def lib():
         L.emt_run.argtypes = [vp, i32, vp]
         L.emt_run_noalloc.argtypes = [vp, i32, vp]
         L.emt_tune.argtypes = [vp, i32, vp, ctypes.POINTER(ctypes.c_int32)]
+        L.emt_time_rotation.argtypes = [vp, i32, vp, ctypes.POINTER(ctypes.c_float)]
         L.emt_sync.argtypes = [vp]
         L.emt_get_best.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_double), f32p]
         L.emt_get_best_all.argtypes = [vp, f32p]
@@ -248,6 +249,13 @@ class Engine:
         fastest; returns schedule | 0x100 when graph replay won."""
         out = ctypes.c_int32(0)
         self._check(lib().emt_tune(self._h, int(generations), stream, ctypes.byref(out)), "emt_tune")
+        return out.value
+
+    def time_rotation(self, reps, stream=None):
+        """Mean duration (ms) of one rotation-GEMM launch (large islands)."""
+        out = ctypes.c_float(0.0)
+        self._check(lib().emt_time_rotation(self._h, int(reps), stream, ctypes.byref(out)),
+                    "emt_time_rotation")
         return out.value
 
     def run_noalloc(self, generations, stream=None, sync=True):
