@@ -109,12 +109,12 @@ struct emt_handle {
   CUtensorMap tmap;
   // large islands (any D > 128): HBM-resident pipeline (emt_large.cuh)
   bool large = false, large_tc = false;
-  int lKp = 0, lNq = 0, ldp = 4, lgrid = 0;
+  int lKp = 0, lNq = 0, ldp = 4, lgrid = 1;
   int64_t lrows = 0;
   size_t lsel_smem = 0;
   DevBuf<float> d_U, d_ftr, d_ttr, d_S, d_Z, d_qbig;
   DevBuf<int64_t> d_srow, d_qrow;
-  DevBuf<int32_t> d_rank, d_flag, d_rlist, d_rcount;
+  DevBuf<int32_t> d_rank, d_flag, d_ties, d_ntie, d_work, d_nwork;
   CUtensorMap smap, qmap;
 
   int fail(int code, const std::string& msg) {
@@ -313,16 +313,17 @@ int large_upload(emt_handle* h, int64_t pop, int32_t fit) {
   }
   h->lrows = rows;
   h->ldp = dpmax;
-  h->lsel_smem = emt::large_select_smem(dpmax);
-  int sms = 0;
+  int sms = 0, occ = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
-  h->lgrid = std::max(1, 2 * sms);  // re-check CTAs: two per SM, persistent
+  occ = emt_large_recheck_occupancy(dpmax);
+  h->lgrid = std::max(1, sms * std::max(1, occ));  // persistent re-check grid
+  h->lsel_smem = emt::large_select_smem(dpmax);
   const int planes = h->large_tc ? 2 : 1;
   cudaError_t e;
   if ((e = h->d_U.ensure((size_t)pop)) || (e = h->d_ftr.ensure((size_t)fit)) ||
       (e = h->d_ttr.ensure((size_t)fit)) || (e = h->d_rank.ensure((size_t)fit)) ||
-      (e = h->d_flag.ensure((size_t)fit)) || (e = h->d_rlist.ensure((size_t)2 * fit)) ||
-      (e = h->d_rcount.ensure(1)) ||
+      (e = h->d_flag.ensure((size_t)fit)) || (e = h->d_ties.ensure((size_t)fit)) ||
+      (e = h->d_ntie.ensure(n)) || (e = h->d_work.ensure((size_t)fit)) || (e = h->d_nwork.ensure(1)) ||
       (e = h->d_srow.ensure(n)) || (e = h->d_qrow.ensure(n)) ||
       (e = h->d_S.ensure((size_t)planes * rows * h->lKp)) ||
       (e = h->d_Z.ensure((size_t)rows * h->lNq)))
@@ -660,8 +661,10 @@ emt::LargeArgs large_args(emt_handle* h) {
   a.gen = h->d_gen.p;
   a.rank = h->d_rank.p;
   a.flag = h->d_flag.p;
-  a.rlist = h->d_rlist.p;
-  a.rcount = h->d_rcount.p;
+  a.ties = h->d_ties.p;
+  a.ntie = h->d_ntie.p;
+  a.work = h->d_work.p;
+  a.nwork = h->d_nwork.p;
   a.algorithm = h->cfg.algorithm;
   a.F = h->cfg.F;
   a.CR = h->cfg.CR;

@@ -107,8 +107,10 @@ struct LargeArgs {
   uint32_t* gen;
   int32_t* rank;         // per member: rank order of the task (byrank)
   int32_t* flag;         // per trial row: 0 keep, 1 replace (FP32), 2 near tie, 3 replace (re-checked)
-  int32_t* rlist;        // near ties of the step: (task, row) pairs
-  int32_t* rcount;       // their number
+  int32_t* ties;         // per task (fit offsets): its near-tie rows, in order found
+  int32_t* ntie;         // per task: their number
+  int32_t* work;         // re-check work items: task << 16 | first tie of the item
+  int32_t* nwork;        // their number
   int32_t algorithm;
   float F, CR, eta_c, p_c, eta_m, p_m;
   uint64_t seed;
@@ -279,7 +281,8 @@ int emt_large_gemm(const emt::LargeArgs& a, const void* smap, const void* qmap, 
 int emt_large_eval(const emt::LargeArgs& a, int which, int rows, void* stream);
 int emt_large_select(const emt::LargeArgs& a, int mode, void* stream);
 int emt_large_best(const emt::BestArgs& a, int maxD, void* stream);
+int emt_large_recheck_occupancy(int maxDP);
 // selection of a generation (mode SEL_GENERATION) or a transfer import
-// (SEL_IMPORT): classify, re-check near ties on the whole GPU, apply
+// (SEL_IMPORT): classify, re-check each task's near ties in batches, apply
 int emt_large_selection(const emt::LargeArgs& a, int mode, int maxDP, int grid, void* stream);
 int emt_launch_best(const emt::BestArgs& a, void* stream);

@@ -651,6 +651,9 @@ __device__ __forceinline__ int sel_target(const LargeArgs& a, const TaskDev& td,
   return mode == SEL_IMPORT ? a.rank[td.fit_off + td.NP - k + c] : c;
 }
 
+constexpr int kPairs = 2;           // near ties per re-check work item
+constexpr int kJobs = 2 * kPairs;   // rotations per item (trial and parent)
+
 __global__ void __launch_bounds__(256) classify_kernel(const LargeArgs a, int mode) {
   const int task = blockIdx.x;
   const TaskDev td = a.tasks[task];
@@ -659,6 +662,9 @@ __global__ void __launch_bounds__(256) classify_kernel(const LargeArgs a, int mo
   const int nrows = sel_rows(a, task, mode, k);
   const bool strict = mode == SEL_IMPORT;
   const bool recheck = !(a.flags & FLAG_NO_RECHECK);
+  __shared__ int nt;
+  if (threadIdx.x == 0) nt = 0;
+  __syncthreads();
   for (int c = threadIdx.x; c < nrows; c += blockDim.x) {
     const int m = sel_target(a, td, mode, k, c);
     const float ft = a.ftr[td.fit_off + c], fp = a.fit32[td.fit_off + m];
@@ -666,120 +672,165 @@ __global__ void __launch_bounds__(256) classify_kernel(const LargeArgs a, int mo
     int f = d32 ? 1 : 0;
     if (recheck && fabsf(ft - fp) <= a.ttr[td.fit_off + c] + a.tol32[td.fit_off + m]) {
       f = 2;
-      const int r = atomicAdd(a.rcount, 1);
-      a.rlist[2 * r] = task;
-      a.rlist[2 * r + 1] = c;
+      a.ties[td.fit_off + atomicAdd(&nt, 1)] = c;
     }
     a.flag[td.fit_off + c] = f;
   }
+  __syncthreads();
+  // work items of up to kPairs ties each, to the GPU-wide queue
+  if (threadIdx.x == 0) {
+    a.ntie[task] = nt;
+    const int items = (nt + kPairs - 1) / kPairs;
+    if (items) {
+      const int w0 = atomicAdd(a.nwork, items);
+      for (int i = 0; i < items; ++i) a.work[w0 + i] = (task << 16) | (i * kPairs);
+    }
+  }
 }
 
-// z = Q (x - o) of one row by the whole CTA: pr holds the exact split of
-// x - o; output n is the compensated dot product of dot2_pair, in the same
-// order, so the values equal precise_rotation's.
-__device__ void cta_precise_rotation(const float* __restrict__ x, const float* __restrict__ o,
-                                     const float* __restrict__ qt, int DP, int D, float2* pr,
-                                     double* zbuf) {
-  for (int k = threadIdx.x; k < D; k += blockDim.x) {
-    float sh, sl;
-    two_sum(x[k], -o[k], sh, sl);
-    pr[k] = make_float2(sh, sl);
-  }
-  __syncthreads();
-  for (int n = threadIdx.x; n < D; n += blockDim.x) {
-    float S = 0.f, C = 0.f;
-    for (int k = 0; k < D; ++k) {
-      const float2 hl = pr[k];
-      const float q = qt[(size_t)k * DP + n];
-      const float p = __fmul_rn(q, hl.x);
-      const float e = __fmaf_rn(q, hl.x, -p);
-      float t, te;
-      two_sum(S, p, t, te);
-      S = t;
-      C = __fmaf_rn(q, hl.y, __fadd_rn(C, __fadd_rn(te, e)));
-    }
-    zbuf[n] = (double)S + (double)C;
-  }
-  __syncthreads();
+// Re-check work item: up to kPairs near ties of one task.  A persistent grid
+// takes items from the queue (balance: ties of all tasks spread over all
+// SMs); within an item the compensated rotations of up to kJobs rows share
+// every load of Q (each output keeps dot2_pair's order, so the values equal
+// precise_rotation's); warp p then decides pair p (identical trial, tier 2,
+// tier 3 / exact Weierstrass, as select_and_replace does).
+
+__host__ __device__ inline size_t recheck_smem(int DP) {
+  return (size_t)kJobs * DP * (sizeof(double) + sizeof(float2));
 }
 
 __global__ void __launch_bounds__(256) recheck_kernel(const LargeArgs a, int mode) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  __shared__ int sh_same, sh_dec;
-  __shared__ double sh_ft, sh_fp;
-  const int count = *a.rcount;
-  const int warp = threadIdx.x >> 5;
-  for (int r = blockIdx.x; r < count; r += gridDim.x) {
-    const int task = a.rlist[2 * r], c = a.rlist[2 * r + 1];
+  __shared__ int njob;
+  __shared__ const float* jrow[kJobs];
+  __shared__ int pair_c[kPairs], pair_m[kPairs], pair_same[kPairs], pair_zt[kPairs], pair_zp[kPairs];
+  const int items = *a.nwork;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const bool strict = mode == SEL_IMPORT;
+  for (int w = blockIdx.x; w < items; w += gridDim.x) {
+    const int task = a.work[w] >> 16, b0 = a.work[w] & 0xFFFF;
     const TaskDev td = a.tasks[task];
-    const int D = td.D, DP = td.DP;
-    double* zt = reinterpret_cast<double*>(smraw);
-    double* zp = zt + DP;
-    float2* pr = reinterpret_cast<float2*>(zp + DP);
     int k = 0;
     sel_rows(a, task, mode, k);
-    const int m = sel_target(a, td, mode, k, c);
-    const bool strict = mode == SEL_IMPORT;
-    const float* u = a.U + td.pop_off + (size_t)c * DP;
-    const float* x = a.pop + td.pop_off + (size_t)m * DP;
+    const int D = td.D, DP = td.DP;
+    double* zb = reinterpret_cast<double*>(smraw);                    // kJobs x DP
+    float2* pr = reinterpret_cast<float2*>(zb + (size_t)kJobs * DP);  // kJobs x DP
     const float* o = a.shift + td.o_off;
     const float* qt = a.qt + td.q_off;
     const FnConst fc = fn_const(td, a.recheck_rel);
-    if (threadIdx.x == 0) sh_same = 1;
-    __syncthreads();
-    for (int j = threadIdx.x; j < D; j += blockDim.x)
-      if (__float_as_uint(u[j]) != __float_as_uint(x[j])) sh_same = 0;
-    __syncthreads();
-    double fp = a.fit64[td.fit_off + m];
-    if (sh_same) {
-      if (threadIdx.x == 0) {
-        sh_dec = strict ? 0 : 1;
-        sh_ft = fp;
-        sh_fp = fp;
+    const int total = a.ntie[task];
+    // ---- the item: up to kPairs ties, their rows to rotate ----
+    if (threadIdx.x < kPairs) {
+      const int p = threadIdx.x;
+      pair_c[p] = -1;
+      if (b0 + p < total) {
+        const int c = a.ties[td.fit_off + b0 + p];
+        pair_c[p] = c;
+        pair_m[p] = sel_target(a, td, mode, k, c);
       }
-    } else {
-      cta_precise_rotation(u, o, qt, DP, D, pr, zt);
-      const bool need_p = isnan(fp);
-      if (need_p) cta_precise_rotation(x, o, qt, DP, D, pr, zp);
-      if (warp == 0) {
+    }
+    __syncthreads();
+    if (threadIdx.x < kPairs) pair_same[threadIdx.x] = 1;
+    __syncthreads();
+    for (int p = 0; p < kPairs; ++p) {
+      if (pair_c[p] < 0) continue;
+      const float* u = a.U + td.pop_off + (size_t)pair_c[p] * DP;
+      const float* x = a.pop + td.pop_off + (size_t)pair_m[p] * DP;
+      for (int j = threadIdx.x; j < D; j += blockDim.x)
+        if (__float_as_uint(u[j]) != __float_as_uint(x[j])) pair_same[p] = 0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int nj = 0;
+      for (int p = 0; p < kPairs; ++p) {
+        pair_zt[p] = pair_zp[p] = -1;
+        if (pair_c[p] < 0 || pair_same[p]) continue;
+        pair_zt[p] = nj;
+        jrow[nj++] = a.U + td.pop_off + (size_t)pair_c[p] * DP;
+        if (isnan(a.fit64[td.fit_off + pair_m[p]])) {
+          pair_zp[p] = nj;
+          jrow[nj++] = a.pop + td.pop_off + (size_t)pair_m[p] * DP;
+        }
+      }
+      njob = nj;
+    }
+    __syncthreads();
+    const int nj = njob;
+    if (nj > 0) {
+      // exact splits x - o of every job row
+      for (int it = threadIdx.x; it < nj * D; it += blockDim.x) {
+        const int j = it / D, kk = it - j * D;
+        float sh, sl;
+        two_sum(jrow[j][kk], -o[kk], sh, sl);
+        pr[(size_t)j * DP + kk] = make_float2(sh, sl);
+      }
+      __syncthreads();
+      for (int n = threadIdx.x; n < D; n += blockDim.x) {
+        float S[kJobs], C[kJobs];
+#pragma unroll
+        for (int j = 0; j < kJobs; ++j) S[j] = C[j] = 0.f;
+        for (int kk = 0; kk < D; ++kk) {
+          const float q = qt[(size_t)kk * DP + n];
+#pragma unroll
+          for (int j = 0; j < kJobs; ++j) {
+            if (j < nj) {
+              const float2 hl = pr[(size_t)j * DP + kk];
+              const float pp = __fmul_rn(q, hl.x);
+              const float e = __fmaf_rn(q, hl.x, -pp);
+              float t, te;
+              two_sum(S[j], pp, t, te);
+              S[j] = t;
+              C[j] = __fmaf_rn(q, hl.y, __fadd_rn(C[j], __fadd_rn(te, e)));
+            }
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < kJobs; ++j)
+          if (j < nj) zb[(size_t)j * DP + n] = (double)S[j] + (double)C[j];
+      }
+    }
+    __syncthreads();
+    // ---- decisions: warp p decides pair p ----
+    if (warp < kPairs && pair_c[warp] >= 0) {
+      const int p = warp, c = pair_c[p], m = pair_m[p];
+      double fp = a.fit64[td.fit_off + m], ft = fp, fpv = fp;
+      bool d64;
+      if (pair_same[p]) {
+        d64 = !strict;
+      } else {
+        const double* zt = zb + (size_t)pair_zt[p] * DP;
+        const double* zp = pair_zp[p] >= 0 ? zb + (size_t)pair_zp[p] * DP : nullptr;
         const bool tier2 = fc.fid != F_WEIERSTRASS && fc.fid != F_SPHERE && fc.fid != F_ROSENBROCK;
         bool decided = false;
-        int dec = 0;
-        double ft = __longlong_as_double(0x7FF8000000000000ll), fpv = fp;
+        ft = __longlong_as_double(0x7FF8000000000000ll);
+        d64 = false;
         if (tier2) {
           double et, ep = 0.0;
           const double t2 = eval_tier2(fc, zt, &et);
           double p2 = fp;
-          if (need_p) p2 = eval_tier2(fc, zp, &ep);
+          if (zp) p2 = eval_tier2(fc, zp, &ep);
           if (fabs(t2 - p2) > et + ep) {
-            dec = strict ? (t2 < p2) : (t2 <= p2);
+            d64 = strict ? (t2 < p2) : (t2 <= p2);
             decided = true;
           }
         }
         if (!decided) {
           ft = fc.fid == F_WEIERSTRASS ? eval_weier_precise(fc, zt) : eval_tier3(fc, zt);
-          if (need_p) fpv = fc.fid == F_WEIERSTRASS ? eval_weier_precise(fc, zp) : eval_tier3(fc, zp);
-          dec = strict ? (ft < fpv) : (ft <= fpv);
-        }
-        if ((threadIdx.x & 31) == 0) {
-          sh_dec = dec;
-          sh_ft = ft;
-          sh_fp = fpv;
+          if (zp) fpv = fc.fid == F_WEIERSTRASS ? eval_weier_precise(fc, zp) : eval_tier3(fc, zp);
+          d64 = strict ? (ft < fpv) : (ft <= fpv);
         }
       }
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      const bool d64 = sh_dec != 0;
-      const float f32t = a.ftr[td.fit_off + c], f32p = a.fit32[td.fit_off + m];
-      const bool d32 = strict ? (f32t < f32p) : (f32t <= f32p);
-      a.flag[td.fit_off + c] = d64 ? 3 : 0;
-      // FP64 value of whichever vector member m holds afterwards
-      a.fit64[td.fit_off + m] = d64 ? sh_ft : sh_fp;
-      if (a.stats) {
-        atomicAdd(a.stats + 0, 1ull);
-        if (d64 != d32) atomicAdd(a.stats + 1, 1ull);
-        if (sh_same) atomicAdd(a.stats + 6, 1ull);
+      if (lane == 0) {
+        const float f32t = a.ftr[td.fit_off + c], f32p = a.fit32[td.fit_off + m];
+        const bool d32 = strict ? (f32t < f32p) : (f32t <= f32p);
+        a.flag[td.fit_off + c] = d64 ? 3 : 0;
+        // FP64 value of whichever vector member m holds afterwards
+        a.fit64[td.fit_off + m] = d64 ? ft : fpv;
+        if (a.stats) {
+          atomicAdd(a.stats + 0, 1ull);
+          if (d64 != d32) atomicAdd(a.stats + 1, 1ull);
+          if (pair_same[p]) atomicAdd(a.stats + 6, 1ull);
+        }
       }
     }
     __syncthreads();
@@ -913,13 +964,27 @@ int emt_large_select(const emt::LargeArgs& a, int mode, void* stream) {
 }
 
 int emt_large_selection(const emt::LargeArgs& a, int mode, int maxDP, int grid, void* stream) {
-  cudaError_t e = cudaMemsetAsync(a.rcount, 0, sizeof(int32_t), (cudaStream_t)stream);
+  cudaError_t e = cudaMemsetAsync(a.nwork, 0, sizeof(int32_t), (cudaStream_t)stream);
   if (e != cudaSuccess) return (int)e;
   emt::large::classify_kernel<<<a.n_tasks, 256, 0, (cudaStream_t)stream>>>(a, mode);
-  const size_t sm = sizeof(double) * 2 * (size_t)maxDP + sizeof(float2) * (size_t)maxDP;
+  const size_t sm = emt::large::recheck_smem(maxDP);
+  e = cudaFuncSetAttribute(emt::large::recheck_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)sm);
+  if (e != cudaSuccess) return (int)e;
   emt::large::recheck_kernel<<<grid, 256, sm, (cudaStream_t)stream>>>(a, mode);
   emt::large::apply_kernel<<<a.n_tasks, 256, 0, (cudaStream_t)stream>>>(a, mode);
   return (int)cudaGetLastError();
+}
+
+int emt_large_recheck_occupancy(int maxDP) {
+  const size_t sm = emt::large::recheck_smem(maxDP);
+  if (cudaFuncSetAttribute(emt::large::recheck_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)sm) != cudaSuccess)
+    return 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, emt::large::recheck_kernel, 256, sm) != cudaSuccess)
+    return 1;
+  return n;
 }
 
 int emt_large_best(const emt::BestArgs& a, int maxD, void* stream) {
