@@ -769,8 +769,32 @@ __global__ void __launch_bounds__(256) recheck_kernel(const LargeArgs a, int mod
         float S[kJobs], C[kJobs];
 #pragma unroll
         for (int j = 0; j < kJobs; ++j) S[j] = C[j] = 0.f;
-        for (int kk = 0; kk < D; ++kk) {
-          const float q = qt[(size_t)kk * DP + n];
+        // Q loads issued kAhead steps ahead of the dependent compensated updates
+        constexpr int kAhead = 16;
+        const float* qcol = qt + n;
+        int kk = 0;
+        for (; kk + kAhead <= D; kk += kAhead) {
+          float qv[kAhead];
+#pragma unroll
+          for (int u = 0; u < kAhead; ++u) qv[u] = __ldg(qcol + (size_t)(kk + u) * DP);
+#pragma unroll
+          for (int u = 0; u < kAhead; ++u)
+#pragma unroll
+            for (int j = 0; j < kJobs; ++j) {
+              if (j < nj) {
+                const float q = qv[u];
+                const float2 hl = pr[(size_t)j * DP + kk + u];
+                const float pp = __fmul_rn(q, hl.x);
+                const float e = __fmaf_rn(q, hl.x, -pp);
+                float t, te;
+                two_sum(S[j], pp, t, te);
+                S[j] = t;
+                C[j] = __fmaf_rn(q, hl.y, __fadd_rn(C[j], __fadd_rn(te, e)));
+              }
+            }
+        }
+        for (; kk < D; ++kk) {
+          const float q = __ldg(qcol + (size_t)kk * DP);
 #pragma unroll
           for (int j = 0; j < kJobs; ++j) {
             if (j < nj) {
