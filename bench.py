@@ -498,18 +498,23 @@ def large_cpu_baseline(threads, n_tasks=16, gens=2, seed=1):
     import orc
     orc.build()
     p = orc.params(algorithm=2, eta_c=15.0, p_c=0.9, eta_m=15.0, p_m=-1.0, seed=seed)
-    tasks, X, f32, f64 = [], [], [], []
-    for t in range(n_tasks):
+    from concurrent.futures import ThreadPoolExecutor
+
+    def make(t):  # the oracle's FP64 QR releases the GIL: tasks build in parallel
         fid = t % 7
         lo, hi = orc.box(fid)
         Q = orc.gen_rotation(seed, t, LARGE_DIM).astype(np.float32)
         o = orc.gen_shift(seed, t, LARGE_DIM, lo, hi)
         ot = orc.OTask(fid, LARGE_DIM, LARGE_POP, lo, hi, Q, o, 0, t)
         x = orc.gen_population(seed, t, LARGE_POP, LARGE_DIM, lo, hi)
-        f32.append(np.array([ot.eval32(r)[0] for r in x], np.float32))
-        tasks.append(ot)
-        X.append(x)
-        f64.append(np.full(LARGE_POP, np.nan))
+        return ot, x, np.array([ot.eval32(r)[0] for r in x], np.float32)
+
+    with ThreadPoolExecutor(threads) as ex:
+        built = list(ex.map(make, range(n_tasks)))
+    tasks = [b[0] for b in built]
+    X = [b[1] for b in built]
+    f32 = [b[2] for b in built]
+    f64 = [np.full(LARGE_POP, np.nan) for _ in range(n_tasks)]
     secs = orc.run_threads(p, tasks, X, f32, f64, 0, gens, 1, threads)
     ev = n_tasks * LARGE_POP * gens
     return {"value": ev / secs, "unit": UNIT, "cores": threads, "kind": "port",

@@ -275,7 +275,7 @@ static double fvalue64(int fid, uint32_t flags, int D, const double* z, double* 
 }
 
 double orc_eval64(const orc_task* t, const float* x, double* scale, double* zout) {
-  double zb[512];
+  double zb[1024]; /* D <= 1024, the engine's largest island */
   double* z = zout ? zout : zb;
   rotate64(t, x, z);
   return fvalue64(t->fid, t->flags, t->D, z, scale);
@@ -355,7 +355,7 @@ static void weier_terms32(float z, float* sum, float* sabs) {
 
 float orc_eval32(const orc_task* t, const float* x, float* scale) {
   int D = t->D;
-  float z[512];
+  float z[1024]; /* D <= 1024 */
   for (int n = 0; n < D; ++n) {
     if (!t->Q) { z[n] = x[n] - t->o[n]; continue; }
     float acc = 0.f;
