@@ -139,7 +139,19 @@ typedef struct emt_config {
   int32_t schedule;          /* emt_schedule: how an epoch's islands are launched */
   int32_t use_graph;         /* 1: emt_run captures its epoch sequence in a CUDA
                                 graph once and replays it when it recurs        */
-  int32_t reserved[5];
+  /* Sub-islands (the reference's slots of one block, IslandMigration,
+   * SG-EMTF.cu:1138-1218): each island of NP members splits into subislands
+   * groups of NP / subislands (NP must divide; 0 or 1 = one group).  DE and GA
+   * draw partners within the member's own group.  Before the trials of
+   * generation g, when g > 1 and (g - 1) % migration_interval == 0, the r-th
+   * best of group s replaces the r-th worst of group s + 1 (mod subislands),
+   * r < migration_count, when strictly better, all from the pre-migration
+   * state; near ties are decided like any selection.  Islands of D <= 128. */
+  int32_t subislands;
+  int32_t migration_interval; /* generations between migrations; 0 = none       */
+  int32_t migration_count;    /* members each group sends; 0 = NP/subislands/8,
+                                 at least 1; 2 * count <= NP / subislands       */
+  int32_t reserved[2];
 } emt_config;
 
 /* How emt_run launches an epoch's islands (results are identical).  The
@@ -192,6 +204,7 @@ typedef struct emt_stats {
   uint64_t recheck_identical; /* re-checks of a trial bit-identical to its parent */
   int32_t epoch_launches;     /* kernel launches per epoch under the schedule in use */
   int32_t schedule_used;      /* emt_schedule in use | 0x100 when graphs replay  */
+  uint64_t migrations_accepted; /* sub-island migrants that replaced a member   */
 } emt_stats;
 
 /* Fills *cfg with DE/rand/1/bin, F = 0.5, CR = 0.9, SBX eta 15 / p_c 0.9,

@@ -487,11 +487,19 @@ static inline float clampf_box(float v, float lo, float hi) {
   return v;
 }
 
+/* members per sub-island: operators draw partners within the member's own
+ * sub-island (the reference's two slots of one block, SG-EMTF.cu:1138-1218,
+ * evolve apart between migrations) */
+static int sub_size(const orc_params* p, const orc_task* t) {
+  return p->subislands > 1 ? t->NP / p->subislands : t->NP;
+}
+
 static void de_indices(const orc_params* p, const orc_task* t, uint32_t gen, int i, int* r1o,
                        int* r2o, int* r3o, int* jro) {
   uint32_t w[4];
-  int NP = t->NP;
+  const int NP = sub_size(p, t), base = (i / NP) * NP;
   orc_draw(p->seed, t->id, gen, (uint32_t)i, ORC_P_DE_INDEX, 0, w);
+  i -= base;
   int r1 = (int)(w[0] % (uint32_t)(NP - 1));
   if (r1 >= i) r1++;
   int a = i < r1 ? i : r1, b = i < r1 ? r1 : i;
@@ -506,14 +514,15 @@ static void de_indices(const orc_params* p, const orc_task* t, uint32_t gen, int
   if (r3 >= s0) r3++;
   if (r3 >= s1) r3++;
   if (r3 >= s2) r3++;
-  *r1o = r1; *r2o = r2; *r3o = r3;
+  *r1o = r1 + base; *r2o = r2 + base; *r3o = r3 + base;
   *jro = (int)(w[3] % (uint32_t)t->D);
 }
 
 static int ga_parent(const orc_params* p, const orc_task* t, uint32_t gen, int i) {
   uint32_t w[4];
+  const int NP = sub_size(p, t), base = (i / NP) * NP;
   orc_draw(p->seed, t->id, gen, (uint32_t)i, ORC_P_GA_PARENT, 0, w);
-  return (int)(w[0] % (uint32_t)t->NP);
+  return base + (int)(w[0] % (uint32_t)NP);
 }
 
 void orc_trial(const orc_params* p, const orc_task* t, const float* X, uint32_t gen, int i,
@@ -536,8 +545,8 @@ void orc_trial(const orc_params* p, const orc_task* t, const float* X, uint32_t 
   }
   /* GA: SBX on the pair (i, i^1) of drawn parents, then polynomial mutation */
   int r0 = ga_parent(p, t, gen, i);
-  int pi = i ^ 1;
-  int partner = pi < NP ? ga_parent(p, t, gen, pi) : r0;
+  int pi = i ^ 1, NPs = sub_size(p, t);
+  int partner = (pi < NP && pi / NPs == i / NPs) ? ga_parent(p, t, gen, pi) : r0;
   const float *x0 = X + (size_t)r0 * D, *x1 = X + (size_t)partner * D;
   float ec = 1.f / (p->eta_c + 1.f);
   float em1 = p->eta_m + 1.f, em = 1.f / em1;
@@ -727,6 +736,84 @@ int orc_transfer_in(const orc_params* p, const orc_task* t, const orc_task* pt,
 }
 
 /* ------------------------------------------------------------------ */
+/* ring migration between sub-islands                                   */
+/* ------------------------------------------------------------------ */
+int orc_migration_due(const orc_params* p, uint32_t gen) {
+  return p->subislands > 1 && p->mig_interval > 0 && gen > 1u &&
+         (gen - 1u) % (uint32_t)p->mig_interval == 0u;
+}
+
+int orc_migration_count(const orc_params* p, int NP) {
+  const int NPs = NP / (p->subislands > 1 ? p->subislands : 1);
+  if (p->mig_count > 0) return p->mig_count;
+  const int m = NPs / 8;
+  return m < 1 ? 1 : m;
+}
+
+int orc_migrate(const orc_params* p, const orc_task* t, float* X, float* fit32, double* fit64,
+                int mode) {
+  const int D = t->D, NP = t->NP, S = p->subislands > 1 ? p->subislands : 1;
+  const int NPs = NP / S, m = orc_migration_count(p, NP), k = S * m;
+  int replaced = 0;
+  int* byrank = (int*)malloc(sizeof(int) * NP);
+  for (int i = 0; i < NP; ++i) { /* rank within the member's sub-island */
+    const int base = (i / NPs) * NPs;
+    int r = 0;
+    for (int j = base; j < base + NPs; ++j)
+      if (fit32[j] < fit32[i] || (fit32[j] == fit32[i] && j < i)) ++r;
+    byrank[base + r] = i;
+  }
+  /* candidates are the pre-migration members: c = s * m + r is the r-th best
+   * of sub-island s, sent to the r-th worst of sub-island s + 1 (mod S) */
+  float* C = (float*)malloc(sizeof(float) * (size_t)k * D);
+  int* target = (int*)malloc(sizeof(int) * k);
+  for (int c = 0; c < k; ++c) {
+    const int s = c / m, r = c - s * m, d = (s + 1) % S;
+    memcpy(C + (size_t)c * D, X + (size_t)byrank[s * NPs + r] * D, sizeof(float) * D);
+    target[c] = byrank[d * NPs + NPs - 1 - r];
+  }
+  for (int c = 0; c < k; ++c) {
+    const int tm = target[c];
+    float* cv = C + (size_t)c * D;
+    float* xm = X + (size_t)tm * D;
+    int acc;
+    double f64 = NAN;
+    float f32 = NAN;
+    if (mode == 0) {
+      f64 = orc_eval64(t, cv, NULL, NULL);
+      if (isnan(fit64[tm])) fit64[tm] = orc_eval64(t, xm, NULL, NULL);
+      acc = f64 < fit64[tm];
+    } else {
+      float sc, sm;
+      f32 = orc_eval32(t, cv, &sc);
+      orc_eval32(t, xm, &sm);
+      double win = recheck_window(p, t, cv, f32, sc) + recheck_window(p, t, xm, fit32[tm], sm);
+      if (!(p->flags & ORC_FLAG_NO_RECHECK) && fabs((double)f32 - (double)fit32[tm]) <= win) {
+        if (memcmp(cv, xm, sizeof(float) * D) == 0) {
+          acc = 0; /* identical: a tie, and migration needs strictly better */
+        } else {
+          f64 = orc_eval64(t, cv, NULL, NULL);
+          if (isnan(fit64[tm])) fit64[tm] = orc_eval64(t, xm, NULL, NULL);
+          acc = f64 < fit64[tm];
+        }
+      } else {
+        acc = f32 < fit32[tm];
+      }
+    }
+    if (acc) {
+      memcpy(xm, cv, sizeof(float) * D);
+      fit64[tm] = f64;
+      fit32[tm] = mode == 0 ? (float)f64 : f32;
+      ++replaced;
+    }
+  }
+  free(C);
+  free(target);
+  free(byrank);
+  return replaced;
+}
+
+/* ------------------------------------------------------------------ */
 /* multi-threaded CPU run over tasks                                    */
 /* ------------------------------------------------------------------ */
 typedef struct {
@@ -749,9 +836,12 @@ static void* run_worker(void* arg) {
     int t = c->next++;
     pthread_mutex_unlock(&c->mu);
     if (t >= c->n) break;
-    for (int g = 0; g < c->gens; ++g)
-      orc_generation(c->p, &c->tasks[t], c->X[t], c->f32[t], c->f64[t],
-                     c->gen0 + (uint32_t)g + 1u, c->mode, NULL);
+    for (int g = 0; g < c->gens; ++g) {
+      const uint32_t G = c->gen0 + (uint32_t)g + 1u;
+      if (orc_migration_due(c->p, G))
+        orc_migrate(c->p, &c->tasks[t], c->X[t], c->f32[t], c->f64[t], c->mode);
+      orc_generation(c->p, &c->tasks[t], c->X[t], c->f32[t], c->f64[t], G, c->mode, NULL);
+    }
   }
   return NULL;
 }

@@ -92,6 +92,10 @@ typedef struct orc_params {
   uint64_t seed;
   double recheck_rel;
   uint32_t flags;
+  int subislands;   /* sub-islands per island (1 = one island); operators draw
+                       partners within the member's sub-island            */
+  int mig_interval; /* generations between ring migrations (0 = none)     */
+  int mig_count;    /* members each sub-island sends                      */
 } orc_params;
 
 int orc_box(int fid, int reference_boxes, float* lo, float* hi);
@@ -134,6 +138,16 @@ void orc_rank(const float* fit32, int NP, int* rank);
 /* Elite transfer into task t from partner p (elites: partner's top k rows,
  * k*Dp floats with row stride Dp).  gen: the generation number after which
  * the transfer happens.  Returns the number of members replaced. */
+/* Ring migration between the sub-islands of one island (IslandMigration,
+ * SG-EMTF.cu:1138-1218, generalised from two slots to a ring): ranks each
+ * sub-island by fit32; the i-th best of sub-island s replaces the i-th worst
+ * of s + 1 when strictly better (FP64 in mode 0), all from the
+ * pre-migration state.  Runs before the trials of generation gen when
+ * orc_migration_due(p, gen).  Returns the replacements. */
+int orc_migration_due(const orc_params* p, uint32_t gen);
+int orc_migration_count(const orc_params* p, int NP);
+int orc_migrate(const orc_params* p, const orc_task* t, float* X, float* fit32, double* fit64,
+                int mode);
 int orc_transfer_partner(const orc_params* p, uint32_t t, uint32_t n_tasks, uint32_t gen);
 int orc_transfer_in(const orc_params* p, const orc_task* t, const orc_task* partner,
                     const float* elites, int k, float* X, float* fit32, double* fit64,

@@ -44,7 +44,8 @@ class Params(ctypes.Structure):
                 ("eta_c", ctypes.c_float), ("p_c", ctypes.c_float), ("eta_m", ctypes.c_float),
                 ("p_m", ctypes.c_float), ("transfer_mix", ctypes.c_float),
                 ("seed", ctypes.c_uint64), ("recheck_rel", ctypes.c_double),
-                ("flags", ctypes.c_uint32)]
+                ("flags", ctypes.c_uint32), ("subislands", ctypes.c_int),
+                ("mig_interval", ctypes.c_int), ("mig_count", ctypes.c_int)]
 
 
 class CvrpParams(ctypes.Structure):
@@ -101,6 +102,13 @@ def lib():
         L.orc_transfer_in.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(Task),
                                       ctypes.POINTER(Task), _F32P, ctypes.c_int, _F32P, _F32P,
                                       _F64P, ctypes.c_uint32, ctypes.c_int]
+        L.orc_migration_due.restype = ctypes.c_int
+        L.orc_migration_due.argtypes = [ctypes.POINTER(Params), ctypes.c_uint32]
+        L.orc_migration_count.restype = ctypes.c_int
+        L.orc_migration_count.argtypes = [ctypes.POINTER(Params), ctypes.c_int]
+        L.orc_migrate.restype = ctypes.c_int
+        L.orc_migrate.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(Task), _F32P, _F32P,
+                                  _F64P, ctypes.c_int]
         L.orc_run_threads.restype = ctypes.c_double
         L.orc_run_threads.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(Task), ctypes.c_int,
                                       ctypes.POINTER(_F32P), ctypes.POINTER(_F32P),
@@ -211,9 +219,10 @@ class OTask:
 
 
 def params(algorithm=DE_RAND1, F=0.5, CR=0.9, eta_c=15.0, p_c=0.9, eta_m=15.0, p_m=-1.0,
-           transfer_mix=0.4, seed=1, recheck_rel=0.0, flags=0):
+           transfer_mix=0.4, seed=1, recheck_rel=0.0, flags=0, subislands=1, mig_interval=0,
+           mig_count=0):
     return Params(algorithm, F, CR, eta_c, p_c, eta_m, p_m, transfer_mix, seed, recheck_rel,
-                  flags)
+                  flags, subislands, mig_interval, mig_count)
 
 
 def generation(p, t, X, fit32, fit64, gen, mode):
@@ -245,6 +254,20 @@ def transfer_in(p, t, pt, elites, X, fit32, fit64, gen, mode):
     return lib().orc_transfer_in(ctypes.byref(p), ctypes.byref(t.c), ctypes.byref(pt.c),
                                  _p32(elites), elites.shape[0], _p32(X), _p32(fit32),
                                  _p64(fit64), gen, mode)
+
+
+def migration_due(p, gen):
+    return bool(lib().orc_migration_due(ctypes.byref(p), gen))
+
+
+def migration_count(p, NP):
+    return lib().orc_migration_count(ctypes.byref(p), NP)
+
+
+def migrate(p, t, X, fit32, fit64, mode):
+    """Ring migration between the sub-islands of task t; returns replacements."""
+    return lib().orc_migrate(ctypes.byref(p), ctypes.byref(t.c), _p32(X), _p32(fit32),
+                             _p64(fit64), mode)
 
 
 def run_threads(p, tasks, X, fit32, fit64, gen0, gens, mode, threads):

@@ -482,7 +482,7 @@ int upload(emt_handle* h) {
       (e = h->d_qt.ensure((size_t)q)) != cudaSuccess ||
       (e = h->d_shift.ensure((size_t)o)) != cudaSuccess ||
       (e = h->d_gen.ensure(n)) != cudaSuccess ||
-      (e = h->d_stats.ensure(7)) != cudaSuccess || (e = h->d_err.ensure(1)) != cudaSuccess ||
+      (e = h->d_stats.ensure(emt::kStats)) != cudaSuccess || (e = h->d_err.ensure(1)) != cudaSuccess ||
       (e = h->d_best_idx.ensure(n)) != cudaSuccess ||
       (e = h->d_best_f32.ensure(n)) != cudaSuccess ||
       (e = h->d_best_f64.ensure(n)) != cudaSuccess)
@@ -496,7 +496,7 @@ int upload(emt_handle* h) {
       (e = cudaMemcpy(h->d_shift.p, ho.data(), sizeof(float) * ho.size(), cudaMemcpyHostToDevice)) ||
       (e = cudaMemset(h->d_gen.p, 0, sizeof(uint32_t) * n)) ||
       (e = cudaMemset(h->d_pop.p, 0, sizeof(float) * (size_t)pop)) ||
-      (e = cudaMemset(h->d_stats.p, 0, sizeof(unsigned long long) * 7)) ||
+      (e = cudaMemset(h->d_stats.p, 0, sizeof(unsigned long long) * emt::kStats)) ||
       (e = cudaMemset(h->d_zcb.p, 0xFF, sizeof(float) * 2 * (size_t)fit)) ||
       (e = cudaMemset(h->d_err.p, 0, sizeof(int32_t))))
     return h->cuda_fail(e, "upload");
@@ -566,6 +566,9 @@ emt::EpochArgs base_args(emt_handle* h, int mode) {
   a.smem_bytes = h->smem_bytes;
   a.tc_np = h->tc_np;
   a.tc_kp = h->tc_kp;
+  a.subislands = h->cfg.subislands > 1 ? h->cfg.subislands : 1;
+  a.mig_interval = h->cfg.migration_interval;
+  a.mig_count = h->cfg.migration_count;
   return a;
 }
 
@@ -893,7 +896,9 @@ int emt_create(const emt_config* cfg, emt_handle_t** out) {
       !(cfg->eta_c >= 0.f) || !(cfg->eta_m >= 0.f) || !(cfg->p_m <= 1.f) ||
       !std::isfinite(cfg->F) || cfg->transfer_interval < 0 ||
       !(cfg->transfer_rate > 0.f && cfg->transfer_rate <= 1.f) ||
-      !(cfg->transfer_mix >= 0.f && cfg->transfer_mix <= 1.f) || !(cfg->recheck_rel >= 0.0))
+      !(cfg->transfer_mix >= 0.f && cfg->transfer_mix <= 1.f) || !(cfg->recheck_rel >= 0.0) ||
+      cfg->subislands < 0 || cfg->subislands > EMT_MAX_POP / 4 || cfg->migration_interval < 0 ||
+      cfg->migration_count < 0)
     return EMT_ERR_INVALID_ARG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return EMT_ERR_CUDA;
@@ -930,6 +935,17 @@ int emt_add_tasks(emt_handle_t* h, int32_t n, const emt_task_desc* td) {
       return h->fail(EMT_ERR_INVALID_ARG, "task " + std::to_string(i) + ": dim out of range");
     if (d.pop < 4 || d.pop > EMT_MAX_POP)
       return h->fail(EMT_ERR_INVALID_ARG, "task " + std::to_string(i) + ": pop out of range");
+    if (h->cfg.subislands > 1) {
+      const int S = h->cfg.subislands, NPs = d.pop / S;
+      const int m = h->cfg.migration_count > 0 ? h->cfg.migration_count : std::max(1, NPs / 8);
+      if (d.pop % S != 0 || NPs < 4 || 2 * m > NPs)
+        return h->fail(EMT_ERR_INVALID_ARG, "task " + std::to_string(i) +
+                                                ": pop must split into sub-islands of >= 4 "
+                                                "members, each sending at most half");
+      if (d.dim > emt::kMaxDim)
+        return h->fail(EMT_ERR_UNSUPPORTED, "task " + std::to_string(i) +
+                                                ": sub-islands serve islands of D <= 128");
+    }
     if (d.dim <= emt::kMaxDim && (size_t)smem_cap < emt::smem_layout(d.dim, d.pop, false).total)
       return h->fail(EMT_ERR_UNSUPPORTED, "task " + std::to_string(i) +
                                               ": island does not fit in shared memory");
@@ -1384,7 +1400,7 @@ int emt_get_stats(emt_handle_t* h, emt_stats* out) {
   if (h->d_stats.p) {
     int rc = emt_sync(h);
     if (rc) return rc;
-    unsigned long long s[7];
+    unsigned long long s[emt::kStats];
     cudaError_t e = cudaMemcpy(s, h->d_stats.p, sizeof(s), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return h->cuda_fail(e, "copy stats");
     out->recheck_differential = s[4];
@@ -1394,6 +1410,7 @@ int emt_get_stats(emt_handle_t* h, emt_stats* out) {
     out->recheck_flips = s[1];
     out->transfers_accepted = s[2];
     out->evaluations = s[3];
+    out->migrations_accepted = s[7];
     out->generations = h->initialized ? (uint64_t)h->gdone * h->tasks.size() : 0;
   }
   out->device_ms = h->device_ms;

@@ -39,6 +39,8 @@ constexpr size_t kSmemLimit = 227 * 1024;
 
 enum Mode : int { MODE_EPOCH = 0, MODE_INIT = 1, MODE_EVAL = 2 };
 
+constexpr int kStats = 8;  // device counters, indexed as in EpochArgs::stats
+
 struct EpochArgs {
   const TaskDev* tasks;
   const int32_t* order;  // CTA -> task (longest-first)
@@ -67,6 +69,7 @@ struct EpochArgs {
                               // [4] re-checks decided by the differential form
                               // [5] member anchors (compensated rotations) computed
                               // [6] re-checks of bit-identical trials
+                              // [7] sub-island migrants accepted
   // per member: compensated rotation z_h, z_l (2 * DP floats, at 2 * pop_off)
   // and {error bound, refresh limit} (at 2 * fit_off); NaN bound = not cached
   float* zc;
@@ -74,6 +77,8 @@ struct EpochArgs {
   int32_t* err;               // first kernel-side check that fired (0 = none)
   size_t smem_bytes;          // dynamic shared memory the launch provides
   int32_t tc_np, tc_kp;       // tensor-core form: padded N and K of the B tiles
+  // sub-islands: groups per island (1 = none), migration interval and count
+  int32_t subislands, mig_interval, mig_count;
 };
 
 // Islands too large for one CTA's shared memory (D > kMaxDim, up to

@@ -279,14 +279,17 @@ __device__ void build_trials(const Smem& s, const EpochArgs& a, const TaskDev& t
                              uint32_t G, int DP, int NPP) {
   const int D = td.D, NP = td.NP;
   const float lo = td.lo, hi = td.hi;
+  // partners come from the member's own sub-island of NPs members
+  const int NPs = NP / a.subislands;
   if (a.algorithm == 0 || a.algorithm == 1) {
     for (int i = threadIdx.x; i < NP; i += kThreads) {
       const U4 w = draw(a.seed, (uint32_t)task, G, (uint32_t)i, P_DE_INDEX, 0);
+      const int base = a.subislands > 1 ? (i / NPs) * NPs : 0;
       int r1, r2, r3, jr;
-      de_indices(w, i, NP, D, r1, r2, r3, jr);
-      s.idx[4 * i + 0] = a.algorithm == 0 ? r1 : i;
-      s.idx[4 * i + 1] = r2;
-      s.idx[4 * i + 2] = r3;
+      de_indices(w, i - base, NPs, D, r1, r2, r3, jr);
+      s.idx[4 * i + 0] = a.algorithm == 0 ? base + r1 : i;
+      s.idx[4 * i + 1] = base + r2;
+      s.idx[4 * i + 2] = base + r3;
       s.idx[4 * i + 3] = jr;
     }
     __syncthreads();
@@ -319,8 +322,11 @@ __device__ void build_trials(const Smem& s, const EpochArgs& a, const TaskDev& t
   }
   // GA: parent index per member (CrossPrep, SG-EMTF.cu:803-812), SBX on the
   // pair (i, i^1) (:711-749) and polynomial mutation (:565-605).
-  for (int i = threadIdx.x; i < NP; i += kThreads)
-    s.idx[i] = (int)(draw(a.seed, (uint32_t)task, G, (uint32_t)i, P_GA_PARENT, 0).x % (uint32_t)NP);
+  for (int i = threadIdx.x; i < NP; i += kThreads) {
+    const int base = a.subislands > 1 ? (i / NPs) * NPs : 0;
+    s.idx[i] = base + (int)(draw(a.seed, (uint32_t)task, G, (uint32_t)i, P_GA_PARENT, 0).x %
+                            (uint32_t)NPs);
+  }
   __syncthreads();
   const float ec = fdiv(1.f, fadd(a.eta_c, 1.f));
   const float em1 = fadd(a.eta_m, 1.f), em = fdiv(1.f, em1);
@@ -331,7 +337,8 @@ __device__ void build_trials(const Smem& s, const EpochArgs& a, const TaskDev& t
     const int b = it / NP, i = it - b * NP;
     const int r0 = s.idx[i];
     const int pi = i ^ 1;
-    const int partner = pi < NP ? s.idx[pi] : r0;
+    const bool paired = pi < NP && (a.subislands == 1 || pi / NPs == i / NPs);
+    const int partner = paired ? s.idx[pi] : r0;
     const U4 ws = draw(a.seed, (uint32_t)task, G, (uint32_t)i, P_GA_SBX, (uint32_t)b);
     const U4 wm = draw(a.seed, (uint32_t)task, G, (uint32_t)i, P_GA_PM, (uint32_t)b);
 #pragma unroll
@@ -545,6 +552,50 @@ __device__ void rank_members(const Smem& s, int NP, int* byrank) {
   __syncthreads();
 }
 
+// Ring migration between the sub-islands of one island (IslandMigration,
+// SG-EMTF.cu:1138-1218, which exchanges between the two slots of a block):
+// each sub-island is ranked by FP32 fitness (ties by index, as the
+// reference's odd-even transposition sort keeps them); candidate c = s*m + r
+// is a copy of the r-th best of sub-island s and targets the r-th worst of
+// s + 1 (mod S).  Candidates are copied before any replacement, so every
+// exchange starts from the pre-migration state; the decision is the strict
+// transfer selection, re-checks included.  No evaluations: a copy carries its
+// source's FP32 fitness and tolerance.
+__device__ void migrate(const Smem& s, const EpochArgs& a, const FnConst& fc, int NP, int DP,
+                        unsigned long long* st_re, unsigned long long* st_fl) {
+  const int S = a.subislands, NPs = NP / S;
+  const int m = a.mig_count > 0 ? a.mig_count : max(1, NPs / 8), k = S * m;
+  int* byrank = s.idx;       // NP ints
+  int* target = s.idx + NP;  // k <= NP / 2 ints
+  for (int i = threadIdx.x; i < NP; i += kThreads) {
+    const int base = (i / NPs) * NPs;
+    const float fi = s.fit[i];
+    int r = 0;
+    for (int j = base; j < base + NPs; ++j) {
+      const float fj = s.fit[j];
+      r += (fj < fi || (fj == fi && j < i)) ? 1 : 0;
+    }
+    byrank[base + r] = i;
+  }
+  __syncthreads();
+  const int nq = DP >> 2;
+  for (int it = threadIdx.x; it < k * nq; it += kThreads) {
+    const int c = it / nq, q = it - c * nq;
+    const int sc = c / m, src = byrank[sc * NPs + (c - sc * m)];
+    reinterpret_cast<float4*>(s.U + c * DP)[q] = reinterpret_cast<const float4*>(s.X + src * DP)[q];
+  }
+  for (int c = threadIdx.x; c < k; c += kThreads) {
+    const int sc = c / m, r = c - sc * m, src = byrank[sc * NPs + r];
+    const int dst = sc + 1 == S ? 0 : sc + 1;
+    target[c] = byrank[dst * NPs + NPs - 1 - r];
+    s.ftr[c] = s.fit[src];
+    s.ttr[c] = s.tol[src];
+  }
+  __syncthreads();
+  const int acc = select_and_replace(s, a, fc, k, target, true, DP, st_re, st_fl);
+  if (acc && a.stats) atomicAdd(a.stats + 7, (unsigned long long)acc);
+}
+
 __device__ __forceinline__ int transfer_k(float rate, int NP) {
   int k = (int)(rate * (float)NP + 0.5f);
   return k < 1 ? 1 : (k > NP ? NP : k);
@@ -731,6 +782,9 @@ __device__ __forceinline__ void epoch_body(const EpochArgs& a, const void* tmap,
     // ---- generations ----
     for (int g = 0; g < a.gens; ++g) {
       const uint32_t G = gen0 + (uint32_t)g + 1u;
+      if (a.subislands > 1 && a.mig_interval > 0 && G > 1u &&
+          (G - 1u) % (uint32_t)a.mig_interval == 0u)
+        migrate(s, a, fc, NP, DP, st_re, st_fl);
       build_trials<TC>(s, a, td, task, G, DP, NPP);
       __syncthreads();
       evaluate_rows<TC>(s, fc, s.U, NP, DP, NPP, s.ftr, s.ttr, phase);

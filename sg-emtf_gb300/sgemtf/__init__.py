@@ -57,7 +57,9 @@ class Config(ctypes.Structure):
                 ("transfer_mix", ctypes.c_float), ("flags", ctypes.c_uint32),
                 ("seed", ctypes.c_uint64), ("recheck_rel", ctypes.c_double),
                 ("device", ctypes.c_int32), ("schedule", ctypes.c_int32),
-                ("use_graph", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5)]
+                ("use_graph", ctypes.c_int32), ("subislands", ctypes.c_int32),
+                ("migration_interval", ctypes.c_int32), ("migration_count", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 2)]
 
     def __init__(self, **kw):
         super().__init__()
@@ -83,7 +85,7 @@ class Stats(ctypes.Structure):
                 ("n_tasks", ctypes.c_int32), ("precision_used", ctypes.c_int32),
                 ("recheck_differential", ctypes.c_uint64), ("anchor_rotations", ctypes.c_uint64),
                 ("recheck_identical", ctypes.c_uint64), ("epoch_launches", ctypes.c_int32),
-                ("schedule_used", ctypes.c_int32)]
+                ("schedule_used", ctypes.c_int32), ("migrations_accepted", ctypes.c_uint64)]
 
 
 class TaskDesc:

@@ -19,7 +19,8 @@ def oracle_params(orc, eng):
     c = eng.config
     return orc.params(algorithm=c.algorithm, F=c.F, CR=c.CR, eta_c=c.eta_c, p_c=c.p_c,
                       eta_m=c.eta_m, p_m=c.p_m, transfer_mix=c.transfer_mix, seed=c.seed,
-                      recheck_rel=c.recheck_rel, flags=c.flags)
+                      recheck_rel=c.recheck_rel, flags=c.flags, subislands=max(1, c.subislands),
+                      mig_interval=c.migration_interval, mig_count=c.migration_count)
 
 
 def tolerance(orc, t, x, scale):
