@@ -138,8 +138,12 @@ const float kBoxRef[7][2] = {{-100.f, 100.f}, {-50.f, 50.f},   {-50.f, 50.f}, {-
 const int kRefToFid[7] = {EMT_SPHERE,   EMT_ROSENBROCK,  EMT_ACKLEY,  EMT_RASTRIGIN,
                           EMT_GRIEWANK, EMT_WEIERSTRASS, EMT_SCHWEFEL};
 
-// Relative cost of one gene's function term, for the longest-first order.
-const float kFnCost[7] = {1.f, 16.f, 18.f, 30.f, 6.f, 28.f, 200.f};
+// Relative cost per gene of one island's generation beyond the rotation
+// (D + 40), for the longest-first order.  Fitted to measured island times of
+// 2000-generation runs (D = 50, NP = 64, GB300), where the near-tie re-checks
+// of converged islands dominate: a Rosenbrock island then costs 2.3x and a
+// Weierstrass island 2.8x a Sphere island, Griewank 1.3x, the rest ~1x.
+const float kFnCost[7] = {0.f, 3.f, 0.f, 26.f, 114.f, 7.f, 160.f};
 
 // The Weierstrass offset as the reference's host code computes it
 // (SG-EMTF.cu:354-361): PI = 3.1415926 (double), b_ *= 3 in float, cosf.
