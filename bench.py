@@ -585,7 +585,8 @@ def main_large(args, rank, world, local):
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             dev_ms = float(t.item())
         results[name] = {"dev_ms": dev_ms, "gemm_ms": gemm_ms, "setup_s": setup, "clocks": clk.summary(),
-                         "rechecks": st["rechecks"], "transfers": st["transfers_accepted"]}
+                         "rechecks": st["rechecks"], "transfers": st["transfers_accepted"],
+                         "max_rel_err": st["max_rel_err"]}
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
@@ -621,6 +622,7 @@ def main_large(args, rank, world, local):
                       "ms_per_step": v["dev_ms"] / args.steps, "rotation_gemm_ms": v["gemm_ms"],
                       "rotation_tflops_algorithmic": flop / (v["gemm_ms"] * 1e-3) / 1e12,
                       "rechecks": v["rechecks"], "transfers_accepted": v["transfers"],
+                      "max_rel_err_vs_fp64": v["max_rel_err"],
                       "setup_s": v["setup_s"]} for k, v in results.items()},
         "roofline": {"bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": gbs / peaks["hbm_gbs"], "traffic": None, "peak_kind": peak_kind,
@@ -807,6 +809,7 @@ def main():
         "forms": {k: {"value": total_evals / (v["dev_ms"] * 1e-3), "ms_per_step": v["dev_ms"] / args.steps,
                       "epoch_kernel_ms": v["epoch_ms"],
                       "rechecks": v["stats"]["rechecks"], "recheck_flips": v["stats"]["recheck_flips"],
+                      "max_rel_err_vs_fp64": v["stats"]["max_rel_err"],
                       "precision_used": v["precision_used"]} for k, v in results.items()},
         "roofline": roof,
         "clocks": r["clocks"],

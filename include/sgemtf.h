@@ -205,6 +205,9 @@ typedef struct emt_stats {
   int32_t epoch_launches;     /* kernel launches per epoch under the schedule in use */
   int32_t schedule_used;      /* emt_schedule in use | 0x100 when graphs replay  */
   uint64_t migrations_accepted; /* sub-island migrants that replaced a member   */
+  double max_rel_err;         /* largest |f32 - f64| / scale over the tasks' best
+                                 members (scale: the sum of |sub-terms| the FP32
+                                 evaluation states); 0 before emt_reset        */
 } emt_stats;
 
 /* Fills *cfg with DE/rand/1/bin, F = 0.5, CR = 0.9, SBX eta 15 / p_c 0.9,

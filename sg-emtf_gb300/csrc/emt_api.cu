@@ -96,7 +96,7 @@ struct emt_handle {
 
   DevBuf<TaskDev> d_tasks;
   DevBuf<int32_t> d_order;
-  DevBuf<float> d_pop, d_fit32, d_tol32, d_qt, d_shift, d_elites[2], d_best_f32;
+  DevBuf<float> d_pop, d_fit32, d_tol32, d_qt, d_shift, d_elites[2], d_best_f32, d_best_err;
   DevBuf<float> d_zc, d_zcb;  // per-member compensated rotations and their bounds
   DevBuf<double> d_fit64, d_best_f64;
   DevBuf<uint32_t> d_gen;
@@ -489,7 +489,7 @@ int upload(emt_handle* h) {
       (e = h->d_stats.ensure(emt::kStats)) != cudaSuccess || (e = h->d_err.ensure(1)) != cudaSuccess ||
       (e = h->d_best_idx.ensure(n)) != cudaSuccess ||
       (e = h->d_best_f32.ensure(n)) != cudaSuccess ||
-      (e = h->d_best_f64.ensure(n)) != cudaSuccess)
+      (e = h->d_best_f64.ensure(n)) != cudaSuccess || (e = h->d_best_err.ensure(n)) != cudaSuccess)
     return h->cuda_fail(e, "cudaMalloc");
   if (h->cfg.transfer_interval > 0 && n > 1)
     for (int b = 0; b < 2; ++b)
@@ -1264,13 +1264,20 @@ static int ensure_ready(emt_handle* h) {
   return emt_sync(h);
 }
 
+emt::BestArgs best_args(emt_handle* h) {
+  return emt::BestArgs{h->d_tasks.p,  (int32_t)h->tasks.size(), h->d_pop.p, h->d_fit32.p,
+                       h->d_fit64.p,  h->d_qt.p, h->d_shift.p, h->d_best_idx.p,
+                       h->d_best_f32.p, h->d_best_f64.p, h->d_tol32.p,
+                       (float)(h->cfg.recheck_rel > 0 ? h->cfg.recheck_rel : 1e-5),
+                       h->d_best_err.p};
+}
+
 int emt_get_best(emt_handle_t* h, int32_t task, double* fitness, float* x) {
   if (!h) return EMT_ERR_INVALID_ARG;
   if (check_task(h, task)) return h->fail(EMT_ERR_INVALID_ARG, "task index out of range");
   int rc = ensure_ready(h);
   if (rc) return rc;
-  emt::BestArgs b{h->d_tasks.p, (int32_t)h->tasks.size(), h->d_pop.p, h->d_fit32.p, h->d_fit64.p,
-                  h->d_qt.p, h->d_shift.p, h->d_best_idx.p, h->d_best_f32.p, h->d_best_f64.p};
+  const emt::BestArgs b = best_args(h);
   int e = h->large ? emt_large_best(b, h->lKp, h->stream) : emt_launch_best(b, h->stream);
   if (e) return h->cuda_fail((cudaError_t)e, "best launch");
   if ((rc = emt_sync(h))) return rc;
@@ -1292,8 +1299,7 @@ int emt_get_best_all(emt_handle_t* h, float* fitness) {
   if (!h || !fitness) return EMT_ERR_INVALID_ARG;
   int rc = ensure_ready(h);
   if (rc) return rc;
-  emt::BestArgs b{h->d_tasks.p, (int32_t)h->tasks.size(), h->d_pop.p, h->d_fit32.p, h->d_fit64.p,
-                  h->d_qt.p, h->d_shift.p, h->d_best_idx.p, h->d_best_f32.p, h->d_best_f64.p};
+  const emt::BestArgs b = best_args(h);
   int e = h->large ? emt_large_best(b, h->lKp, h->stream) : emt_launch_best(b, h->stream);
   if (e) return h->cuda_fail((cudaError_t)e, "best launch");
   cudaError_t ce = cudaMemcpyAsync(fitness, h->d_best_f32.p, sizeof(float) * h->tasks.size(),
@@ -1416,6 +1422,20 @@ int emt_get_stats(emt_handle_t* h, emt_stats* out) {
     out->evaluations = s[3];
     out->migrations_accepted = s[7];
     out->generations = h->initialized ? (uint64_t)h->gdone * h->tasks.size() : 0;
+  }
+  if (h->initialized && !h->tasks.empty()) {
+    // the largest relative error of a task's best FP32 fitness against its
+    // FP64-class value
+    const emt::BestArgs b = best_args(h);
+    int e = h->large ? emt_large_best(b, h->lKp, h->stream) : emt_launch_best(b, h->stream);
+    if (e) return h->cuda_fail((cudaError_t)e, "best launch");
+    std::vector<float> err(h->tasks.size());
+    cudaError_t ce = cudaMemcpyAsync(err.data(), h->d_best_err.p, sizeof(float) * err.size(),
+                                     cudaMemcpyDeviceToHost, h->stream);
+    if (ce != cudaSuccess) return h->cuda_fail(ce, "copy best error");
+    int rc = emt_sync(h);
+    if (rc) return rc;
+    for (float v : err) out->max_rel_err = std::max(out->max_rel_err, (double)v);
   }
   out->device_ms = h->device_ms;
   if (h->uploaded) {
@@ -1547,6 +1567,7 @@ void emt_destroy(emt_handle_t* h) {
   h->d_zc.release();
   h->d_zcb.release();
   h->d_best_f64.release();
+  h->d_best_err.release();
   h->d_gen.release();
   h->d_stats.release();
   h->d_err.release();

@@ -924,6 +924,7 @@ __global__ void __launch_bounds__(32) best_kernel(const BestArgs a) {
     a.best_idx[task] = bi;
     a.best_f32[task] = bf;
     a.best_f64[task] = f64;
+    if (a.best_err) a.best_err[task] = best_rel_err(td, bf, f64, a.tol32[td.fit_off + bi], a.rel);
   }
 }
 

@@ -85,7 +85,8 @@ class Stats(ctypes.Structure):
                 ("n_tasks", ctypes.c_int32), ("precision_used", ctypes.c_int32),
                 ("recheck_differential", ctypes.c_uint64), ("anchor_rotations", ctypes.c_uint64),
                 ("recheck_identical", ctypes.c_uint64), ("epoch_launches", ctypes.c_int32),
-                ("schedule_used", ctypes.c_int32), ("migrations_accepted", ctypes.c_uint64)]
+                ("schedule_used", ctypes.c_int32), ("migrations_accepted", ctypes.c_uint64),
+                ("max_rel_err", ctypes.c_double)]
 
 
 class TaskDesc:

@@ -116,3 +116,27 @@ def test_empty_evaluate_and_zero_generations(sgemtf, orc):
     X0 = eng.population(0)[0]
     eng.run(0)
     assert np.array_equal(eng.population(0)[0], X0)
+
+
+def test_stats_state_max_relative_error(sgemtf, orc):
+    """emt_get_stats reports the largest |f32 - f64| / scale over the tasks'
+    best members (scale as the FP32 evaluation states it); the FP32 form's
+    stated bound is 1e-5 (Weierstrass 5e-5).  Sphere islands at integer
+    points evaluate exactly, so their figure is 0."""
+    specs = [(f, 50, 32, 1) for f in range(7)]
+    eng, tasks = make_engine(sgemtf, orc, specs, seed=5)
+    assert eng.stats()["max_rel_err"] == 0.0  # nothing evaluated yet
+    eng.run(30)
+    s = eng.stats()
+    assert 0.0 < s["max_rel_err"] <= 5e-5
+    for i, t in enumerate(tasks):  # the oracle's own check of the same members
+        X, f = eng.population(i)
+        b = int(np.argmin(f))
+        f64, scale, _ = t.eval64(X[b])
+        assert abs(float(f[b]) - f64) <= 5e-5 * scale
+    exact = sgemtf.Engine(sgemtf.Config(seed=5))
+    exact.add_tasks([sgemtf.TaskDesc(0, 8, 8, rotation=sgemtf.ROTATION_IDENTITY,
+                                     shift=np.zeros(8, np.float32))])
+    exact.reset()
+    exact.set_population(0, np.arange(64, dtype=np.float32).reshape(8, 8) % 5 - 2)
+    assert exact.stats()["max_rel_err"] == 0.0
