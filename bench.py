@@ -67,7 +67,9 @@ def parse():
     p.add_argument("--gens", type=int, default=GENS)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--workload", default="continuous", choices=["continuous", "cvrp", "uneven", "large"])
+    p.add_argument("--workload", default="continuous",
+                   choices=["continuous", "cvrp", "uneven", "large", "quality"])
+    p.add_argument("--seeds", type=int, default=30)
     return p.parse_args()
 
 
@@ -640,9 +642,49 @@ def main_large(args, rank, world, local):
         dist.destroy_process_group()
 
 
+def main_quality(args, rank, world, local):
+    """--workload quality: the statistical harness (sgemtf/quality.py) beside
+    the reference's own recorded runs of the same setting."""
+    if rank != 0:
+        return
+    import sgemtf
+    from sgemtf import quality
+
+    t0 = time.perf_counter()
+    types, rec = quality.run(seeds=args.seeds, device=local)
+    wall = time.perf_counter() - t0
+    ours = quality.summarise(types, rec)
+    golden = os.path.join(ROOT, "tests", "golden")
+    with open(os.path.join(golden, "reference_records_T100.json")) as f:
+        ref = json.load(f)
+    with open(os.path.join(golden, "reference_ano_T100.json")) as f:
+        ref_ano = [float(v) for v in json.load(f)["ano"]]
+    runs = np.array(ref["runs"])  # [18 runs, 100 tasks, (gen 0, gen 1000, 481st)]
+    rtypes = np.array(ref["types"])
+    names = {0: "sphere", 1: "rosenbrock", 2: "ackley", 3: "rastrigin", 4: "griewank",
+             5: "weierstrass", 6: "schwefel"}
+    per_type = {}
+    for rt, v in ours["per_type"].items():
+        r = runs[:, rtypes == rt, 1]
+        per_type[names[rt]] = {
+            "tasks": v["tasks"], "mean": v["mean"], "median": v["median"],
+            "reference_mean": float(r.mean()), "reference_median": float(np.median(r)),
+            "median_ratio": v["median"] / float(np.median(r))}
+    print(json.dumps({
+        "metric": "best fitness after 1000 generations over %d seeds vs the reference's 18 "
+                  "recorded runs (100 tasks, D=50, GA, reference instances)" % args.seeds,
+        "workload": "quality", "seeds": args.seeds, "reference_runs": int(runs.shape[0]),
+        "per_type": per_type, "ano": ours["ano"], "ano_reference": ref_ano,
+        "ano_final": ours["ano"][-1], "ano_reference_final": ref_ano[-1],
+        "island": "256 members (the reference: 512)", "wall_s": wall,
+        "data": "synthetic (reference-distributed diagonal instances, seeded)"}))
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.workload == "quality" and args.impl == "ours":
+        return main_quality(args, rank, world, local)
     if args.workload == "cvrp" and args.impl == "ours":
         return main_cvrp(args, rank, world, local)
     if args.workload == "uneven" and args.impl == "ours":

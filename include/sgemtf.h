@@ -295,6 +295,10 @@ EMT_API int emt_get_population(emt_handle_t* h, int32_t task, float* x, float* f
 /* Replaces one task's population and evaluates it on the device. */
 EMT_API int emt_set_population(emt_handle_t* h, int32_t task, const float* x);
 
+/* A task's function id, dimension and island size, as added. */
+EMT_API int emt_get_task_info(emt_handle_t* h, int32_t task, int32_t* function, int32_t* dim,
+                              int32_t* pop);
+
 /* The rotation (D*D FP32, row-major) and shift (D) the device uses. */
 EMT_API int emt_get_task_params(emt_handle_t* h, int32_t task, float* rotation, float* shift);
 
@@ -369,6 +373,41 @@ EMT_API int emt_cvrp_evaluate(emt_cvrp_handle_t* h, int32_t inst, int32_t count,
 EMT_API int emt_cvrp_get_stats(emt_cvrp_handle_t* h, emt_stats* out);
 EMT_API const char* emt_cvrp_last_error(const emt_cvrp_handle_t* h);
 EMT_API void emt_cvrp_destroy(emt_cvrp_handle_t* h);
+
+/* ---- run records and the reference's output files (emt_records.cpp) ----
+ *
+ * emt_record_run runs `generations` (a multiple of `interval`) in steps of
+ * `interval` and fills record[t * (P + 2) + c], P = generations / interval:
+ * the best FP32 fitness of task t at generation g0 + c * interval for
+ * c = 0..P (g0 = the handle's generation count on entry), then the fitness
+ * of rank 32 * ((NP - 1) / 32) (ascending) of the population on entry, the
+ * reference's "near-worst" (SG-EMTF_DE.cu:1575,1594-1595,1632: best and
+ * first entry of the last 32-member bank of the sorted population). */
+EMT_API int emt_record_run(emt_handle_t* h, int32_t generations, int32_t interval, void* stream,
+                           float* record);
+
+/* Appends one run's rows (tasks x cols floats, "%g " each, newline per task)
+ * and a blank line, the data_record_* layout (SG-EMTF_DE.cu:1791-1809) that
+ * the reference's ANO tool reads run by run (data process/源.cpp:127-149). */
+EMT_API int emt_write_record(const char* path, int32_t tasks, int32_t cols, const float* record);
+
+/* The average normalised objective (data process/源.cpp:172-203) of `runs`
+ * records of `tasks` x `cols` (cols - 1 recording points, then the
+ * near-worst): per task, min over runs of the last point and max over runs
+ * of the near-worst; ano[j] = mean over tasks and runs of
+ * (record - min) / (max - min), 0 where max == min; FP32 arithmetic in the
+ * tool's order.  ano receives cols - 1 floats. */
+EMT_API int emt_ano(int32_t runs, int32_t tasks, int32_t cols, const float* records, float* ano);
+
+/* Appends every task's FP32 fitness in ascending order, one line per task,
+ * then a blank line (output_0.txt, SG-EMTF.cu:1971-1983). */
+EMT_API int emt_write_fitness(emt_handle_t* h, const char* path);
+
+/* Writes para.txt (SG-EMTF.cu:244-264): per task, D pairs "M b" of its
+ * diagonal instance z = M (x + b), i.e. the diagonal rotation's factors and
+ * b = -shift; a blank line; then the tasks' reference type ids.  Tasks whose
+ * rotation is not diagonal have no such form: EMT_ERR_UNSUPPORTED. */
+EMT_API int emt_write_para(emt_handle_t* h, const char* path);
 
 EMT_API const char* emt_last_error(const emt_handle_t* h);
 EMT_API const char* emt_status_string(int status);

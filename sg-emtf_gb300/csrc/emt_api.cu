@@ -1349,6 +1349,17 @@ int emt_set_population(emt_handle_t* h, int32_t task, const float* x) {
   return emt_sync(h);
 }
 
+int emt_get_task_info(emt_handle_t* h, int32_t task, int32_t* function, int32_t* dim,
+                      int32_t* pop) {
+  if (!h) return EMT_ERR_INVALID_ARG;
+  if (check_task(h, task)) return h->fail(EMT_ERR_INVALID_ARG, "task index out of range");
+  const HostTask& t = h->tasks[task];
+  if (function) *function = t.fid;
+  if (dim) *dim = t.D;
+  if (pop) *pop = t.NP;
+  return EMT_OK;
+}
+
 int emt_get_task_params(emt_handle_t* h, int32_t task, float* rotation, float* shift) {
   if (!h) return EMT_ERR_INVALID_ARG;
   if (check_task(h, task)) return h->fail(EMT_ERR_INVALID_ARG, "task index out of range");

@@ -39,10 +39,12 @@ NOALLOC_EXCHANGE_FLOATS = 1 << 19
 
 EXPORTED = [
     "emt_config_default", "emt_function_from_reference", "emt_function_box", "emt_create",
-    "emt_add_tasks", "emt_reset", "emt_run", "emt_run_noalloc", "emt_tune", "emt_time_rotation", "emt_sync", "emt_get_best", "emt_get_best_all",
-    "emt_get_population", "emt_set_population", "emt_get_task_params", "emt_evaluate",
-    "emt_get_stats", "emt_snapshot_size", "emt_snapshot", "emt_restore", "emt_last_error",
-    "emt_status_string", "emt_destroy",
+    "emt_add_tasks", "emt_reset", "emt_run", "emt_run_noalloc", "emt_tune", "emt_time_rotation",
+    "emt_sync", "emt_get_best", "emt_get_best_all",
+    "emt_get_population", "emt_set_population", "emt_get_task_info", "emt_get_task_params",
+    "emt_evaluate", "emt_get_stats", "emt_snapshot_size", "emt_snapshot", "emt_restore",
+    "emt_record_run", "emt_write_record", "emt_ano", "emt_write_fitness", "emt_write_para",
+    "emt_last_error", "emt_status_string", "emt_destroy",
     "emt_cvrp_config_default", "emt_cvrp_create", "emt_cvrp_add_instances", "emt_cvrp_reset",
     "emt_cvrp_run", "emt_cvrp_sync", "emt_cvrp_get_best_all", "emt_cvrp_get_population",
     "emt_cvrp_get_instance", "emt_cvrp_evaluate", "emt_cvrp_get_stats", "emt_cvrp_last_error", "emt_cvrp_destroy",
@@ -169,6 +171,13 @@ def lib():
         L.emt_get_population.argtypes = [vp, i32, f32p, f32p]
         L.emt_set_population.argtypes = [vp, i32, f32p]
         L.emt_get_task_params.argtypes = [vp, i32, f32p, f32p]
+        L.emt_get_task_info.argtypes = [vp, i32, ctypes.POINTER(i32), ctypes.POINTER(i32),
+                                        ctypes.POINTER(i32)]
+        L.emt_record_run.argtypes = [vp, i32, i32, vp, f32p]
+        L.emt_write_record.argtypes = [ctypes.c_char_p, i32, i32, f32p]
+        L.emt_ano.argtypes = [i32, i32, i32, f32p, f32p]
+        L.emt_write_fitness.argtypes = [vp, ctypes.c_char_p]
+        L.emt_write_para.argtypes = [vp, ctypes.c_char_p]
         L.emt_evaluate.argtypes = [vp, i32, i32, f32p, f32p, f32p]
         L.emt_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
         L.emt_snapshot_size.argtypes = [vp, ctypes.POINTER(ctypes.c_size_t)]
@@ -212,6 +221,26 @@ def function_box(fid, reference_boxes=False):
     if rc:
         raise EngineError(rc, "function_box")
     return lo.value, hi.value
+
+
+def ano(records):
+    """Average normalised objective of runs x tasks x cols records (cols - 1
+    recording points, then the near-worst), data process/源.cpp:172-203."""
+    r = np.ascontiguousarray(records, np.float32)
+    runs, tasks, cols = r.shape
+    out = np.zeros(cols - 1, np.float32)
+    rc = lib().emt_ano(runs, tasks, cols, _f32(r), _f32(out))
+    if rc:
+        raise EngineError(rc, "emt_ano: %s" % status_string(rc))
+    return out
+
+
+def write_record(path, record):
+    """Appends one run's tasks x cols record and a blank line (data_record_*)."""
+    r = np.ascontiguousarray(record, np.float32)
+    rc = lib().emt_write_record(os.fsencode(path), r.shape[0], r.shape[1], _f32(r))
+    if rc:
+        raise EngineError(rc, "emt_write_record: %s" % status_string(rc))
 
 
 def _f32(a):
@@ -297,6 +326,27 @@ class Engine:
     def set_population(self, task, x):
         x = np.ascontiguousarray(x, np.float32)
         self._check(lib().emt_set_population(self._h, task, _f32(x)), "emt_set_population")
+
+    def task_info(self, task):
+        f, d, p = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        self._check(lib().emt_get_task_info(self._h, task, ctypes.byref(f), ctypes.byref(d),
+                                            ctypes.byref(p)), "emt_get_task_info")
+        return f.value, d.value, p.value
+
+    def record_run(self, generations, interval, stream=None):
+        """Runs in steps of `interval`; returns tasks x (generations/interval + 2):
+        best FP32 fitness at each recording point, then the near-worst."""
+        cols = generations // interval + 2 if interval > 0 else 2
+        rec = np.zeros((len(self.tasks), cols), np.float32)
+        self._check(lib().emt_record_run(self._h, generations, interval, stream, _f32(rec)),
+                    "emt_record_run")
+        return rec
+
+    def write_fitness(self, path):
+        self._check(lib().emt_write_fitness(self._h, os.fsencode(path)), "emt_write_fitness")
+
+    def write_para(self, path):
+        self._check(lib().emt_write_para(self._h, os.fsencode(path)), "emt_write_para")
 
     def task_params(self, task):
         D, _ = self._dim(task)

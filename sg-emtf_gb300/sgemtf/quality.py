@@ -1,0 +1,82 @@
+"""Statistical quality harness: many seeded runs of the reference's own
+multitask setting, their best-fitness records and the average normalised
+objective (ANO, data process/源.cpp:122-209).
+
+The setting is the one the reference recorded its GA runs in
+(data process/ANO_Tnum/data_record_T_ANO_100.txt): 100 tasks whose function
+types come from glibc srand(0); rand() % 7 with task 0 forced to type 6
+(proposed model/SG-EMTF.cu:307-313); D = 50; diagonal instances
+z = M (x + b), M ~ U(0, 1], b ~ U(0, box width] (:181-195); the reference's
+box table and function variants (:197-214, :1029, :354-361, E = 2.718282);
+its GA (SBX eta 2 with every gene crossed, polynomial mutation eta 5 on every
+gene, :44-49,555,718); best fitness recorded every 50 of 1000 generations.
+Elite transfer is off, as in the shipped reference (:1714).  Islands hold
+256 members, the largest this engine serves; the reference evolved 512 per
+task in 32-member blocks."""
+import ctypes
+
+import numpy as np
+
+from . import (FLAG_REF_ACKLEY_E, FLAG_REF_BOXES, FLAG_REF_GRIEWANK_NO_PRODUCT,
+               FLAG_REF_WEIERSTRASS_CONST, ROTATION_DIAG, Config, Engine, TaskDesc, ano,
+               function_box, lib)
+
+REF_FLAGS = (FLAG_REF_BOXES | FLAG_REF_GRIEWANK_NO_PRODUCT | FLAG_REF_WEIERSTRASS_CONST |
+             FLAG_REF_ACKLEY_E)
+GA = 2
+
+
+def reference_types(n):
+    """The reference's task -> type map: glibc srand(0); rand() % 7, task 0 = 6."""
+    libc = ctypes.CDLL("libc.so.6")
+    libc.srand(0)
+    t = [libc.rand() % 7 for _ in range(n)]
+    if n:
+        t[0] = 6
+    return t
+
+
+def reference_instances(types, D, seed=0):
+    """Diagonal instances M ~ U(0, 1], b ~ U(0, box width], one per task."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for rt in types:
+        fid = lib().emt_function_from_reference(rt)
+        lo, hi = function_box(fid, True)
+        M = (1.0 - rng.uniform(0, 1, D)).astype(np.float32)
+        b = ((1.0 - rng.uniform(0, 1, D)) * (hi - lo)).astype(np.float32)
+        out.append((fid, M, b))
+    return out
+
+
+def run(seeds=30, tasks=100, D=50, pop=256, generations=1000, interval=50, device=0,
+        first_seed=1, subislands=1, migration_interval=0, migration_count=0, instance_seed=0):
+    """Records of `seeds` runs: array [seeds, tasks, generations/interval + 2]
+    (best fitness at each recording point, then the initial near-worst)."""
+    types = reference_types(tasks)
+    inst = reference_instances(types, D, instance_seed)
+    rec = np.zeros((seeds, tasks, generations // interval + 2), np.float32)
+    for s in range(seeds):
+        eng = Engine(Config(seed=first_seed + s, algorithm=GA, eta_c=2.0, p_c=1.0, eta_m=5.0,
+                            p_m=1.0, flags=REF_FLAGS, device=device, subislands=subislands,
+                            migration_interval=migration_interval,
+                            migration_count=migration_count))
+        eng.add_tasks([TaskDesc(fid, D, pop, rotation=ROTATION_DIAG, diag=M, shift=-b)
+                       for fid, M, b in inst])
+        eng.reset()
+        rec[s] = eng.record_run(generations, interval)
+        eng.close()
+    return types, rec
+
+
+def summarise(types, records):
+    """Per reference type: mean and median of the final best over runs x
+    tasks of that type; and the ANO curve of all records."""
+    types = np.asarray(types)
+    final = records[:, :, -2]
+    per_type = {}
+    for rt in sorted(set(types.tolist())):
+        v = final[:, types == rt].astype(np.float64)
+        per_type[int(rt)] = {"mean": float(v.mean()), "median": float(np.median(v)),
+                             "tasks": int((types == rt).sum())}
+    return {"per_type": per_type, "ano": [float(x) for x in ano(records)]}

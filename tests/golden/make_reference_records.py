@@ -1,8 +1,15 @@
-"""Builds tests/golden/reference_records_T100.json from the reference's own
-recorded GA runs, data process/ANO_Tnum/data_record_T_ANO_100.txt (18 runs x
-100 tasks x 22 columns: best fitness at generations 0, 50, ..., 1000, then
-the 481st-best member of the initial population; writer commented at
-proposed model/SG-EMTF.cu:2015-2026).
+"""Builds the fixtures of the reference's own recorded GA runs,
+data process/ANO_Tnum/data_record_T_ANO_100.txt (18 runs x 100 tasks x 22
+columns: best fitness at generations 0, 50, ..., 1000, then the 481st-best
+member of the initial population; writer commented at proposed
+model/SG-EMTF.cu:2015-2026):
+  reference_records_T100.json       the initial and final columns, by type
+  reference_trajectories_T100.npy   every column, float32 [18, 100, 22]
+  reference_ano_T100.json           the ANO curve the reference's tool
+                                    (data process/源.cpp:122-209) computed
+                                    from those runs, as it printed it
+                                    (data process/ANO_Tnum/
+                                    data_record_T_ANO_100_1677482963.txt)
 
 The task -> function map is the reference's: glibc srand(0); rand() % 7 per
 task with task 0 forced to type 6 (SG-EMTF.cu:307-313).  Reference types are
@@ -16,8 +23,12 @@ import ctypes
 import json
 import os
 
+import numpy as np
+
 SRC = "/root/reference/data process/ANO_Tnum/data_record_T_ANO_100.txt"
-OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_records_T100.json")
+SRC_ANO = "/root/reference/data process/ANO_Tnum/data_record_T_ANO_100_1677482963.txt"
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "reference_records_T100.json")
 
 
 def reference_types(n):
@@ -49,7 +60,12 @@ def main():
     }
     with open(OUT, "w") as f:
         json.dump(out, f, separators=(",", ":"))
-    print(OUT, len(runs), "runs")
+    np.save(os.path.join(HERE, "reference_trajectories_T100.npy"), np.array(runs, np.float32))
+    ano = [v.strip() for v in open(SRC_ANO).read().split(",") if v.strip()]
+    with open(os.path.join(HERE, "reference_ano_T100.json"), "w") as f:
+        json.dump({"source": "data process/ANO_Tnum/data_record_T_ANO_100_1677482963.txt",
+                   "ano": ano}, f, indent=0)
+    print(OUT, len(runs), "runs;", len(ano), "ANO points")
 
 
 if __name__ == "__main__":
