@@ -32,6 +32,11 @@ Workload (one "step" = one full optimisation run of every task):
   capacity 50, islands of 128, order crossover + swap + 2-opt, exact int32
   split, elite transfer every 20 generations; a step = 500 generations).
 
+--workload quality: the statistical harness (sg-emtf_gb300/sgemtf/quality.py):
+  --seeds runs (default 30) of the reference's recorded GA setting, 100 tasks,
+  D = 50, 1000 generations recorded every 50, beside the reference's 18
+  recorded runs (per function type mean/median best, ANO curves).
+
 Multi-GPU: tasks are independent between transfers, so each rank runs its own
 batch of tasks (weak scaling, no data-path collective); the timed region is
 bracketed by a barrier and the max over ranks is reported.
