@@ -409,6 +409,67 @@ EMT_API int emt_write_fitness(emt_handle_t* h, const char* path);
  * rotation is not diagonal have no such form: EMT_ERR_UNSUPPORTED. */
 EMT_API int emt_write_para(emt_handle_t* h, const char* path);
 
+/* ---- service mode (emt_service.cpp) ----
+ *
+ * Tasks arrive in batches over time and are served concurrently, the
+ * reference's host scheduler (SG-EMTF.cu:1836-1958: T tasks split into
+ * BATCH_NUM batches that arrive after random gaps, one host thread per task,
+ * average response and solve times, memory use).  Here an admitted batch is
+ * one handle on its own CUDA stream, created with seed = config seed + batch
+ * number; each round of emt_service_step launches the next epoch of every
+ * running batch whose previous epoch has finished, so batches overlap on the
+ * device, and retires batches that have run the service's generation
+ * budget.  A batch's results equal those of a standalone handle with the
+ * same configuration, seed and tasks.  Times are milliseconds on the
+ * service's steady clock, which starts at emt_service_create.  Islands of
+ * D <= 128 (the fused kernel). */
+typedef struct emt_service emt_service_t;
+
+typedef struct emt_service_batch_info {
+  int32_t n_tasks;
+  int32_t state;        /* 0 waiting for its arrival time, 1 running, 2 done */
+  int32_t generations;  /* generations completed                            */
+  int32_t reserved;
+  double arrival_ms;    /* as submitted                                      */
+  double admit_ms;      /* its handle created and its first launch queued    */
+  double done_ms;       /* its last epoch seen complete                      */
+} emt_service_batch_info;
+
+typedef struct emt_service_stats {
+  int32_t batches_submitted, batches_done;
+  int64_t tasks_done;
+  double mean_response_ms;    /* admit - arrival, averaged over finished tasks */
+  double mean_solve_ms;       /* done - arrival, averaged over finished tasks  */
+  double max_device_mem_mb;   /* device memory in use (cudaMemGetInfo), the
+                                 largest sample, one sample per round        */
+  double mean_device_mem_mb;  /* and the mean over rounds                    */
+  uint64_t evaluations;       /* over finished batches                        */
+  int32_t rounds;
+  int32_t reserved;
+} emt_service_stats;
+
+/* generations: budget per batch; epoch: generations per launch (> 0). */
+EMT_API int emt_service_create(const emt_config* cfg, int32_t generations, int32_t epoch,
+                               emt_service_t** out);
+/* Queues a batch that arrives at arrival_ms (0 or a past time: at once);
+ * the task descriptors are copied.  *batch receives its number. */
+EMT_API int emt_service_submit(emt_service_t* s, int32_t n, const emt_task_desc* tasks,
+                               double arrival_ms, int32_t* batch);
+/* One round: admit arrived batches, launch ready epochs, retire finished
+ * batches.  *active (optional) receives the batches still waiting or
+ * running. */
+EMT_API int emt_service_step(emt_service_t* s, int32_t* active);
+/* Rounds until every submitted batch is done; sleeps until the next arrival
+ * when nothing runs. */
+EMT_API int emt_service_drain(emt_service_t* s);
+/* A batch's times and state; best (n_tasks floats, optional) receives each
+ * task's best FP32 fitness once the batch is done. */
+EMT_API int emt_service_batch(emt_service_t* s, int32_t batch, emt_service_batch_info* info,
+                              float* best);
+EMT_API int emt_service_get_stats(emt_service_t* s, emt_service_stats* out);
+EMT_API const char* emt_service_last_error(const emt_service_t* s);
+EMT_API void emt_service_destroy(emt_service_t* s);
+
 EMT_API const char* emt_last_error(const emt_handle_t* h);
 EMT_API const char* emt_status_string(int status);
 EMT_API void emt_destroy(emt_handle_t* h);

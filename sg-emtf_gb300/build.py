@@ -18,7 +18,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libsgemtf.so")
-SOURCES = ["emt_kernels.cu", "emt_api.cu", "emt_cvrp.cu", "emt_records.cpp"]
+SOURCES = ["emt_kernels.cu", "emt_api.cu", "emt_cvrp.cu", "emt_records.cpp", "emt_service.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
          "-Xcompiler", "-fvisibility=hidden", "-I", os.path.join(ROOT, "include")]

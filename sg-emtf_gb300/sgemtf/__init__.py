@@ -44,6 +44,9 @@ EXPORTED = [
     "emt_get_population", "emt_set_population", "emt_get_task_info", "emt_get_task_params",
     "emt_evaluate", "emt_get_stats", "emt_snapshot_size", "emt_snapshot", "emt_restore",
     "emt_record_run", "emt_write_record", "emt_ano", "emt_write_fitness", "emt_write_para",
+    "emt_service_create", "emt_service_submit", "emt_service_step", "emt_service_drain",
+    "emt_service_batch", "emt_service_get_stats", "emt_service_last_error",
+    "emt_service_destroy",
     "emt_last_error", "emt_status_string", "emt_destroy",
     "emt_cvrp_config_default", "emt_cvrp_create", "emt_cvrp_add_instances", "emt_cvrp_reset",
     "emt_cvrp_run", "emt_cvrp_sync", "emt_cvrp_get_best_all", "emt_cvrp_get_population",
@@ -109,6 +112,21 @@ class TaskDesc:
         return TaskDescC(self.function, self.dim, self.pop, self.lo, self.hi, self.rotation,
                          ptr(self.rotation_matrix, ctypes.c_double), ptr(self.diag, ctypes.c_float),
                          ptr(self.shift, ctypes.c_float))
+
+
+class ServiceBatchInfo(ctypes.Structure):
+    _fields_ = [("n_tasks", ctypes.c_int32), ("state", ctypes.c_int32),
+                ("generations", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("arrival_ms", ctypes.c_double), ("admit_ms", ctypes.c_double),
+                ("done_ms", ctypes.c_double)]
+
+
+class ServiceStats(ctypes.Structure):
+    _fields_ = [("batches_submitted", ctypes.c_int32), ("batches_done", ctypes.c_int32),
+                ("tasks_done", ctypes.c_int64), ("mean_response_ms", ctypes.c_double),
+                ("mean_solve_ms", ctypes.c_double), ("max_device_mem_mb", ctypes.c_double),
+                ("mean_device_mem_mb", ctypes.c_double), ("evaluations", ctypes.c_uint64),
+                ("rounds", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class CvrpConfig(ctypes.Structure):
@@ -178,6 +196,17 @@ def lib():
         L.emt_ano.argtypes = [i32, i32, i32, f32p, f32p]
         L.emt_write_fitness.argtypes = [vp, ctypes.c_char_p]
         L.emt_write_para.argtypes = [vp, ctypes.c_char_p]
+        L.emt_service_create.argtypes = [ctypes.POINTER(Config), i32, i32, ctypes.POINTER(vp)]
+        L.emt_service_submit.argtypes = [vp, i32, ctypes.POINTER(TaskDescC), ctypes.c_double,
+                                         ctypes.POINTER(i32)]
+        L.emt_service_step.argtypes = [vp, ctypes.POINTER(i32)]
+        L.emt_service_drain.argtypes = [vp]
+        L.emt_service_batch.argtypes = [vp, i32, ctypes.POINTER(ServiceBatchInfo), f32p]
+        L.emt_service_get_stats.argtypes = [vp, ctypes.POINTER(ServiceStats)]
+        L.emt_service_last_error.argtypes = [vp]
+        L.emt_service_last_error.restype = ctypes.c_char_p
+        L.emt_service_destroy.argtypes = [vp]
+        L.emt_service_destroy.restype = None
         L.emt_evaluate.argtypes = [vp, i32, i32, f32p, f32p, f32p]
         L.emt_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
         L.emt_snapshot_size.argtypes = [vp, ctypes.POINTER(ctypes.c_size_t)]
@@ -397,6 +426,67 @@ class Engine:
 
     def __exit__(self, *a):
         self.close()
+
+
+class Service:
+    """Service mode (emt_service_*): batches of tasks that arrive over time,
+    each served by its own handle and stream, concurrently on one GPU."""
+
+    def __init__(self, config=None, generations=1000, epoch=50):
+        self.config = config or Config()
+        self._s = ctypes.c_void_p()
+        self._tasks = {}
+        rc = lib().emt_service_create(ctypes.byref(self.config), generations, epoch,
+                                      ctypes.byref(self._s))
+        if rc:
+            raise EngineError(rc, "emt_service_create: %s" % status_string(rc))
+
+    def _check(self, rc, what):
+        if rc:
+            raise EngineError(rc, "%s: %s" % (what, lib().emt_service_last_error(self._s).decode()))
+
+    def submit(self, tasks, arrival_ms=0.0):
+        arr = (TaskDescC * len(tasks))(*[t.c() for t in tasks])
+        b = ctypes.c_int32()
+        self._check(lib().emt_service_submit(self._s, len(tasks), arr, float(arrival_ms),
+                                             ctypes.byref(b)), "emt_service_submit")
+        self._tasks[b.value] = len(tasks)
+        return b.value
+
+    def step(self):
+        left = ctypes.c_int32()
+        self._check(lib().emt_service_step(self._s, ctypes.byref(left)), "emt_service_step")
+        return left.value
+
+    def drain(self):
+        self._check(lib().emt_service_drain(self._s), "emt_service_drain")
+
+    def batch(self, b):
+        info = ServiceBatchInfo()
+        self._check(lib().emt_service_batch(self._s, b, ctypes.byref(info), None),
+                    "emt_service_batch")
+        d = {k: getattr(info, k) for k, _ in ServiceBatchInfo._fields_ if k != "reserved"}
+        best = None
+        if info.state == 2:
+            best = np.zeros(info.n_tasks, np.float32)
+            self._check(lib().emt_service_batch(self._s, b, None, _f32(best)), "emt_service_batch")
+        return d, best
+
+    def stats(self):
+        st = ServiceStats()
+        self._check(lib().emt_service_get_stats(self._s, ctypes.byref(st)), "emt_service_get_stats")
+        return {k: getattr(st, k) for k, _ in ServiceStats._fields_ if k != "reserved"}
+
+    def close(self):
+        if self._s:
+            lib().emt_service_destroy(self._s)
+            self._s = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class CvrpEngine:
