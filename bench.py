@@ -37,6 +37,10 @@ Workload (one "step" = one full optimisation run of every task):
   D = 50, 1000 generations recorded every 50, beside the reference's 18
   recorded runs (per function type mean/median best, ANO curves).
 
+--workload service: service mode (emt_service_*): 10000 tasks in 100 batches
+  arriving after seeded U(0, 100) ms gaps, 1000 generations each; mean
+  response and solve times, device memory, whole-run evals/s.
+
 Multi-GPU: tasks are independent between transfers, so each rank runs its own
 batch of tasks (weak scaling, no data-path collective); the timed region is
 bracketed by a barrier and the max over ranks is reported.
@@ -73,7 +77,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--workload", default="continuous",
-                   choices=["continuous", "cvrp", "uneven", "large", "quality"])
+                   choices=["continuous", "cvrp", "uneven", "large", "quality", "service"])
     p.add_argument("--seeds", type=int, default=30)
     return p.parse_args()
 
@@ -685,9 +689,49 @@ def main_quality(args, rank, world, local):
         "data": "synthetic (reference-distributed diagonal instances, seeded)"}))
 
 
+def main_service(args, rank, world, local):
+    """--workload service: the reference's service experiment
+    (proposed model/SG-EMTF.cu:1836-1958): T tasks split at seeded random
+    points into 100 batches that arrive after U(0, 100) ms gaps, each run for
+    the generation budget; mean response and solve times, device memory and
+    whole-run throughput."""
+    if rank != 0:
+        return
+    import sgemtf
+
+    n = 10000 if args.tasks == TASKS else args.tasks
+    gens = 1000 if args.gens == GENS else args.gens
+    batches = 100
+    rng = np.random.default_rng(7)
+    cuts = np.sort(rng.choice(np.arange(1, n), batches - 1, replace=False))
+    bounds = [0] + cuts.tolist() + [n]
+    gaps = rng.uniform(0.0, 100.0, batches)
+    arrival = np.concatenate([[0.0], np.cumsum(gaps)[:-1]])
+    svc = sgemtf.Service(sgemtf.Config(seed=1, device=local), generations=gens, epoch=50)
+    for i in range(batches):
+        svc.submit([sgemtf.TaskDesc(t % 7, DIM, POP) for t in range(bounds[i], bounds[i + 1])],
+                   arrival_ms=float(arrival[i]))
+    t0 = time.perf_counter()
+    svc.drain()
+    wall = time.perf_counter() - t0
+    st = svc.stats()
+    svc.close()
+    print(json.dumps({
+        "metric": "service mode: %d tasks in %d batches arriving over %.0f ms, %d generations "
+                  "each (D=%d, NP=%d, DE/rand/1/bin)" % (n, batches, arrival[-1], gens, DIM, POP),
+        "workload": "service", "value": st["evaluations"] / wall, "unit": "evals/s",
+        "mean_response_ms": st["mean_response_ms"], "mean_solve_ms": st["mean_solve_ms"],
+        "max_device_mem_mb": st["max_device_mem_mb"], "mean_device_mem_mb": st["mean_device_mem_mb"],
+        "wall_s": wall, "evaluations": st["evaluations"], "rounds": st["rounds"],
+        "last_arrival_ms": float(arrival[-1]),
+        "data": "synthetic (seeded tasks, seeded-QR rotations, seeded arrival schedule)"}))
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.workload == "service" and args.impl == "ours":
+        return main_service(args, rank, world, local)
     if args.workload == "quality" and args.impl == "ours":
         return main_quality(args, rank, world, local)
     if args.workload == "cvrp" and args.impl == "ours":
