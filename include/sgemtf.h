@@ -78,8 +78,10 @@ typedef enum emt_algorithm {
 /* Arithmetic of the rotation z = Q (x - o) behind every evaluation. */
 typedef enum emt_precision {
   EMT_ROT_FP32 = 0,   /* FP32 FMA on CUDA cores                          */
-  EMT_ROT_TF32X3 = 1, /* tcgen05 tensor cores, hi/lo TF32 split, 3 products,
-                         FP32 accumulation in tensor memory               */
+  EMT_ROT_TF32X3 = 1, /* tcgen05 tensor cores, hi/lo TF32 split of both
+                         operands, FP32 accumulation in tensor memory: 3
+                         products for islands of D <= 128; for larger ones
+                         both lo parts rounded to TF32 and all 4 products */
   EMT_ROT_AUTO = 2    /* the fastest form the device supports            */
 } emt_precision;
 

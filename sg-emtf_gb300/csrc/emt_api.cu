@@ -351,7 +351,7 @@ int large_upload(emt_handle* h, int64_t pop, int32_t fit) {
         const float v = ht.Q[(size_t)r * ht.D + c];
         const float vh = tf32_hi(v);
         hi[(size_t)r * h->lKp + c] = vh;
-        lo[(size_t)r * h->lKp + c] = v - vh;
+        lo[(size_t)r * h->lKp + c] = tf32_hi(v - vh);  // rounded, as the S planes are
       }
     if ((e = cudaMemcpy(h->d_qbig.p + (size_t)t * per, hi.data(), sizeof(float) * per, cudaMemcpyHostToDevice)) ||
         (e = cudaMemcpy(h->d_qbig.p + plane + (size_t)t * per, lo.data(), sizeof(float) * per, cudaMemcpyHostToDevice)))

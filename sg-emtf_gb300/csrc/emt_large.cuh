@@ -6,8 +6,8 @@
 //   build   trial genes (DE or GA, the same arithmetic and Philox stream as
 //           the fused kernel) and the rotation operand s = u - o, split into
 //           TF32 hi/lo planes for the tensor-core form;
-//   gemm    Z = S Q^T for every task: tcgen05.mma kind::tf32 (3 products,
-//           hi*hi + hi*lo + lo*hi, FP32 accumulation in tensor memory), 128 x
+//   gemm    Z = S Q^T for every task: tcgen05.mma kind::tf32 (4 products of
+//           the rounded hi/lo pairs, FP32 accumulation in tensor memory), 128 x
 //           256 tiles fed by TMA (128B swizzle) through a 2-stage mbarrier
 //           pipeline; or FP32 CUDA-core tiles (128 x 128, 8 x 8 per thread);
 //   eval    one warp per row: f and its rounding window from the Z row;
@@ -49,13 +49,16 @@ __device__ __forceinline__ int transfer_partner(const LargeArgs& a, int t, uint3
   return (int)p;
 }
 
-// Operand row of s = v - o: FP32 (FP32 form) or TF32 hi/lo planes.
+// Operand row of s = v - o: FP32 (FP32 form) or TF32 hi/lo planes, both
+// rounded to nearest TF32 (v = hi + lo + r, |r| <= 2^-24 |v|, unbiased; the
+// tensor core would otherwise truncate lo, and over K = 1000 products that
+// bias reaches 1e-5 of the fitness scale).
 __device__ __forceinline__ void put_s(const LargeArgs& a, int64_t row, int j, float v) {
   float* p = a.S + row * a.Kp + j;
   if (a.tc) {
     const float hi = tc::tf32_round(v);
     p[0] = hi;
-    p[a.split] = v - hi;
+    p[a.split] = tc::tf32_round(v - hi);
   } else {
     p[0] = v;
   }
@@ -343,7 +346,8 @@ __global__ void __launch_bounds__(192, 1)
     tc::mbar_init(done, 1);
     ctl[0] = ctl[1] = ctl[2] = 0;
   }
-  if (warp == 1) tc::tmem_alloc(tslot, kLargeBN);
+  // two accumulators of kLargeBN columns: hi.hi, and the three small products
+  if (warp == 1) tc::tmem_alloc(tslot, 2 * kLargeBN);
   tc::fence_before();
   __syncthreads();
   tc::fence_after();
@@ -377,12 +381,18 @@ __global__ void __launch_bounds__(192, 1)
       }
       tc::fence_after();
       const uint32_t st = sbase + s * kStageBytes;
-      const uint32_t pa[3] = {0u, 0u, kTileA}, pb[3] = {0u, kTileB, 0u};
-      for (int p = 0; p < 3; ++p)
+      // all four products of the hi/lo pairs.  Each MMA step loses about
+      // 2^-24 of its accumulator's magnitude (measured: with the four products
+      // in one accumulator |f - f64| reached 1.3e-5 of the scale at K = 1000),
+      // so hi.hi accumulates alone and hi.lo + lo.hi + lo.lo, 2^-11 smaller,
+      // in the second accumulator; the epilogue adds the two in FP32.
+      const uint32_t pa[4] = {0u, 0u, kTileA, kTileA}, pb[4] = {0u, kTileB, 0u, kTileB};
+      for (int p = 0; p < 4; ++p)
         for (int ks = 0; ks < 4; ++ks) {
           const uint64_t ad = tc::sdesc_sw128(st + pa[p] + 32u * ks);
           const uint64_t bd = tc::sdesc_sw128(st + 2 * kTileA + pb[p] + 32u * ks);
-          tc::mma_tf32(tmem, ad, bd, idesc, (kb | p | ks) ? 1u : 0u);
+          const uint32_t acc = p == 0 ? ((kb | ks) ? 1u : 0u) : ((kb | (p - 1) | ks) ? 1u : 0u);
+          tc::mma_tf32(tmem + (p ? (uint32_t)kLargeBN : 0u), ad, bd, idesc, acc);
         }
       tc::mma_commit(empty0 + 8 * s);
       ctl[2] = kb + 1;
@@ -397,8 +407,11 @@ __global__ void __launch_bounds__(192, 1)
     if (ok) {
       float* zr = a.Z + (a.srow[task] + row) * (int64_t)a.Nq + n0;
       for (int c0 = 0; c0 < kLargeBN; c0 += 16) {
-        float v[16];
+        float v[16], w[16];
         tc::tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, v);
+        tc::tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(kLargeBN + c0), w);
+#pragma unroll
+        for (int g = 0; g < 16; ++g) v[g] = __fadd_rn(v[g], w[g]);
         if (row < td.NP)
 #pragma unroll
           for (int g = 0; g < 4; ++g)
@@ -419,7 +432,7 @@ __global__ void __launch_bounds__(192, 1)
   }
   if (warp == 1) {
     tc::fence_after();
-    tc::tmem_dealloc(tmem, kLargeBN);
+    tc::tmem_dealloc(tmem, 2 * kLargeBN);
   }
 }
 
@@ -651,7 +664,11 @@ __device__ __forceinline__ int sel_target(const LargeArgs& a, const TaskDev& td,
   return mode == SEL_IMPORT ? a.rank[td.fit_off + td.NP - k + c] : c;
 }
 
-constexpr int kPairs = 2;           // near ties per re-check work item
+// near ties per re-check work item: one keeps the item's scratch at 32 KB
+// (D = 1000), so five CTAs share an SM and hide the latency of the Q stream;
+// two or four per item share each Q load but cost occupancy (config 4 step:
+// 1.84 s with one, 1.91 s with two, 3.35 s with four)
+constexpr int kPairs = 1;
 constexpr int kJobs = 2 * kPairs;   // rotations per item (trial and parent)
 
 __global__ void __launch_bounds__(256) classify_kernel(const LargeArgs a, int mode) {

@@ -57,6 +57,25 @@ def test_large_fitness_within_window(sgemtf, orc, precision):
 
 
 @pytest.mark.parametrize("precision", [0, 1])
+def test_large_fitness_within_window_d1000(sgemtf, orc, precision):
+    """The stated 1e-5 of the scale at D = 1000, where the tensor-core form's
+    FP32 accumulation runs over 128 K-steps (Weierstrass: its own window)."""
+    specs = [(f, 1000, 32, 1) for f in (0, 3, 4, 6)]
+    try:
+        eng, tasks = make_engine(sgemtf, orc, specs, seed=5, precision=precision)
+    except sgemtf.EngineError as e:
+        pytest.skip(str(e))
+    eng.reset()
+    for i, t in enumerate(tasks):
+        X, f = eng.population(i)
+        for r in range(0, t.NP, 2):
+            f64, scale, _ = t.eval64(X[r])
+            lim = 5e-5 * scale if t.c.fid == orc.WEIERSTRASS else 1e-5 * scale
+            assert abs(float(f[r]) - f64) <= lim, (precision, i, r, abs(float(f[r]) - f64) / scale)
+    eng.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
 def test_large_transfer_epochs(sgemtf, orc, precision):
     specs = [(0, 150, 16, 1), (1, 150, 16, 1), (6, 140, 12, 1), (2, 200, 20, 1)]
     interval = 3
