@@ -33,7 +33,8 @@ struct HostTask {
   std::vector<float> Q;  // D*D row-major, the operator the device applies
   std::vector<float> o;  // D
   float woff = 0.f, qnorm = 1.f;
-  uint32_t qr_id = 0;  // task id whose seeded rotation is still to be generated
+  uint32_t qr_id = UINT32_MAX;    // task id whose seeded rotation is still to be generated
+  const double* dense = nullptr;  // caller's FP64 matrix still to be checked and converted
   double woff64 = 0.0;
 };
 
@@ -928,7 +929,6 @@ int emt_add_tasks(emt_handle_t* h, int32_t n, const emt_task_desc* td) {
   if (n < 0 || (n > 0 && !td)) return h->fail(EMT_ERR_INVALID_ARG, "bad task array");
   const int smem_cap = max_smem_optin(h->device);
   std::vector<HostTask> add;
-  std::vector<int> qr_pending;
   add.reserve(n);
   for (int i = 0; i < n; ++i) {
     const emt_task_desc& d = td[i];
@@ -970,15 +970,11 @@ int emt_add_tasks(emt_handle_t* h, int32_t n, const emt_task_desc* td) {
         for (int k = 0; k < D; ++k) ht.Q[(size_t)k * D + k] = 1.f;
         break;
       case EMT_ROTATION_SEEDED_QR:
-        qr_pending.push_back((int)add.size());  // generated below, in parallel
         ht.qr_id = id;
         break;
       case EMT_ROTATION_DENSE:
         if (!d.rotation_matrix) return h->fail(EMT_ERR_INVALID_ARG, "dense rotation without matrix");
-        for (size_t k = 0; k < (size_t)D * D; ++k) {
-          if (!std::isfinite(d.rotation_matrix[k])) return h->fail(EMT_ERR_INVALID_ARG, "non-finite rotation");
-          ht.Q[k] = (float)d.rotation_matrix[k];
-        }
+        ht.dense = d.rotation_matrix;  // checked and converted below, in parallel
         break;
       case EMT_ROTATION_DIAG:
         if (!d.diag) return h->fail(EMT_ERR_INVALID_ARG, "diagonal rotation without factors");
@@ -1004,23 +1000,26 @@ int emt_add_tasks(emt_handle_t* h, int32_t n, const emt_task_desc* td) {
     ht.woff = (float)ht.woff64;
     add.push_back(std::move(ht));
   }
-  // seeded rotations (an O(D^3) FP64 QR each) on all host cores
-  if (!qr_pending.empty()) {
-    const int nth = (int)std::min<size_t>(qr_pending.size(), std::max(1u, std::thread::hardware_concurrency()));
-    std::vector<std::thread> pool;
-    for (int w = 0; w < nth; ++w)
-      pool.emplace_back([&, w] {
-        std::vector<double> Q;
-        for (size_t k = w; k < qr_pending.size(); k += nth) {
-          HostTask& ht = add[qr_pending[k]];
-          seeded_rotation(h->cfg.seed, ht.qr_id, ht.D, Q);
-          for (size_t e = 0; e < Q.size(); ++e) ht.Q[e] = (float)Q[e];
-        }
-      });
-    for (auto& th : pool) th.join();
-  }
-  for (auto& ht : add) {
+  // the O(D^2) and O(D^3) work per task on all host cores: seeded rotations
+  // (an FP64 QR each), caller matrices (checked finite, rounded to FP32) and
+  // every rotation's largest row norm
+  std::vector<char> bad(add.size(), 0);
+  auto finish = [&](size_t i, std::vector<double>& Q) {
+    HostTask& ht = add[i];
     const int D = ht.D;
+    if (ht.qr_id != UINT32_MAX) {
+      seeded_rotation(h->cfg.seed, ht.qr_id, D, Q);
+      for (size_t e = 0; e < Q.size(); ++e) ht.Q[e] = (float)Q[e];
+    } else if (ht.dense) {
+      for (size_t k = 0; k < (size_t)D * D; ++k) {
+        if (!std::isfinite(ht.dense[k])) {
+          bad[i] = 1;
+          return;
+        }
+        ht.Q[k] = (float)ht.dense[k];
+      }
+    }
+    ht.dense = nullptr;
     double qn = 0.0;
     for (int r = 0; r < D; ++r) {
       double s = 0.0;
@@ -1028,7 +1027,26 @@ int emt_add_tasks(emt_handle_t* h, int32_t n, const emt_task_desc* td) {
       qn = std::max(qn, std::sqrt(s));
     }
     ht.qnorm = (float)qn;
+  };
+  size_t work = 0;
+  for (const auto& ht : add) work += (size_t)ht.D * ht.D * (ht.qr_id != UINT32_MAX ? ht.D : 1);
+  const int nth = work < 200000 ? 1
+                              : (int)std::min<size_t>(add.size(),
+                                                      std::max(1u, std::thread::hardware_concurrency()));
+  if (nth <= 1) {
+    std::vector<double> Q;
+    for (size_t i = 0; i < add.size(); ++i) finish(i, Q);
+  } else {
+    std::vector<std::thread> pool;
+    for (int w = 0; w < nth; ++w)
+      pool.emplace_back([&, w] {
+        std::vector<double> Q;
+        for (size_t i = w; i < add.size(); i += nth) finish(i, Q);
+      });
+    for (auto& th : pool) th.join();
   }
+  for (size_t i = 0; i < add.size(); ++i)
+    if (bad[i]) return h->fail(EMT_ERR_INVALID_ARG, "task " + std::to_string(i) + ": non-finite rotation");
   for (auto& t : add) h->tasks.push_back(std::move(t));
   h->uploaded = false;
   h->initialized = false;

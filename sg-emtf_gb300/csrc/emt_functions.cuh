@@ -602,6 +602,15 @@ __device__ double eval_tier2(const FnConst& fc, const double* zbuf, double* err)
   return f;
 }
 
+// |f32 - f64| / scale of one member, as BestArgs::best_err defines it: the
+// scale the FP32 evaluation stated, tol / rel (Weierstrass: 2D + |offset|).
+__device__ __forceinline__ float best_rel_err(const TaskDev& td, float f32, double f64, float tol,
+                                              float rel) {
+  const double scale = td.fid == F_WEIERSTRASS ? 2.0 * td.D + fabs((double)td.woff)
+                                               : (double)tol / (double)rel;
+  return scale > 0.0 ? (float)(fabs((double)f32 - f64) / scale) : 0.f;
+}
+
 // Weierstrass from the FP64-class rotation: exactly reduced terms (FP32/INT).
 __device__ double eval_weier_precise(const FnConst& fc, const double* zbuf) {
   const int lane = threadIdx.x & 31;

@@ -276,14 +276,6 @@ struct BestArgs {
   float* best_err;
 };
 
-// |f32 - f64| / scale of one member, as BestArgs::best_err defines it.
-EMT_HD float best_rel_err(const TaskDev& td, float f32, double f64, float tol, float rel) {
-  const bool weierstrass = td.fid == 6;
-  const double scale = weierstrass ? 2.0 * td.D + (td.woff < 0.f ? -(double)td.woff : (double)td.woff)
-                                   : (double)tol / (double)rel;
-  const double d = (double)f32 - f64;
-  return scale > 0.0 ? (float)((d < 0.0 ? -d : d) / scale) : 0.f;
-}
 
 }  // namespace emt
 

@@ -95,7 +95,8 @@ class Stats(ctypes.Structure):
 
 
 class TaskDesc:
-    """One task; arrays are kept alive here until add_tasks copies them."""
+    """One task; arrays are kept alive here until add_tasks copies them.  The
+    fields are fixed at construction (the C descriptor is built once)."""
 
     def __init__(self, function, dim, pop, lo=0.0, hi=0.0, rotation=ROTATION_SEEDED_QR,
                  rotation_matrix=None, diag=None, shift=None):
@@ -106,12 +107,14 @@ class TaskDesc:
         self.diag = None if diag is None else np.ascontiguousarray(diag, np.float32)
         self.shift = None if shift is None else np.ascontiguousarray(shift, np.float32)
 
-    def c(self):
         def ptr(a, t):
             return None if a is None else a.ctypes.data_as(ctypes.POINTER(t))
-        return TaskDescC(self.function, self.dim, self.pop, self.lo, self.hi, self.rotation,
-                         ptr(self.rotation_matrix, ctypes.c_double), ptr(self.diag, ctypes.c_float),
-                         ptr(self.shift, ctypes.c_float))
+        self._c = TaskDescC(self.function, self.dim, self.pop, self.lo, self.hi, self.rotation,
+                            ptr(self.rotation_matrix, ctypes.c_double),
+                            ptr(self.diag, ctypes.c_float), ptr(self.shift, ctypes.c_float))
+
+    def c(self):
+        return self._c
 
 
 class ServiceBatchInfo(ctypes.Structure):
@@ -293,7 +296,8 @@ class Engine:
 
     def add_tasks(self, descs):
         descs = list(descs)
-        arr = (TaskDescC * len(descs))(*[d.c() for d in descs])
+        arr = (TaskDescC * len(descs)).from_buffer_copy(b"".join(bytes(d.c()) for d in descs)) \
+            if descs else (TaskDescC * 0)()
         self._check(lib().emt_add_tasks(self._h, len(descs), arr), "emt_add_tasks")
         self.tasks.extend(descs)
 
