@@ -148,7 +148,7 @@ typedef struct emt_config {
    * generation g, when g > 1 and (g - 1) % migration_interval == 0, the r-th
    * best of group s replaces the r-th worst of group s + 1 (mod subislands),
    * r < migration_count, when strictly better, all from the pre-migration
-   * state; near ties are decided like any selection.  Islands of D <= 128. */
+   * state; near ties are decided like any selection. */
   int32_t subislands;
   int32_t migration_interval; /* generations between migrations; 0 = none       */
   int32_t migration_count;    /* members each group sends; 0 = NP/subislands/8,

@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <new>
 #include <numeric>
@@ -438,11 +439,15 @@ int upload(emt_handle* h) {
   if (e0 != cudaSuccess) return h->cuda_fail(e0, "cudaSetDevice");
   h->task_smem.assign(n, 0);
   std::vector<int> occ(n, 1);
+  std::map<size_t, int> occ_of;  // one occupancy query per distinct shared-memory size
   for (int t = 0; t < n && !h->large; ++t) {
     const HostTask& ht = h->tasks[t];
     h->task_smem[t] = h->use_tc ? emt::tc_layout(ht.D, ht.NP, h->tc_np, h->tc_kp).total
                                 : emt::smem_layout(ht.D, ht.NP, h->table[t].qt_in_smem != 0).total;
-    occ[t] = emt_epoch_occupancy(h->use_tc, h->task_smem[t]);
+    auto it = occ_of.find(h->task_smem[t]);
+    if (it == occ_of.end())
+      it = occ_of.emplace(h->task_smem[t], emt_epoch_occupancy(h->use_tc, h->task_smem[t])).first;
+    occ[t] = it->second;
     if (occ[t] <= 0) return h->fail(EMT_ERR_UNSUPPORTED, "an island does not fit on an SM");
   }
   std::vector<int32_t> border(h->order);
@@ -688,6 +693,9 @@ emt::LargeArgs large_args(emt_handle* h) {
   a.stats = h->d_stats.p;
   a.err = h->d_err.p;
   a.select_smem = h->lsel_smem;
+  a.subislands = h->cfg.subislands > 1 ? h->cfg.subislands : 1;
+  a.mig_interval = h->cfg.migration_interval;
+  a.mig_count = h->cfg.migration_count;
   return a;
 }
 
@@ -723,7 +731,17 @@ int large_epoch(emt_handle* h, int gens, int imp, int exp, int parity, cudaStrea
     if (!e) e = emt_large_eval(a, 1, emt::kMaxPop, stream);
     if (!e) e = emt_large_selection(a, emt::large::SEL_IMPORT, h->ldp, h->lgrid, stream);
   }
-  for (int g = 0; g < gens && !e; ++g) e = large_generation(h, a, stream);
+  const bool migrate = a.subislands > 1 && a.mig_interval > 0;
+  for (int g = 0; g < gens && !e; ++g) {
+    // ring migration before the trials when the generation calls for it; the
+    // kernels decide that from each task's counter, so a replayed graph of
+    // this sequence stays right whatever generation it starts at
+    if (migrate) {
+      e = emt_large_select(a, emt::large::SEL_MIGRATE, stream);
+      if (!e) e = emt_large_selection(a, emt::large::SEL_MIGRATE, h->ldp, h->lgrid, stream);
+    }
+    if (!e) e = large_generation(h, a, stream);
+  }
   if (!e && exp) e = emt_large_select(a, emt::large::SEL_EXPORT, stream);
   return e;
 }
@@ -946,9 +964,6 @@ int emt_add_tasks(emt_handle_t* h, int32_t n, const emt_task_desc* td) {
         return h->fail(EMT_ERR_INVALID_ARG, "task " + std::to_string(i) +
                                                 ": pop must split into sub-islands of >= 4 "
                                                 "members, each sending at most half");
-      if (d.dim > emt::kMaxDim)
-        return h->fail(EMT_ERR_UNSUPPORTED, "task " + std::to_string(i) +
-                                                ": sub-islands serve islands of D <= 128");
     }
     if (d.dim <= emt::kMaxDim && (size_t)smem_cap < emt::smem_layout(d.dim, d.pop, false).total)
       return h->fail(EMT_ERR_UNSUPPORTED, "task " + std::to_string(i) +

@@ -127,11 +127,17 @@ struct LargeArgs {
   unsigned long long* stats;
   int32_t* err;
   size_t select_smem;    // dynamic shared memory of the selection kernel
+  int32_t subislands, mig_interval, mig_count;  // sub-islands per island (1 = none)
 };
 
 namespace large {
 enum BuildMode : int { BUILD_X = 0, BUILD_TRIALS = 1, BUILD_CANDIDATES = 2 };
-enum SelectMode : int { SEL_GENERATION = 0, SEL_IMPORT = 1, SEL_EXPORT = 2, SEL_RANK = 3 };
+// SEL_MIGRATE: the select kernel prepares the migrants (trial rows, their
+// fitness, targets in the rank buffer); the selection pipeline then decides
+// them strictly, as a transfer import
+enum SelectMode : int {
+  SEL_GENERATION = 0, SEL_IMPORT = 1, SEL_EXPORT = 2, SEL_RANK = 3, SEL_MIGRATE = 4
+};
 }  // namespace large
 
 // Dynamic shared memory of the large-island selection kernel: per-warp

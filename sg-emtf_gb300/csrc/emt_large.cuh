@@ -37,6 +37,18 @@ __device__ __forceinline__ FnConst fn_const(const TaskDev& td, float rel) {
 
 // Transfer partner and candidate count of task t at generation gen0 (the
 // fused kernel's rule); -1 when there is none.
+// migrants each sub-island sends, and whether generation gen[t] + 1 opens
+// with a migration (as the fused kernel's epoch loop decides it)
+__device__ __forceinline__ int migration_count(const LargeArgs& a, int NP) {
+  const int NPs = NP / a.subislands;
+  return a.mig_count > 0 ? a.mig_count : max(1, NPs / 8);
+}
+__device__ __forceinline__ bool migration_due(const LargeArgs& a, int t) {
+  const uint32_t G = a.gen[t] + 1u;
+  return a.subislands > 1 && a.mig_interval > 0 && G > 1u &&
+         (G - 1u) % (uint32_t)a.mig_interval == 0u;
+}
+
 __device__ __forceinline__ int transfer_partner(const LargeArgs& a, int t, uint32_t gen0, int& k) {
   if (a.n_tasks < 2) return -1;
   const U4 w = draw(a.seed, (uint32_t)t, gen0, 0u, P_TRANSFER_PARTNER, 0);
@@ -146,17 +158,19 @@ __global__ void __launch_bounds__(256) build_kernel(const LargeArgs a, int mode)
     }
     return;
   }
-  // ---- trials of generation G ----
+  // ---- trials of generation G (partners from the member's sub-island) ----
   const uint32_t G = gen0 + 1u;
+  const int NPs = NP / a.subislands;
   if (a.algorithm == 0 || a.algorithm == 1) {
     if (threadIdx.x < nrow) {
       const int i = i0 + threadIdx.x;
+      const int base = a.subislands > 1 ? (i / NPs) * NPs : 0;
       const U4 w = draw(a.seed, (uint32_t)task, G, (uint32_t)i, P_DE_INDEX, 0);
       int r1, r2, r3, jr;
-      de_indices(w, i, NP, D, r1, r2, r3, jr);
-      sidx[threadIdx.x][0] = a.algorithm == 0 ? r1 : i;
-      sidx[threadIdx.x][1] = r2;
-      sidx[threadIdx.x][2] = r3;
+      de_indices(w, i - base, NPs, D, r1, r2, r3, jr);
+      sidx[threadIdx.x][0] = a.algorithm == 0 ? base + r1 : i;
+      sidx[threadIdx.x][1] = base + r2;
+      sidx[threadIdx.x][2] = base + r3;
       sidx[threadIdx.x][3] = jr;
     }
     __syncthreads();
@@ -186,12 +200,15 @@ __global__ void __launch_bounds__(256) build_kernel(const LargeArgs a, int mode)
   // mutation -- the fused kernel's build_trials, gene for gene
   if (threadIdx.x < nrow) {
     const int i = i0 + threadIdx.x;
+    const int base = a.subislands > 1 ? (i / NPs) * NPs : 0;
     sidx[threadIdx.x][0] =
-        (int)(draw(a.seed, (uint32_t)task, G, (uint32_t)i, P_GA_PARENT, 0).x % (uint32_t)NP);
+        base + (int)(draw(a.seed, (uint32_t)task, G, (uint32_t)i, P_GA_PARENT, 0).x % (uint32_t)NPs);
     const int pi = i ^ 1;
-    spart[threadIdx.x] = pi < NP ? (int)(draw(a.seed, (uint32_t)task, G, (uint32_t)pi, P_GA_PARENT, 0).x %
-                                         (uint32_t)NP)
-                                 : sidx[threadIdx.x][0];
+    const bool paired = pi < NP && (a.subislands == 1 || pi / NPs == i / NPs);
+    spart[threadIdx.x] =
+        paired ? base + (int)(draw(a.seed, (uint32_t)task, G, (uint32_t)pi, P_GA_PARENT, 0).x %
+                              (uint32_t)NPs)
+               : sidx[threadIdx.x][0];
   }
   __syncthreads();
   const float ec = fdiv(1.f, fadd(a.eta_c, 1.f));
@@ -626,6 +643,36 @@ __global__ void __launch_bounds__(256) select_kernel(const LargeArgs a, int mode
         el[(size_t)c * DP + j] = s.X[(size_t)s.idx[c] * DP + j];
       }
     }
+  } else if (mode == SEL_MIGRATE) {
+    // ring migration between sub-islands (IslandMigration, SG-EMTF.cu:1138-1218),
+    // as the fused kernel's migrate(): rank each sub-island by FP32 fitness,
+    // copy the r-th best of sub-island s to trial row s*m + r with its
+    // fitness, target the r-th worst of s + 1 (the pipeline decides)
+    if (!migration_due(a, task)) return;  // uniform over the CTA
+    const int S = a.subislands, NPs = NP / S, m = migration_count(a, NP), k = S * m;
+    int* rk = s.idx;  // NP ints: member of each within-sub-island rank
+    for (int i = threadIdx.x; i < NP; i += kThreads) {
+      const int base = (i / NPs) * NPs;
+      const float fi = s.fit[i];
+      int r = 0;
+      for (int j = base; j < base + NPs; ++j) {
+        const float fj = s.fit[j];
+        r += (fj < fi || (fj == fi && j < i)) ? 1 : 0;
+      }
+      rk[base + r] = i;
+    }
+    __syncthreads();
+    for (int it = threadIdx.x; it < k * DP; it += kThreads) {
+      const int c = it / DP, j = it - c * DP, sc = c / m;
+      s.U[(size_t)c * DP + j] = s.X[(size_t)rk[sc * NPs + (c - sc * m)] * DP + j];
+    }
+    for (int c = threadIdx.x; c < k; c += kThreads) {
+      const int sc = c / m, r = c - sc * m, src = rk[sc * NPs + r];
+      const int dst = sc + 1 == S ? 0 : sc + 1;
+      byrank[c] = rk[dst * NPs + NPs - 1 - r];
+      s.ftr[c] = s.fit[src];
+      s.ttr[c] = s.tol[src];
+    }
   } else {  // SEL_IMPORT: candidates in trial rows [0, k) against ranks NP - k + c
     int k = 0;
     if (transfer_partner(a, task, a.gen[task], k) < 0) return;
@@ -653,6 +700,10 @@ __global__ void __launch_bounds__(256) select_kernel(const LargeArgs a, int mode
 // rows of the step and the member each one competes with
 __device__ __forceinline__ int sel_rows(const LargeArgs& a, int task, int mode, int& k) {
   const TaskDev td = a.tasks[task];
+  if (mode == SEL_MIGRATE) {
+    k = migration_due(a, task) ? a.subislands * migration_count(a, td.NP) : 0;
+    return k;
+  }
   if (mode == SEL_IMPORT) {
     k = 0;
     if (transfer_partner(a, task, a.gen[task], k) < 0) return 0;
@@ -661,7 +712,9 @@ __device__ __forceinline__ int sel_rows(const LargeArgs& a, int task, int mode, 
   return td.NP;
 }
 __device__ __forceinline__ int sel_target(const LargeArgs& a, const TaskDev& td, int mode, int k, int c) {
-  return mode == SEL_IMPORT ? a.rank[td.fit_off + td.NP - k + c] : c;
+  return mode == SEL_IMPORT    ? a.rank[td.fit_off + td.NP - k + c]
+         : mode == SEL_MIGRATE ? a.rank[td.fit_off + c]
+                               : c;
 }
 
 // near ties per re-check work item: one keeps the item's scratch at 32 KB
@@ -677,7 +730,7 @@ __global__ void __launch_bounds__(256) classify_kernel(const LargeArgs a, int mo
   if (!large_ok(td)) return;
   int k = 0;
   const int nrows = sel_rows(a, task, mode, k);
-  const bool strict = mode == SEL_IMPORT;
+  const bool strict = mode == SEL_IMPORT || mode == SEL_MIGRATE;  // candidates must be better
   const bool recheck = !(a.flags & FLAG_NO_RECHECK);
   __shared__ int nt;
   if (threadIdx.x == 0) nt = 0;
@@ -723,7 +776,7 @@ __global__ void __launch_bounds__(256) recheck_kernel(const LargeArgs a, int mod
   __shared__ int pair_c[kPairs], pair_m[kPairs], pair_same[kPairs], pair_zt[kPairs], pair_zp[kPairs];
   const int items = *a.nwork;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const bool strict = mode == SEL_IMPORT;
+  const bool strict = mode == SEL_IMPORT || mode == SEL_MIGRATE;  // candidates must be better
   for (int w = blockIdx.x; w < items; w += gridDim.x) {
     const int task = a.work[w] >> 16, b0 = a.work[w] & 0xFFFF;
     const TaskDev td = a.tasks[task];
@@ -911,6 +964,8 @@ __global__ void __launch_bounds__(256) apply_kernel(const LargeArgs a, int mode)
     if (mode == SEL_GENERATION) {
       a.gen[task] += 1u;
       if (a.stats) atomicAdd(a.stats + 3, (unsigned long long)td.NP);
+    } else if (mode == SEL_MIGRATE) {  // copies carry their fitness: no evaluations
+      if (acc && a.stats) atomicAdd(a.stats + 7, (unsigned long long)acc);
     } else if (a.stats) {
       if (acc) atomicAdd(a.stats + 2, (unsigned long long)acc);
       atomicAdd(a.stats + 3, (unsigned long long)k);

@@ -71,6 +71,20 @@ def test_migration_with_transfer_tc(sgemtf, orc, alg):
             precision=sgemtf.ROT_TF32X3, migration_count=3)
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("alg", [0, 2])
+def test_migration_large_islands(sgemtf, orc, precision, alg):
+    """The HBM-resident pipeline (any D > 128 in the handle): sub-island
+    draws in its trial kernel, migration through its selection pipeline."""
+    specs = [(0, 150, 32, 1), (4, 200, 32, 1), (6, 129, 16, 1), (2, 10, 24, 1)]
+    try:
+        migrated = _replay(sgemtf, orc, specs, 2, 3, 4, algorithm=alg, precision=precision,
+                           migration_count=3)
+    except sgemtf.EngineError as e:
+        pytest.skip(str(e))
+    assert migrated > 0
+
+
 def test_migration_inside_long_epochs(sgemtf, orc):
     """One run of many generations migrates at every interval inside the
     kernel; the same run cut into interval-long epochs gives the same state."""
@@ -103,9 +117,7 @@ def test_subisland_arguments(sgemtf):
         with pytest.raises(sgemtf.EngineError) as e:
             eng.add_tasks([sgemtf.TaskDesc(**bad)])
         assert e.value.status == sgemtf.ERR_INVALID_ARG
-    with pytest.raises(sgemtf.EngineError) as e:
-        eng.add_tasks([sgemtf.TaskDesc(0, 200, 32)])
-    assert e.value.status == sgemtf.ERR_UNSUPPORTED
+    eng.add_tasks([sgemtf.TaskDesc(0, 200, 32)])  # large islands split too
     eng2 = sgemtf.Engine(sgemtf.Config(seed=1, subislands=2, migration_count=5))
     with pytest.raises(sgemtf.EngineError) as e:
         eng2.add_tasks([sgemtf.TaskDesc(0, 4, 16)])
