@@ -436,9 +436,9 @@ def main_uneven(args, rank, world, local):
         return [a.elapsed_time(b) for a, b in evs]
 
     names = {(1, 0): "single", (1, 1): "single+graph", (2, 0): "buckets", (2, 1): "buckets+graph",
-             (3, 0): "per_task", (3, 1): "per_task+graph"}
+             (3, 0): "per_task", (3, 1): "per_task+graph", (4, 0): "queue", (4, 1): "queue+graph"}
     forms = {}
-    for key in [(1, 0), (1, 1), (2, 0), (2, 1), (3, 0)]:
+    for key in [(1, 0), (1, 1), (2, 0), (2, 1), (4, 0), (4, 1), (3, 0)]:
         eng = engine(*key)
         k = args.steps if key[0] != 3 else 1
         steps(eng, min(args.warmup, 1) if key[0] == 3 else args.warmup)

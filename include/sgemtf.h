@@ -167,7 +167,10 @@ typedef enum emt_schedule {
   EMT_SCHEDULE_BUCKETS = 2,  /* islands grouped by resident CTAs per SM, one
                                 launch per group with its own shared-memory size,
                                 groups concurrent on side streams               */
-  EMT_SCHEDULE_PER_TASK = 3  /* one single-CTA launch per island, 8 streams     */
+  EMT_SCHEDULE_PER_TASK = 3, /* one single-CTA launch per island, 8 streams     */
+  EMT_SCHEDULE_QUEUE = 4     /* one persistent launch, SMs x resident CTAs, each
+                                CTA taking the next island (longest first) from
+                                a device work queue                            */
 } emt_schedule;
 
 typedef struct emt_task_desc {

@@ -103,7 +103,8 @@ struct emt_handle {
   DevBuf<double> d_fit64, d_best_f64;
   DevBuf<uint32_t> d_gen;
   DevBuf<unsigned long long> d_stats;
-  DevBuf<int32_t> d_err, d_best_idx;
+  DevBuf<int32_t> d_err, d_best_idx, d_queue;
+  int queue_grid = 1;  // persistent grid of EMT_SCHEDULE_QUEUE: SMs x resident CTAs
   // tensor-core form: Q hi/lo tiles [task][2][Np][Kp] and their TMA map
   bool use_tc = false;
   int tc_np = 0, tc_kp = 0;
@@ -464,6 +465,12 @@ int upload(emt_handle* h) {
     h->buckets.back().smem = std::max(h->buckets.back().smem, h->task_smem[t]);
   }
   h->order.insert(h->order.end(), border.begin(), border.end());
+  if (!h->large) {  // the persistent grid: every SM slot the largest island allows
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+    h->queue_grid =
+        std::max(1, sms * std::max(1, emt_epoch_occupancy(h->use_tc, h->smem_bytes, true)));
+  }
   if (h->gexec) {
     cudaGraphExecDestroy(h->gexec);
     h->gexec = nullptr;
@@ -493,6 +500,7 @@ int upload(emt_handle* h) {
       (e = h->d_shift.ensure((size_t)o)) != cudaSuccess ||
       (e = h->d_gen.ensure(n)) != cudaSuccess ||
       (e = h->d_stats.ensure(emt::kStats)) != cudaSuccess || (e = h->d_err.ensure(1)) != cudaSuccess ||
+      (e = h->d_queue.ensure(1)) != cudaSuccess ||
       (e = h->d_best_idx.ensure(n)) != cudaSuccess ||
       (e = h->d_best_f32.ensure(n)) != cudaSuccess ||
       (e = h->d_best_f64.ensure(n)) != cudaSuccess || (e = h->d_best_err.ensure(n)) != cudaSuccess)
@@ -754,6 +762,12 @@ int launch_sched(emt_handle* h, emt::EpochArgs a, int sched, cudaStream_t stream
   const int n = (int)h->tasks.size();
   if (sched == EMT_SCHEDULE_SINGLE || (sched == EMT_SCHEDULE_BUCKETS && h->buckets.size() == 1))
     return emt_launch_epoch_noattr(a, n, stream, tm);
+  if (sched == EMT_SCHEDULE_QUEUE) {  // one persistent launch over the work queue
+    int e = (int)cudaMemsetAsync(h->d_queue.p, 0, sizeof(int32_t), stream);
+    a.queue = h->d_queue.p;
+    if (!e) e = emt_launch_epoch_noattr(a, std::min(n, h->queue_grid), stream, tm);
+    return e;
+  }
   int e = (int)cudaEventRecord(h->fork_ev, stream);
   const int nside = sched == EMT_SCHEDULE_BUCKETS ? (int)h->buckets.size() : emt_handle::kSide;
   for (int i = 0; i < nside && !e; ++i) e = (int)cudaStreamWaitEvent(h->side[i], h->fork_ev, 0);
@@ -926,7 +940,7 @@ int emt_create(const emt_config* cfg, emt_handle_t** out) {
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return EMT_ERR_CUDA;
   if (cfg->device < 0 || cfg->device >= ndev) return EMT_ERR_INVALID_ARG;
-  if (cfg->schedule < EMT_SCHEDULE_AUTO || cfg->schedule > EMT_SCHEDULE_PER_TASK ||
+  if (cfg->schedule < EMT_SCHEDULE_AUTO || cfg->schedule > EMT_SCHEDULE_QUEUE ||
       (cfg->use_graph != 0 && cfg->use_graph != 1))
     return EMT_ERR_INVALID_ARG;
   emt_handle* h = new (std::nothrow) emt_handle();
@@ -1134,7 +1148,8 @@ int emt_tune(emt_handle_t* h, int32_t generations, void* stream, int32_t* chosen
     if (rc) return rc;
   }
   h->stream = (cudaStream_t)stream;
-  std::vector<int> cands{EMT_SCHEDULE_SINGLE, EMT_SCHEDULE_SINGLE | 0x100};
+  std::vector<int> cands{EMT_SCHEDULE_SINGLE, EMT_SCHEDULE_SINGLE | 0x100, EMT_SCHEDULE_QUEUE,
+                         EMT_SCHEDULE_QUEUE | 0x100};
   if (h->buckets.size() > 1) {
     cands.push_back(EMT_SCHEDULE_BUCKETS);
     cands.push_back(EMT_SCHEDULE_BUCKETS | 0x100);
@@ -1485,7 +1500,7 @@ int emt_get_stats(emt_handle_t* h, emt_stats* out) {
   if (h->uploaded) {
     const int sched = effective_schedule(h);
     out->schedule_used = sched | (effective_graph(h) ? 0x100 : 0);
-    out->epoch_launches = sched == EMT_SCHEDULE_SINGLE ? 1
+    out->epoch_launches = sched == EMT_SCHEDULE_SINGLE || sched == EMT_SCHEDULE_QUEUE ? 1
                           : sched == EMT_SCHEDULE_BUCKETS ? (int32_t)h->buckets.size()
                                                           : (int32_t)h->tasks.size();
   }

@@ -79,6 +79,7 @@ struct EpochArgs {
   int32_t tc_np, tc_kp;       // tensor-core form: padded N and K of the B tiles
   // sub-islands: groups per island (1 = none), migration interval and count
   int32_t subislands, mig_interval, mig_count;
+  int32_t* queue;  // non-null: persistent grid taking islands from this counter
 };
 
 // Islands too large for one CTA's shared memory (D > kMaxDim, up to
@@ -290,7 +291,8 @@ struct BestArgs {
 int emt_launch_epoch(const emt::EpochArgs& a, int grid, void* stream, const void* tmap = nullptr);
 int emt_launch_epoch_noattr(const emt::EpochArgs& a, int grid, void* stream, const void* tmap);
 int emt_epoch_smem_attr(bool tc, size_t bytes);
-int emt_epoch_occupancy(bool tc, size_t bytes);
+// resident CTAs per SM of the epoch kernel (queue: its persistent-queue twin)
+int emt_epoch_occupancy(bool tc, size_t bytes, bool queue = false);
 int emt_launch_eval(const emt::EvalArgs& a, void* stream);
 // large islands (emt_large.cuh)
 int emt_large_init(const emt::LargeArgs& a, void* stream);

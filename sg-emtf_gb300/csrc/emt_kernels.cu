@@ -603,9 +603,7 @@ __device__ __forceinline__ int transfer_k(float rate, int NP) {
 
 template <bool TC>
 __device__ __forceinline__ void epoch_body(const EpochArgs& a, const void* tmap,
-                                           unsigned char* smem_raw) {
-  const int task = a.single_task >= 0 ? a.single_task
-                                      : (a.order ? a.order[blockIdx.x] : (int)blockIdx.x);
+                                           unsigned char* smem_raw, int task) {
   if (task < 0 || task >= a.n_tasks) {
     if (threadIdx.x == 0) report(a.err, CHECK_BAD_DESCRIPTOR);
     return;
@@ -825,17 +823,50 @@ __device__ __forceinline__ void epoch_body(const EpochArgs& a, const void* tmap,
   }
 }
 
+// One island per CTA (order[blockIdx.x], or single_task), or (QUEUE) a
+// persistent grid: each CTA takes the next island of the longest-first
+// order from the counter until none is left.  Separate instantiations keep
+// the one-island kernels' registers as they are.
+template <bool TC, bool QUEUE>
+__device__ __forceinline__ void epoch_entry(const EpochArgs& a, const void* tmap,
+                                            unsigned char* smem_raw) {
+  if constexpr (!QUEUE) {
+    epoch_body<TC>(a, tmap, smem_raw,
+                   a.single_task >= 0 ? a.single_task
+                                      : (a.order ? a.order[blockIdx.x] : (int)blockIdx.x));
+  } else {
+    __shared__ int item;
+    for (;;) {
+      __syncthreads();  // the previous island is written back; item is free
+      if (threadIdx.x == 0) item = atomicAdd(a.queue, 1);
+      __syncthreads();
+      const int i = item;
+      if (i >= a.n_tasks) return;
+      epoch_body<TC>(a, tmap, smem_raw, a.order ? a.order[i] : i);
+    }
+  }
+}
+
 // FP32 form: three islands of D = 50, NP = 64 share an SM (~68 KB each).
 __global__ void __launch_bounds__(kThreads, 3) epoch_kernel(const EpochArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  epoch_body<false>(a, nullptr, smem_raw);
+  epoch_entry<false, false>(a, nullptr, smem_raw);
+}
+__global__ void __launch_bounds__(kThreads, 3) epoch_kernel_queue(const EpochArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  epoch_entry<false, true>(a, nullptr, smem_raw);
 }
 
 // Tensor-core form: two islands per SM (~100 KB of operands and state each).
 __global__ void __launch_bounds__(kThreads, 2) epoch_kernel_tc(const EpochArgs a,
                                                                 const __grid_constant__ CUtensorMap tmap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  epoch_body<true>(a, &tmap, smem_raw);
+  epoch_entry<true, false>(a, &tmap, smem_raw);
+}
+__global__ void __launch_bounds__(kThreads, 2) epoch_kernel_tc_queue(
+    const EpochArgs a, const __grid_constant__ CUtensorMap tmap) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  epoch_entry<true, true>(a, &tmap, smem_raw);
 }
 
 // Evaluates n caller points of one task in chunks of up to 64 rows per CTA
@@ -959,32 +990,44 @@ int emt_launch_epoch(const emt::EpochArgs& a, int grid, void* stream, const void
 // caller has raised it to cover a.smem_bytes); usable inside stream capture.
 int emt_launch_epoch_noattr(const emt::EpochArgs& a, int grid, void* stream, const void* tmap) {
   if (grid <= 0) return 0;
-  if (tmap)
-    emt::epoch_kernel_tc<<<grid, emt::kThreads, a.smem_bytes, (cudaStream_t)stream>>>(
-        a, *reinterpret_cast<const CUtensorMap*>(tmap));
-  else
-    emt::epoch_kernel<<<grid, emt::kThreads, a.smem_bytes, (cudaStream_t)stream>>>(a);
+  const cudaStream_t st = (cudaStream_t)stream;
+  if (tmap) {
+    const CUtensorMap& m = *reinterpret_cast<const CUtensorMap*>(tmap);
+    if (a.queue)
+      emt::epoch_kernel_tc_queue<<<grid, emt::kThreads, a.smem_bytes, st>>>(a, m);
+    else
+      emt::epoch_kernel_tc<<<grid, emt::kThreads, a.smem_bytes, st>>>(a, m);
+  } else if (a.queue) {
+    emt::epoch_kernel_queue<<<grid, emt::kThreads, a.smem_bytes, st>>>(a);
+  } else {
+    emt::epoch_kernel<<<grid, emt::kThreads, a.smem_bytes, st>>>(a);
+  }
   return (int)cudaGetLastError();
 }
 
 // Raises the epoch kernel's dynamic shared-memory limit to bytes.
 int emt_epoch_smem_attr(bool tc, size_t bytes) {
-  const cudaError_t e =
-      tc ? cudaFuncSetAttribute(emt::epoch_kernel_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)bytes)
-         : cudaFuncSetAttribute(emt::epoch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)bytes);
+  const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
+  cudaError_t e = tc ? cudaFuncSetAttribute(emt::epoch_kernel_tc, at, (int)bytes)
+                     : cudaFuncSetAttribute(emt::epoch_kernel, at, (int)bytes);
+  if (e == cudaSuccess)  // the persistent-queue twin of the same form
+    e = tc ? cudaFuncSetAttribute(emt::epoch_kernel_tc_queue, at, (int)bytes)
+           : cudaFuncSetAttribute(emt::epoch_kernel_queue, at, (int)bytes);
   return (int)e;
 }
 
 // Resident CTAs per SM of the epoch kernel with `bytes` of dynamic shared
 // memory (0 if it cannot launch).
-int emt_epoch_occupancy(bool tc, size_t bytes) {
+int emt_epoch_occupancy(bool tc, size_t bytes, bool queue) {
   int n = 0;
   if (emt_epoch_smem_attr(tc, bytes) != 0) return 0;
-  const cudaError_t e =
-      tc ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, emt::epoch_kernel_tc, emt::kThreads, bytes)
-         : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, emt::epoch_kernel, emt::kThreads, bytes);
+  cudaError_t e;
+  if (queue)
+    e = tc ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, emt::epoch_kernel_tc_queue, emt::kThreads, bytes)
+           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, emt::epoch_kernel_queue, emt::kThreads, bytes);
+  else
+    e = tc ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, emt::epoch_kernel_tc, emt::kThreads, bytes)
+           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, emt::epoch_kernel, emt::kThreads, bytes);
   return e == cudaSuccess ? n : 0;
 }
 

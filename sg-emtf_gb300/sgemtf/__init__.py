@@ -33,7 +33,7 @@ FLAG_REF_BOXES = 0x8
 FLAG_NO_RECHECK = 0x10
 FLAG_RIGOROUS_WINDOW = 0x20
 FLAG_NO_DIFF_RECHECK = 0x40
-SCHEDULE_AUTO, SCHEDULE_SINGLE, SCHEDULE_BUCKETS, SCHEDULE_PER_TASK = 0, 1, 2, 3
+SCHEDULE_AUTO, SCHEDULE_SINGLE, SCHEDULE_BUCKETS, SCHEDULE_PER_TASK, SCHEDULE_QUEUE = 0, 1, 2, 3, 4
 MAX_DIM, MAX_POP = 128, 256
 NOALLOC_EXCHANGE_FLOATS = 1 << 19
 

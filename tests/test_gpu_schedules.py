@@ -34,7 +34,7 @@ def run_with(sgemtf, orc, schedule, graph, gens_list, interval=5):
     return out
 
 
-@pytest.mark.parametrize("schedule,graph", [(2, 0), (3, 0), (1, 1), (2, 1), (3, 1)])
+@pytest.mark.parametrize("schedule,graph", [(2, 0), (3, 0), (4, 0), (1, 1), (2, 1), (3, 1), (4, 1)])
 def test_schedules_bit_identical(sgemtf, orc, schedule, graph):
     gens = [3, 7, 5, 5, 1]  # epochs that start and end off the transfer boundaries
     ref, st_ref = run_with(sgemtf, orc, 1, 0, gens)
@@ -95,6 +95,6 @@ def test_tune_keeps_results(sgemtf, orc):
 
 def test_rejects_bad_schedule(sgemtf):
     with pytest.raises(sgemtf.EngineError):
-        sgemtf.Engine(sgemtf.Config(schedule=4))
+        sgemtf.Engine(sgemtf.Config(schedule=5))
     with pytest.raises(sgemtf.EngineError):
         sgemtf.Engine(sgemtf.Config(use_graph=2))
