@@ -112,12 +112,14 @@ struct emt_handle {
   CUtensorMap tmap;
   // large islands (any D > 128): HBM-resident pipeline (emt_large.cuh)
   bool large = false, large_tc = false;
-  int lKp = 0, lNq = 0, ldp = 4, lgrid = 1;
+  int lKp = 0, lNq = 0, ldp = 4;
+  int32_t lrot_grid = 1, ldecide_grid = 1;
   int64_t lrows = 0;
   size_t lsel_smem = 0;
   DevBuf<float> d_U, d_ftr, d_ttr, d_S, d_Z, d_qbig;
   DevBuf<int64_t> d_srow, d_qrow;
-  DevBuf<int32_t> d_rank, d_flag, d_ties, d_ntie, d_work, d_nwork;
+  DevBuf<int32_t> d_rank, d_flag, d_ties, d_ntie, d_work, d_nwork, d_tjob, d_jobs, d_njob, d_rwork;
+  DevBuf<double> d_zr;  // re-check rotations of the large-island pipeline
   CUtensorMap smap, qmap;
 
   int fail(int code, const std::string& msg) {
@@ -320,17 +322,19 @@ int large_upload(emt_handle* h, int64_t pop, int32_t fit) {
   }
   h->lrows = rows;
   h->ldp = dpmax;
-  int sms = 0, occ = 0;
+  int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
-  occ = emt_large_recheck_occupancy(dpmax);
-  h->lgrid = std::max(1, sms * std::max(1, occ));  // persistent re-check grid
+  emt_large_recheck_grids(sms, &h->lrot_grid, &h->ldecide_grid);  // persistent re-check grids
   h->lsel_smem = emt::large_select_smem(dpmax);
   const int planes = h->large_tc ? 2 : 1;
   cudaError_t e;
   if ((e = h->d_U.ensure((size_t)pop)) || (e = h->d_ftr.ensure((size_t)fit)) ||
       (e = h->d_ttr.ensure((size_t)fit)) || (e = h->d_rank.ensure((size_t)fit)) ||
       (e = h->d_flag.ensure((size_t)fit)) || (e = h->d_ties.ensure((size_t)fit)) ||
-      (e = h->d_ntie.ensure(n)) || (e = h->d_work.ensure((size_t)fit)) || (e = h->d_nwork.ensure(1)) ||
+      (e = h->d_ntie.ensure(n)) || (e = h->d_work.ensure((size_t)fit)) || (e = h->d_nwork.ensure(2)) ||
+      (e = h->d_tjob.ensure((size_t)fit)) || (e = h->d_jobs.ensure(2 * (size_t)fit)) ||
+      (e = h->d_njob.ensure(n)) || (e = h->d_rwork.ensure(2 * (size_t)fit + 8 * (size_t)n)) ||
+      (e = h->d_zr.ensure(2 * (size_t)pop)) ||
       (e = h->d_srow.ensure(n)) || (e = h->d_qrow.ensure(n)) ||
       (e = h->d_S.ensure((size_t)planes * rows * h->lKp)) ||
       (e = h->d_Z.ensure((size_t)rows * h->lNq)))
@@ -404,6 +408,9 @@ int upload(emt_handle* h) {
   h->large = false;
   for (const auto& t : h->tasks) h->large |= t.D > emt::kMaxDim;
   if (h->large) {
+    // the pipeline's work items carry the task index in 15 bits
+    if (h->tasks.size() > 32767)
+      return h->fail(EMT_ERR_UNSUPPORTED, "a handle with islands of D > 128 holds at most 32767 tasks");
     h->large_tc = h->cfg.precision != EMT_ROT_FP32 && device_has_tcgen05(h->device);
     if (!h->large_tc && h->cfg.precision == EMT_ROT_TF32X3)
       return h->fail(EMT_ERR_UNSUPPORTED, "tensor-core form needs an sm_10x device");
@@ -684,8 +691,15 @@ emt::LargeArgs large_args(emt_handle* h) {
   a.flag = h->d_flag.p;
   a.ties = h->d_ties.p;
   a.ntie = h->d_ntie.p;
+  a.tjob = h->d_tjob.p;
+  a.jobs = h->d_jobs.p;
+  a.njob = h->d_njob.p;
+  a.zr = h->d_zr.p;
   a.work = h->d_work.p;
+  a.rwork = h->d_rwork.p;
   a.nwork = h->d_nwork.p;
+  a.rot_grid = h->lrot_grid;
+  a.decide_grid = h->ldecide_grid;
   a.algorithm = h->cfg.algorithm;
   a.F = h->cfg.F;
   a.CR = h->cfg.CR;
@@ -721,7 +735,7 @@ int large_generation(emt_handle* h, const emt::LargeArgs& a, cudaStream_t stream
   int e = emt_large_build(a, emt::large::BUILD_TRIALS, stream);
   if (!e) e = emt_large_gemm(a, &h->smap, &h->qmap, stream);
   if (!e) e = emt_large_eval(a, 1, emt::kMaxPop, stream);
-  if (!e) e = emt_large_selection(a, emt::large::SEL_GENERATION, h->ldp, h->lgrid, stream);
+  if (!e) e = emt_large_selection(a, emt::large::SEL_GENERATION, stream);
   return e;
 }
 
@@ -737,7 +751,7 @@ int large_epoch(emt_handle* h, int gens, int imp, int exp, int parity, cudaStrea
     if (!e) e = emt_large_build(a, emt::large::BUILD_CANDIDATES, stream);
     if (!e) e = emt_large_gemm(a, &h->smap, &h->qmap, stream);
     if (!e) e = emt_large_eval(a, 1, emt::kMaxPop, stream);
-    if (!e) e = emt_large_selection(a, emt::large::SEL_IMPORT, h->ldp, h->lgrid, stream);
+    if (!e) e = emt_large_selection(a, emt::large::SEL_IMPORT, stream);
   }
   const bool migrate = a.subislands > 1 && a.mig_interval > 0;
   for (int g = 0; g < gens && !e; ++g) {
@@ -746,7 +760,7 @@ int large_epoch(emt_handle* h, int gens, int imp, int exp, int parity, cudaStrea
     // this sequence stays right whatever generation it starts at
     if (migrate) {
       e = emt_large_select(a, emt::large::SEL_MIGRATE, stream);
-      if (!e) e = emt_large_selection(a, emt::large::SEL_MIGRATE, h->ldp, h->lgrid, stream);
+      if (!e) e = emt_large_selection(a, emt::large::SEL_MIGRATE, stream);
     }
     if (!e) e = large_generation(h, a, stream);
   }

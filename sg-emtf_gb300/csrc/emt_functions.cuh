@@ -116,6 +116,43 @@ __device__ __forceinline__ double warp_prod64(double v) {
   return v;
 }
 
+// Reduction teams for the FP64-class evaluations: a warp (lanes over genes,
+// as the fused kernel runs them) or a whole CTA (the large-island decisions,
+// where one warp alone would set the launch length on the FP64 pipe).  With
+// WarpTeam the evaluations below run exactly the warp operations.
+struct WarpTeam {
+  __device__ __forceinline__ int rank() const { return threadIdx.x & 31; }
+  __device__ __forceinline__ int size() const { return 32; }
+  __device__ __forceinline__ double sum(double v) const { return warp_sum64(v); }
+  __device__ __forceinline__ double prod(double v) const { return warp_prod64(v); }
+  __device__ __forceinline__ int any(int p) const { return __any_sync(0xFFFFFFFFu, p); }
+};
+struct CtaTeam {
+  double* scratch;  // shared memory, one double per warp of the CTA
+  __device__ __forceinline__ int rank() const { return threadIdx.x; }
+  __device__ __forceinline__ int size() const { return blockDim.x; }
+  // warp partials combined in warp order, the same value in every thread
+  __device__ __forceinline__ double sum(double v) const {
+    v = warp_sum64(v);
+    if ((threadIdx.x & 31) == 0) scratch[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double r = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r += scratch[w];
+    __syncthreads();
+    return r;
+  }
+  __device__ __forceinline__ double prod(double v) const {
+    v = warp_prod64(v);
+    if ((threadIdx.x & 31) == 0) scratch[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double r = 1.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r *= scratch[w];
+    __syncthreads();
+    return r;
+  }
+  __device__ __forceinline__ int any(int p) const { return __syncthreads_or(p); }
+};
+
 // Bound on the Weierstrass error caused by rounding of the rotation, per
 // member: |dz_j| <= (gamma_{D+1} + 2^-20) * |q_j|_2 * |x - o|_2 (Cauchy-Schwarz
 // on the worst-case FP32 dot-product bound, plus the TF32 split error), pushed
@@ -419,24 +456,26 @@ __device__ __forceinline__ double rsqrt_d(double v) {
   return r;
 }
 
-// Tier 3: f in double precision from the FP64-class rotation zbuf.
-__device__ double eval_tier3(const FnConst& fc, const double* zbuf) {
-  const int lane = threadIdx.x & 31;
+// Tier 3: f in double precision from the FP64-class rotation zbuf, by the
+// calling team.
+template <class Team>
+__device__ double eval_tier3_t(const FnConst& fc, const double* zbuf, const Team& tm) {
+  const int r0 = tm.rank(), st = tm.size();
   const int D = fc.D;
   double a = 0.0, b = 0.0, c = 1.0;
   switch (fc.fid) {
     case F_SPHERE:
-      for (int j = lane; j < D; j += 32) a = fma(zbuf[j], zbuf[j], a);
+      for (int j = r0; j < D; j += st) a = fma(zbuf[j], zbuf[j], a);
       break;
     case F_RASTRIGIN:
-      for (int j = lane; j < D; j += 32) {
+      for (int j = r0; j < D; j += st) {
         const double v = zbuf[j];
         const double sp = fabs(v) < 0x1p-12 ? sinpi_small(v) : sinpi(v);
         a += fma(20.0 * sp, sp, v * v);
       }
       break;
     case F_ACKLEY:
-      for (int j = lane; j < D; j += 32) {
+      for (int j = r0; j < D; j += st) {
         const double v = zbuf[j];
         const double sp = fabs(v) < 0x1p-12 ? sinpi_small(v) : sinpi(v);
         a = fma(v, v, a);
@@ -444,7 +483,7 @@ __device__ double eval_tier3(const FnConst& fc, const double* zbuf) {
       }
       break;
     case F_GRIEWANK:
-      for (int j = lane; j < D; j += 32) {
+      for (int j = r0; j < D; j += st) {
         const double v = zbuf[j];
         a = fma(v, v, a);
         if (!(fc.flags & FLAG_REF_GRIEWANK_NO_PRODUCT)) {
@@ -454,14 +493,14 @@ __device__ double eval_tier3(const FnConst& fc, const double* zbuf) {
       }
       break;
     case F_ROSENBROCK:
-      for (int j = lane; j + 1 < D; j += 32) {
+      for (int j = r0; j + 1 < D; j += st) {
         const double v = zbuf[j], n = zbuf[j + 1];
         const double t1 = v * v - n, t2 = v - 1.0;
         a += 100.0 * t1 * t1 + t2 * t2;
       }
       break;
     case F_SCHWEFEL:
-      for (int j = lane; j < D; j += 32) {
+      for (int j = r0; j < D; j += st) {
         const double v = zbuf[j], av = fabs(v);
         if (av > 0.0) a += v * sin(av * rsqrt_d(av));
       }
@@ -469,18 +508,18 @@ __device__ double eval_tier3(const FnConst& fc, const double* zbuf) {
     default:
       break;
   }
-  a = warp_sum64(a);
+  a = tm.sum(a);
   double f;
   switch (fc.fid) {
     case F_ACKLEY: {
-      b = warp_sum64(b);
+      b = tm.sum(b);
       const double e = 2.718281828459045;
       const double eref = (fc.flags & FLAG_REF_ACKLEY_E) ? 2.718282 - e : 0.0;
       f = -20.0 * expm1(-0.2 * sqrt(a / D)) - e * expm1(-2.0 * b / D) + eref;
       break;
     }
     case F_GRIEWANK:
-      c = warp_prod64(c);
+      c = tm.prod(c);
       f = (1.0 - c) + a / 4000.0;
       break;
     case F_SCHWEFEL:
@@ -492,20 +531,24 @@ __device__ double eval_tier3(const FnConst& fc, const double* zbuf) {
   }
   return f;
 }
+__device__ double eval_tier3(const FnConst& fc, const double* zbuf) {
+  return eval_tier3_t(fc, zbuf, WarpTeam{});
+}
 
 // Tier 2: f from the FP64-class rotation zbuf with FP32 function terms on the
 // rounded z, summed in double, and *err, a first-order bound on |f - f(z)|:
 // per gene |g'(z)| |z - fl(z)| + 8u (|g| + |sub-terms|).  Sphere and
 // Rosenbrock need no transcendental and go straight to tier 3.
-__device__ double eval_tier2(const FnConst& fc, const double* zbuf, double* err) {
-  const int lane = threadIdx.x & 31;
+template <class Team>
+__device__ double eval_tier2_t(const FnConst& fc, const double* zbuf, double* err, const Team& tm) {
+  const int r0 = tm.rank(), st = tm.size();
   const int D = fc.D;
   const double u = 0x1p-24;
   double a = 0.0, b = 0.0, e = 0.0, eb = 0.0, lg = 0.0, c = 1.0;
   int neg = 0;
   switch (fc.fid) {
     case F_RASTRIGIN:
-      for (int j = lane; j < D; j += 32) {
+      for (int j = r0; j < D; j += st) {
         const double v = zbuf[j];
         const float zf = (float)v;
         const double dz = fabs(v - (double)zf);
@@ -516,7 +559,7 @@ __device__ double eval_tier2(const FnConst& fc, const double* zbuf, double* err)
       }
       break;
     case F_ACKLEY:
-      for (int j = lane; j < D; j += 32) {
+      for (int j = r0; j < D; j += st) {
         const double v = zbuf[j];
         const float zf = (float)v;
         const double dz = fabs(v - (double)zf);
@@ -527,7 +570,7 @@ __device__ double eval_tier2(const FnConst& fc, const double* zbuf, double* err)
       }
       break;
     case F_GRIEWANK:
-      for (int j = lane; j < D; j += 32) {
+      for (int j = r0; j < D; j += st) {
         const double v = zbuf[j];
         a = fma(v, v, a);
         if (!(fc.flags & FLAG_REF_GRIEWANK_NO_PRODUCT)) {
@@ -548,7 +591,7 @@ __device__ double eval_tier2(const FnConst& fc, const double* zbuf, double* err)
       }
       break;
     case F_SCHWEFEL:
-      for (int j = lane; j < D; j += 32) {
+      for (int j = r0; j < D; j += st) {
         const double v = zbuf[j];
         const float zf = (float)v;
         const double dz = fabs(v - (double)zf);
@@ -561,13 +604,13 @@ __device__ double eval_tier2(const FnConst& fc, const double* zbuf, double* err)
     default:
       break;
   }
-  a = warp_sum64(a);
-  e = warp_sum64(e);
+  a = tm.sum(a);
+  e = tm.sum(e);
   double f;
   switch (fc.fid) {
     case F_ACKLEY: {
-      b = warp_sum64(b);
-      eb = warp_sum64(eb);
+      b = tm.sum(b);
+      eb = tm.sum(eb);
       const double ee = 2.718281828459045;
       const double eref = (fc.flags & FLAG_REF_ACKLEY_E) ? 2.718282 - ee : 0.0;
       const double x2 = exp(-2.0 * b / D);
@@ -581,10 +624,10 @@ __device__ double eval_tier2(const FnConst& fc, const double* zbuf, double* err)
         om = 0.0;
         e = 0.0;
       } else {
-        c = warp_prod64(c);
-        lg = warp_sum64(lg);
-        eb = warp_sum64(eb);
-        neg = __any_sync(0xFFFFFFFFu, neg);
+        c = tm.prod(c);
+        lg = tm.sum(lg);
+        eb = tm.sum(eb);
+        neg = tm.any(neg);
         om = neg ? 1.0 - c : -expm1(lg);
         e = neg ? 1e300 : fabs(c) * eb;  // a sign change: leave it to tier 3
       }
@@ -601,6 +644,9 @@ __device__ double eval_tier2(const FnConst& fc, const double* zbuf, double* err)
   *err = 2.0 * e;  // safety factor on the first-order bound
   return f;
 }
+__device__ double eval_tier2(const FnConst& fc, const double* zbuf, double* err) {
+  return eval_tier2_t(fc, zbuf, err, WarpTeam{});
+}
 
 // |f32 - f64| / scale of one member, as BestArgs::best_err defines it: the
 // scale the FP32 evaluation stated, tol / rel (Weierstrass: 2D + |offset|).
@@ -612,12 +658,15 @@ __device__ __forceinline__ float best_rel_err(const TaskDev& td, float f32, doub
 }
 
 // Weierstrass from the FP64-class rotation: exactly reduced terms (FP32/INT).
-__device__ double eval_weier_precise(const FnConst& fc, const double* zbuf) {
-  const int lane = threadIdx.x & 31;
+template <class Team>
+__device__ double eval_weier_precise_t(const FnConst& fc, const double* zbuf, const Team& tm) {
   double acc = 0.0;
-  for (int n = lane; n < fc.D; n += 32) acc += (double)weier_gene_precise(zbuf[n]);
-  acc = warp_sum64(acc);
+  for (int n = tm.rank(); n < fc.D; n += tm.size()) acc += (double)weier_gene_precise(zbuf[n]);
+  acc = tm.sum(acc);
   return acc + fc.woff64;
+}
+__device__ double eval_weier_precise(const FnConst& fc, const double* zbuf) {
+  return eval_weier_precise_t(fc, zbuf, WarpTeam{});
 }
 
 // FP64-class fitness of x (shared or global memory row) by the calling warp

@@ -115,8 +115,14 @@ struct LargeArgs {
   int32_t* flag;         // per trial row: 0 keep, 1 replace (FP32), 2 near tie, 3 replace (re-checked)
   int32_t* ties;         // per task (fit offsets): its near-tie rows, in order found
   int32_t* ntie;         // per task: their number
-  int32_t* work;         // re-check work items: task << 16 | first tie of the item
-  int32_t* nwork;        // their number
+  int32_t* tjob;         // per near tie (fit offsets): trial job | (member job + 1) << 16
+  int32_t* jobs;         // per task (2 x fit offsets): rows to rotate, row | 1 << 16 for a member
+  int32_t* njob;         // per task: their number
+  double* zr;            // FP64-class rotations of the jobs, 2 x pop offsets, stride DP
+  int32_t* work;         // decision work items: task << 16 | tie
+  int32_t* rwork;        // rotation work items: task << 16 | column block << 12 | job chunk
+  int32_t* nwork;        // [0] decision items, [1] rotation items
+  int32_t rot_grid, decide_grid;  // persistent grids of the two re-check kernels
   int32_t algorithm;
   float F, CR, eta_c, p_c, eta_m, p_m;
   uint64_t seed;
@@ -301,8 +307,10 @@ int emt_large_gemm(const emt::LargeArgs& a, const void* smap, const void* qmap, 
 int emt_large_eval(const emt::LargeArgs& a, int which, int rows, void* stream);
 int emt_large_select(const emt::LargeArgs& a, int mode, void* stream);
 int emt_large_best(const emt::BestArgs& a, int maxD, void* stream);
-int emt_large_recheck_occupancy(int maxDP);
-// selection of a generation (mode SEL_GENERATION) or a transfer import
-// (SEL_IMPORT): classify, re-check each task's near ties in batches, apply
-int emt_large_selection(const emt::LargeArgs& a, int mode, int maxDP, int grid, void* stream);
+// persistent grids of the re-check rotation and decision kernels on sms SMs
+void emt_large_recheck_grids(int sms, int32_t* rot, int32_t* decide);
+// selection of a generation (SEL_GENERATION), a transfer import (SEL_IMPORT)
+// or a migration (SEL_MIGRATE): classify, rotate the near ties' rows, decide
+// them, apply
+int emt_large_selection(const emt::LargeArgs& a, int mode, void* stream);
 int emt_launch_best(const emt::BestArgs& a, void* stream);

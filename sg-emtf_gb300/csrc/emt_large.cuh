@@ -689,11 +689,13 @@ __global__ void __launch_bounds__(256) select_kernel(const LargeArgs a, int mode
 // selection split for parallelism.  The per-task CTA above would re-check a
 // task's near ties with its 8 warps while most SMs idle; at D = 1000 each
 // re-check rotates 10^6 compensated products.  Instead:
-//   classify (CTA per task): FP32 decisions; near ties to a global list;
-//   recheck  (persistent grid): one CTA per near tie, the compensated
-//            rotation spread over its 256 threads (the same per-output
-//            arithmetic as precise_rotation, so the same bits), then warp 0
-//            evaluates the FP64-class terms (tiers 2/3, exact Weierstrass);
+//   classify (CTA per task): FP32 decisions; near ties listed, identical
+//            trials decided, the rows to rotate listed as jobs;
+//   rot      (persistent grid): a task's jobs in chunks of 8, 128 outputs
+//            per item, every load of Q shared by the chunk's rows (the same
+//            per-output arithmetic as precise_rotation, so the same bits);
+//   decide   (persistent grid, a warp per near tie): tiers 2/3, exact
+//            Weierstrass, from the stored rotations;
 //   apply    (CTA per task): accepted rows into the island, counters.
 // ---------------------------------------------------------------------------
 
@@ -717,12 +719,11 @@ __device__ __forceinline__ int sel_target(const LargeArgs& a, const TaskDev& td,
                                : c;
 }
 
-// near ties per re-check work item: one keeps the item's scratch at 32 KB
-// (D = 1000), so five CTAs share an SM and hide the latency of the Q stream;
-// two or four per item share each Q load but cost occupancy (config 4 step:
-// 1.84 s with one, 1.91 s with two, 3.35 s with four)
-constexpr int kPairs = 1;
-constexpr int kJobs = 2 * kPairs;   // rotations per item (trial and parent)
+// near-tie rows rotated per work item (registers: 2 per job and thread) and
+// the k-tile of their exact splits staged in shared memory
+constexpr int kRotJobs = 8;
+constexpr int kRotTile = 128;
+constexpr int kRotCols = 128;  // outputs per item: one per thread of a 128-thread CTA
 
 __global__ void __launch_bounds__(256) classify_kernel(const LargeArgs a, int mode) {
   const int task = blockIdx.x;
@@ -732,8 +733,10 @@ __global__ void __launch_bounds__(256) classify_kernel(const LargeArgs a, int mo
   const int nrows = sel_rows(a, task, mode, k);
   const bool strict = mode == SEL_IMPORT || mode == SEL_MIGRATE;  // candidates must be better
   const bool recheck = !(a.flags & FLAG_NO_RECHECK);
-  __shared__ int nt;
-  if (threadIdx.x == 0) nt = 0;
+  const int D = td.D, DP = td.DP;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __shared__ int nt, nj;
+  if (threadIdx.x == 0) nt = nj = 0;
   __syncthreads();
   for (int c = threadIdx.x; c < nrows; c += blockDim.x) {
     const int m = sel_target(a, td, mode, k, c);
@@ -747,128 +750,107 @@ __global__ void __launch_bounds__(256) classify_kernel(const LargeArgs a, int mo
     a.flag[td.fit_off + c] = f;
   }
   __syncthreads();
-  // work items of up to kPairs ties each, to the GPU-wide queue
+  // a warp per near tie: an identical trial is decided here (the same vector
+  // has the same fitness: accepted unless the selection is strict); any other
+  // gets a rotation job, and one for its member when that member's
+  // FP64-class value is not cached, and a decision item
+  const int ties = nt;
+  for (int i = warp; i < ties; i += blockDim.x >> 5) {
+    const int c = a.ties[td.fit_off + i], m = sel_target(a, td, mode, k, c);
+    const float* u = a.U + td.pop_off + (size_t)c * DP;
+    const float* x = a.pop + td.pop_off + (size_t)m * DP;
+    bool diff = false;
+    for (int j = lane; j < D; j += 32) diff |= __float_as_uint(u[j]) != __float_as_uint(x[j]);
+    diff = __any_sync(0xFFFFFFFFu, diff);
+    if (lane != 0) continue;
+    if (!diff) {
+      const float f32t = a.ftr[td.fit_off + c], f32p = a.fit32[td.fit_off + m];
+      const bool d32 = strict ? (f32t < f32p) : (f32t <= f32p), d64 = !strict;
+      a.flag[td.fit_off + c] = d64 ? 3 : 0;  // member m keeps its cached FP64 value
+      a.tjob[td.fit_off + i] = -1;
+      if (a.stats) {
+        atomicAdd(a.stats + 0, 1ull);
+        if (d64 != d32) atomicAdd(a.stats + 1, 1ull);
+        atomicAdd(a.stats + 6, 1ull);
+      }
+      continue;
+    }
+    const bool member = isnan(a.fit64[td.fit_off + m]);
+    const int j = atomicAdd(&nj, member ? 2 : 1);
+    a.jobs[2 * td.fit_off + j] = c;
+    if (member) a.jobs[2 * td.fit_off + j + 1] = (1 << 16) | m;
+    a.tjob[td.fit_off + i] = j | ((member ? j + 2 : 0) << 16);
+    a.work[atomicAdd(a.nwork + 0, 1)] = (task << 16) | i;
+  }
+  __syncthreads();
   if (threadIdx.x == 0) {
-    a.ntie[task] = nt;
-    const int items = (nt + kPairs - 1) / kPairs;
-    if (items) {
-      const int w0 = atomicAdd(a.nwork, items);
-      for (int i = 0; i < items; ++i) a.work[w0 + i] = (task << 16) | (i * kPairs);
+    a.ntie[task] = ties;
+    a.njob[task] = nj;
+    const int blocks = (D + kRotCols - 1) / kRotCols, chunks = (nj + kRotJobs - 1) / kRotJobs;
+    if (chunks) {
+      const int w0 = atomicAdd(a.nwork + 1, blocks * chunks);
+      for (int b = 0; b < blocks; ++b)
+        for (int q = 0; q < chunks; ++q) a.rwork[w0 + b * chunks + q] = (task << 16) | (b << 12) | q;
     }
   }
 }
 
-// Re-check work item: up to kPairs near ties of one task.  A persistent grid
-// takes items from the queue (balance: ties of all tasks spread over all
-// SMs); within an item the compensated rotations of up to kJobs rows share
-// every load of Q (each output keeps dot2_pair's order, so the values equal
-// precise_rotation's); warp p then decides pair p (identical trial, tier 2,
-// tier 3 / exact Weierstrass, as select_and_replace does).
-
-__host__ __device__ inline size_t recheck_smem(int DP) {
-  return (size_t)kJobs * DP * (sizeof(double) + sizeof(float2));
-}
-
-__global__ void __launch_bounds__(256) recheck_kernel(const LargeArgs a, int mode) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  __shared__ int njob;
-  __shared__ const float* jrow[kJobs];
-  __shared__ int pair_c[kPairs], pair_m[kPairs], pair_same[kPairs], pair_zt[kPairs], pair_zp[kPairs];
-  const int items = *a.nwork;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const bool strict = mode == SEL_IMPORT || mode == SEL_MIGRATE;  // candidates must be better
+// Rotation work item: outputs [128 b, 128 b + 128) of up to kRotJobs rows of
+// one task (small items keep the grid busy when few islands have near ties).  A persistent grid takes items from the queue; each thread owns
+// one output and streams its column of Q once for all the item's rows, the
+// exact splits x - o of the rows staged in shared memory a k-tile at a time.
+// Each output keeps dot2_pair's order over k, so the values equal
+// precise_rotation's.
+__global__ void __launch_bounds__(kRotCols) rot_kernel(const LargeArgs a) {
+  __shared__ __align__(16) float2 pr[kRotTile][kRotJobs];
+  __shared__ const float* jrow[kRotJobs];
+  const int items = a.nwork[1];
   for (int w = blockIdx.x; w < items; w += gridDim.x) {
-    const int task = a.work[w] >> 16, b0 = a.work[w] & 0xFFFF;
+    const int code = a.rwork[w];
+    const int task = code >> 16, blk = (code >> 12) & 15, chunk = code & 0xFFF;
     const TaskDev td = a.tasks[task];
-    int k = 0;
-    sel_rows(a, task, mode, k);
     const int D = td.D, DP = td.DP;
-    double* zb = reinterpret_cast<double*>(smraw);                    // kJobs x DP
-    float2* pr = reinterpret_cast<float2*>(zb + (size_t)kJobs * DP);  // kJobs x DP
+    const int j0 = chunk * kRotJobs, nj = min(kRotJobs, a.njob[task] - j0);
+    if (threadIdx.x < kRotJobs) {
+      const int t = threadIdx.x;
+      const float* r = nullptr;
+      if (t < nj) {
+        const int jc = a.jobs[2 * td.fit_off + j0 + t];
+        r = ((jc >> 16) ? a.pop : a.U) + td.pop_off + (size_t)(jc & 0xFFFF) * DP;
+      }
+      jrow[t] = r;
+    }
     const float* o = a.shift + td.o_off;
-    const float* qt = a.qt + td.q_off;
-    const FnConst fc = fn_const(td, a.recheck_rel);
-    const int total = a.ntie[task];
-    // ---- the item: up to kPairs ties, their rows to rotate ----
-    if (threadIdx.x < kPairs) {
-      const int p = threadIdx.x;
-      pair_c[p] = -1;
-      if (b0 + p < total) {
-        const int c = a.ties[td.fit_off + b0 + p];
-        pair_c[p] = c;
-        pair_m[p] = sel_target(a, td, mode, k, c);
-      }
-    }
-    __syncthreads();
-    if (threadIdx.x < kPairs) pair_same[threadIdx.x] = 1;
-    __syncthreads();
-    for (int p = 0; p < kPairs; ++p) {
-      if (pair_c[p] < 0) continue;
-      const float* u = a.U + td.pop_off + (size_t)pair_c[p] * DP;
-      const float* x = a.pop + td.pop_off + (size_t)pair_m[p] * DP;
-      for (int j = threadIdx.x; j < D; j += blockDim.x)
-        if (__float_as_uint(u[j]) != __float_as_uint(x[j])) pair_same[p] = 0;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      int nj = 0;
-      for (int p = 0; p < kPairs; ++p) {
-        pair_zt[p] = pair_zp[p] = -1;
-        if (pair_c[p] < 0 || pair_same[p]) continue;
-        pair_zt[p] = nj;
-        jrow[nj++] = a.U + td.pop_off + (size_t)pair_c[p] * DP;
-        if (isnan(a.fit64[td.fit_off + pair_m[p]])) {
-          pair_zp[p] = nj;
-          jrow[nj++] = a.pop + td.pop_off + (size_t)pair_m[p] * DP;
-        }
-      }
-      njob = nj;
-    }
-    __syncthreads();
-    const int nj = njob;
-    if (nj > 0) {
-      // exact splits x - o of every job row
-      for (int it = threadIdx.x; it < nj * D; it += blockDim.x) {
-        const int j = it / D, kk = it - j * D;
-        float sh, sl;
-        two_sum(jrow[j][kk], -o[kk], sh, sl);
-        pr[(size_t)j * DP + kk] = make_float2(sh, sl);
+    const int n = blk * kRotCols + threadIdx.x;
+    const bool live = n < D;
+    const float* qcol = a.qt + td.q_off + (live ? n : 0);
+    float S[kRotJobs], C[kRotJobs];
+#pragma unroll
+    for (int j = 0; j < kRotJobs; ++j) S[j] = C[j] = 0.f;
+    for (int k0 = 0; k0 < D; k0 += kRotTile) {
+      const int kt = min(kRotTile, D - k0);
+      __syncthreads();  // jrow written; the previous tile consumed
+      for (int it = threadIdx.x; it < kRotJobs * kt; it += blockDim.x) {
+        const int j = it / kt, kk = it - j * kt;
+        float sh = 0.f, sl = 0.f;
+        if (j < nj) two_sum(jrow[j][k0 + kk], -o[k0 + kk], sh, sl);
+        pr[kk][j] = make_float2(sh, sl);
       }
       __syncthreads();
-      for (int n = threadIdx.x; n < D; n += blockDim.x) {
-        float S[kJobs], C[kJobs];
+      if (!live) continue;
+      constexpr int kAhead = 16;  // Q loads issued ahead of the dependent updates
+      int kk = 0;
+      for (; kk + kAhead <= kt; kk += kAhead) {
+        float qv[kAhead];
 #pragma unroll
-        for (int j = 0; j < kJobs; ++j) S[j] = C[j] = 0.f;
-        // Q loads issued kAhead steps ahead of the dependent compensated updates
-        constexpr int kAhead = 16;
-        const float* qcol = qt + n;
-        int kk = 0;
-        for (; kk + kAhead <= D; kk += kAhead) {
-          float qv[kAhead];
+        for (int u = 0; u < kAhead; ++u) qv[u] = __ldg(qcol + (size_t)(k0 + kk + u) * DP);
 #pragma unroll
-          for (int u = 0; u < kAhead; ++u) qv[u] = __ldg(qcol + (size_t)(kk + u) * DP);
+        for (int u = 0; u < kAhead; ++u) {
+          const float q = qv[u];
 #pragma unroll
-          for (int u = 0; u < kAhead; ++u)
-#pragma unroll
-            for (int j = 0; j < kJobs; ++j) {
-              if (j < nj) {
-                const float q = qv[u];
-                const float2 hl = pr[(size_t)j * DP + kk + u];
-                const float pp = __fmul_rn(q, hl.x);
-                const float e = __fmaf_rn(q, hl.x, -pp);
-                float t, te;
-                two_sum(S[j], pp, t, te);
-                S[j] = t;
-                C[j] = __fmaf_rn(q, hl.y, __fadd_rn(C[j], __fadd_rn(te, e)));
-              }
-            }
-        }
-        for (; kk < D; ++kk) {
-          const float q = __ldg(qcol + (size_t)kk * DP);
-#pragma unroll
-          for (int j = 0; j < kJobs; ++j) {
+          for (int j = 0; j < kRotJobs; ++j) {
             if (j < nj) {
-              const float2 hl = pr[(size_t)j * DP + kk];
+              const float2 hl = pr[kk + u][j];
               const float pp = __fmul_rn(q, hl.x);
               const float e = __fmaf_rn(q, hl.x, -pp);
               float t, te;
@@ -878,56 +860,88 @@ __global__ void __launch_bounds__(256) recheck_kernel(const LargeArgs a, int mod
             }
           }
         }
-#pragma unroll
-        for (int j = 0; j < kJobs; ++j)
-          if (j < nj) zb[(size_t)j * DP + n] = (double)S[j] + (double)C[j];
       }
-    }
-    __syncthreads();
-    // ---- decisions: warp p decides pair p ----
-    if (warp < kPairs && pair_c[warp] >= 0) {
-      const int p = warp, c = pair_c[p], m = pair_m[p];
-      double fp = a.fit64[td.fit_off + m], ft = fp, fpv = fp;
-      bool d64;
-      if (pair_same[p]) {
-        d64 = !strict;
-      } else {
-        const double* zt = zb + (size_t)pair_zt[p] * DP;
-        const double* zp = pair_zp[p] >= 0 ? zb + (size_t)pair_zp[p] * DP : nullptr;
-        const bool tier2 = fc.fid != F_WEIERSTRASS && fc.fid != F_SPHERE && fc.fid != F_ROSENBROCK;
-        bool decided = false;
-        ft = __longlong_as_double(0x7FF8000000000000ll);
-        d64 = false;
-        if (tier2) {
-          double et, ep = 0.0;
-          const double t2 = eval_tier2(fc, zt, &et);
-          double p2 = fp;
-          if (zp) p2 = eval_tier2(fc, zp, &ep);
-          if (fabs(t2 - p2) > et + ep) {
-            d64 = strict ? (t2 < p2) : (t2 <= p2);
-            decided = true;
+      for (; kk < kt; ++kk) {
+        const float q = __ldg(qcol + (size_t)(k0 + kk) * DP);
+#pragma unroll
+        for (int j = 0; j < kRotJobs; ++j) {
+          if (j < nj) {
+            const float2 hl = pr[kk][j];
+            const float pp = __fmul_rn(q, hl.x);
+            const float e = __fmaf_rn(q, hl.x, -pp);
+            float t, te;
+            two_sum(S[j], pp, t, te);
+            S[j] = t;
+            C[j] = __fmaf_rn(q, hl.y, __fadd_rn(C[j], __fadd_rn(te, e)));
           }
         }
-        if (!decided) {
-          ft = fc.fid == F_WEIERSTRASS ? eval_weier_precise(fc, zt) : eval_tier3(fc, zt);
-          if (zp) fpv = fc.fid == F_WEIERSTRASS ? eval_weier_precise(fc, zp) : eval_tier3(fc, zp);
-          d64 = strict ? (ft < fpv) : (ft <= fpv);
-        }
-      }
-      if (lane == 0) {
-        const float f32t = a.ftr[td.fit_off + c], f32p = a.fit32[td.fit_off + m];
-        const bool d32 = strict ? (f32t < f32p) : (f32t <= f32p);
-        a.flag[td.fit_off + c] = d64 ? 3 : 0;
-        // FP64 value of whichever vector member m holds afterwards
-        a.fit64[td.fit_off + m] = d64 ? ft : fpv;
-        if (a.stats) {
-          atomicAdd(a.stats + 0, 1ull);
-          if (d64 != d32) atomicAdd(a.stats + 1, 1ull);
-          if (pair_same[p]) atomicAdd(a.stats + 6, 1ull);
-        }
       }
     }
-    __syncthreads();
+    if (live) {
+      double* z = a.zr + 2 * td.pop_off + (size_t)j0 * DP + n;
+#pragma unroll
+      for (int j = 0; j < kRotJobs; ++j)
+        if (j < nj) z[(size_t)j * DP] = (double)S[j] + (double)C[j];
+    }
+    __syncthreads();  // jrow of the next item
+  }
+}
+
+// Writes the decision of near tie i (trial row c against member m).
+__device__ __forceinline__ void decide_write(const LargeArgs& a, const TaskDev& td, bool strict,
+                                             int c, int m, bool d64, double ft, double fpv) {
+  const float f32t = a.ftr[td.fit_off + c], f32p = a.fit32[td.fit_off + m];
+  const bool d32 = strict ? (f32t < f32p) : (f32t <= f32p);
+  a.flag[td.fit_off + c] = d64 ? 3 : 0;
+  // FP64 value of whichever vector member m holds afterwards
+  a.fit64[td.fit_off + m] = d64 ? ft : fpv;
+  if (a.stats) {
+    atomicAdd(a.stats + 0, 1ull);
+    if (d64 != d32) atomicAdd(a.stats + 1, 1ull);
+  }
+}
+
+// Decisions of the near ties: a persistent grid, a CTA per tie.  Tier 2,
+// then tier 3 (exact Weierstrass terms for that function), as
+// select_and_replace decides, from the stored rotations of the trial and
+// (when not cached) the member, with the genes over all 256 threads: the
+// FP64 terms of one tie on one warp take ~0.2 ms at D = 1000 on this GPU's
+// FP64 pipe, and a few such ties would set the launch length.
+__global__ void __launch_bounds__(256) decide_kernel(const LargeArgs a, int mode) {
+  __shared__ double scratch[8];
+  const CtaTeam tm{scratch};
+  const bool strict = mode == SEL_IMPORT || mode == SEL_MIGRATE;  // candidates must be better
+  const int items = a.nwork[0];
+  for (int w = blockIdx.x; w < items; w += gridDim.x) {
+    const int task = a.work[w] >> 16, i = a.work[w] & 0xFFFF;
+    const TaskDev td = a.tasks[task];
+    int k = 0;
+    sel_rows(a, task, mode, k);
+    const int c = a.ties[td.fit_off + i], m = sel_target(a, td, mode, k, c);
+    const int tj = a.tjob[td.fit_off + i];
+    const double* zb = a.zr + 2 * td.pop_off;
+    const double* zt = zb + (size_t)(tj & 0xFFFF) * td.DP;
+    const double* zp = (tj >> 16) ? zb + (size_t)((tj >> 16) - 1) * td.DP : nullptr;
+    const FnConst fc = fn_const(td, a.recheck_rel);
+    const double fp = a.fit64[td.fit_off + m];
+    double ft = __longlong_as_double(0x7FF8000000000000ll), fpv = fp;
+    bool d64 = false, decided = false;
+    if (fc.fid != F_WEIERSTRASS && fc.fid != F_SPHERE && fc.fid != F_ROSENBROCK) {
+      double et, ep = 0.0;
+      const double t2 = eval_tier2_t(fc, zt, &et, tm);
+      double p2 = fp;
+      if (zp) p2 = eval_tier2_t(fc, zp, &ep, tm);
+      if (fabs(t2 - p2) > et + ep) {
+        d64 = strict ? (t2 < p2) : (t2 <= p2);
+        decided = true;
+      }
+    }
+    if (!decided) {
+      ft = fc.fid == F_WEIERSTRASS ? eval_weier_precise_t(fc, zt, tm) : eval_tier3_t(fc, zt, tm);
+      if (zp) fpv = fc.fid == F_WEIERSTRASS ? eval_weier_precise_t(fc, zp, tm) : eval_tier3_t(fc, zp, tm);
+      d64 = strict ? (ft < fpv) : (ft <= fpv);
+    }
+    if (threadIdx.x == 0) decide_write(a, td, strict, c, m, d64, ft, fpv);
   }
 }
 
@@ -1060,28 +1074,25 @@ int emt_large_select(const emt::LargeArgs& a, int mode, void* stream) {
   return (int)cudaGetLastError();
 }
 
-int emt_large_selection(const emt::LargeArgs& a, int mode, int maxDP, int grid, void* stream) {
-  cudaError_t e = cudaMemsetAsync(a.nwork, 0, sizeof(int32_t), (cudaStream_t)stream);
+int emt_large_selection(const emt::LargeArgs& a, int mode, void* stream) {
+  cudaError_t e = cudaMemsetAsync(a.nwork, 0, 2 * sizeof(int32_t), (cudaStream_t)stream);
   if (e != cudaSuccess) return (int)e;
   emt::large::classify_kernel<<<a.n_tasks, 256, 0, (cudaStream_t)stream>>>(a, mode);
-  const size_t sm = emt::large::recheck_smem(maxDP);
-  e = cudaFuncSetAttribute(emt::large::recheck_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)sm);
-  if (e != cudaSuccess) return (int)e;
-  emt::large::recheck_kernel<<<grid, 256, sm, (cudaStream_t)stream>>>(a, mode);
+  emt::large::rot_kernel<<<a.rot_grid, emt::large::kRotCols, 0, (cudaStream_t)stream>>>(a);
+  emt::large::decide_kernel<<<a.decide_grid, 256, 0, (cudaStream_t)stream>>>(a, mode);
   emt::large::apply_kernel<<<a.n_tasks, 256, 0, (cudaStream_t)stream>>>(a, mode);
   return (int)cudaGetLastError();
 }
 
-int emt_large_recheck_occupancy(int maxDP) {
-  const size_t sm = emt::large::recheck_smem(maxDP);
-  if (cudaFuncSetAttribute(emt::large::recheck_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)sm) != cudaSuccess)
-    return 1;
-  int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, emt::large::recheck_kernel, 256, sm) != cudaSuccess)
-    return 1;
-  return n;
+void emt_large_recheck_grids(int sms, int32_t* rot, int32_t* decide) {
+  int r = 0, d = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, emt::large::rot_kernel, emt::large::kRotCols, 0) != cudaSuccess)
+    r = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d, emt::large::decide_kernel, 256, 0) != cudaSuccess)
+    d = 1;
+  if (sms < 1) sms = 1;
+  *rot = sms * (r > 1 ? r : 1);
+  *decide = sms * (d > 1 ? d : 1);
 }
 
 int emt_large_best(const emt::BestArgs& a, int maxD, void* stream) {
