@@ -642,7 +642,10 @@ def main_large(args, rank, world, local):
                      "note": "bytes = operand planes read + Z written per launch; the GEMM "
                              "streams every task's rotation from HBM each generation"},
         "clocks": r["clocks"],
-        "gpu_launches": args.steps * (3 + gens * 4 + (epochs - 1) * 5 + epochs),
+        # per step: reset 4 (init, build, rotation, eval); per generation 7
+        # (build, rotation, eval, classify, re-check rotations, decisions,
+        # apply); per transfer import 8 (rank, then the same 7); an export per epoch
+        "gpu_launches": args.steps * (4 + gens * 7 + (epochs - 1) * 8 + epochs),
     }
     if not args.no_cpu:
         line["cpu_baseline"] = large_cpu_baseline(os.cpu_count() or 1)

@@ -730,7 +730,8 @@ int large_eval_members(emt_handle* h, cudaStream_t stream) {
   return e;
 }
 
-// One generation: trials, rotation, evaluation, selection (4 launches).
+// One generation: trials, rotation, evaluation, selection (7 launches: the
+// selection is classify, re-check rotations, decisions, apply).
 int large_generation(emt_handle* h, const emt::LargeArgs& a, cudaStream_t stream) {
   int e = emt_large_build(a, emt::large::BUILD_TRIALS, stream);
   if (!e) e = emt_large_gemm(a, &h->smap, &h->qmap, stream);
