@@ -432,7 +432,10 @@ typedef struct emt_service emt_service_t;
 
 typedef struct emt_service_batch_info {
   int32_t n_tasks;
-  int32_t state;        /* 0 waiting for its arrival time, 1 running, 2 done */
+  int32_t state;        /* 0 waiting for its arrival time, 1 running, 2 done,
+                           3 failed (admission or a launch failed: the step
+                           that met it returned the error; the batch's handle
+                           is released and it is not tried again)          */
   int32_t generations;  /* generations completed                            */
   int32_t reserved;
   double arrival_ms;    /* as submitted                                      */
@@ -464,8 +467,9 @@ EMT_API int emt_service_submit(emt_service_t* s, int32_t n, const emt_task_desc*
  * batches.  *active (optional) receives the batches still waiting or
  * running. */
 EMT_API int emt_service_step(emt_service_t* s, int32_t* active);
-/* Rounds until every submitted batch is done; sleeps until the next arrival
- * when nothing runs. */
+/* Rounds until every submitted batch is done or failed; sleeps until the
+ * next arrival when nothing runs.  Returns at the first failure; calling it
+ * again serves the remaining batches. */
 EMT_API int emt_service_drain(emt_service_t* s);
 /* A batch's times and state; best (n_tasks floats, optional) receives each
  * task's best FP32 fitness once the batch is done. */

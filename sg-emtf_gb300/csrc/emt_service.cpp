@@ -32,7 +32,7 @@ struct Batch {
   std::vector<std::vector<double>> rot;  // deep copies of the caller's arrays
   std::vector<std::vector<float>> diag, shift;
   double arrival = 0.0, admit = -1.0, done = -1.0;
-  int state = 0;  // 0 waiting, 1 running, 2 done
+  int state = 0;  // 0 waiting, 1 running, 2 done, 3 failed
   int gens = 0;       // generations launched
   int completed = 0;  // generations seen complete
   bool inflight = false;
@@ -75,23 +75,35 @@ void release(Batch& b) {
   b.stream = nullptr;
 }
 
+// A batch whose admission or launch failed: its handle, stream and event
+// are released and it is not tried again; the failing call returns rc with
+// the reason in the service's last error.
+int give_up(emt_service* s, Batch& b, int id, int rc, const std::string& why) {
+  const std::string m = "batch " + std::to_string(id) + ": " + why;
+  if (b.stream) cudaStreamSynchronize(b.stream);
+  release(b);
+  b.inflight = false;
+  b.state = 3;
+  return s->fail(rc, m);
+}
+
 int admit(emt_service* s, Batch& b, int id) {
   emt_config c = s->cfg;
   c.seed = s->cfg.seed + (uint64_t)id;
   int rc = emt_create(&c, &b.h);
-  if (rc) return s->fail(rc, "batch " + std::to_string(id) + ": emt_create failed");
+  if (rc) return give_up(s, b, id, rc, "emt_create failed");
   for (size_t t = 0; t < b.desc.size(); ++t) {  // point the copies at this batch's arrays
     b.desc[t].rotation_matrix = b.rot[t].empty() ? nullptr : b.rot[t].data();
     b.desc[t].diag = b.diag[t].empty() ? nullptr : b.diag[t].data();
     b.desc[t].shift = b.shift[t].empty() ? nullptr : b.shift[t].data();
   }
   if ((rc = emt_add_tasks(b.h, (int32_t)b.desc.size(), b.desc.data())))
-    return s->fail(rc, "batch " + std::to_string(id) + ": " + emt_last_error(b.h));
+    return give_up(s, b, id, rc, emt_last_error(b.h));
   cudaError_t e = cudaStreamCreateWithFlags(&b.stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b.ev, cudaEventDisableTiming);
-  if (e != cudaSuccess) return s->cuda_fail(e, "batch stream");
-  if ((rc = emt_reset(b.h, b.stream)))
-    return s->fail(rc, "batch " + std::to_string(id) + ": " + emt_last_error(b.h));
+  if (e != cudaSuccess)
+    return give_up(s, b, id, EMT_ERR_CUDA, std::string("batch stream: ") + cudaGetErrorString(e));
+  if ((rc = emt_reset(b.h, b.stream))) return give_up(s, b, id, rc, emt_last_error(b.h));
   b.admit = s->now();
   b.state = 1;
   return EMT_OK;
@@ -104,28 +116,27 @@ int advance(emt_service* s, Batch& b, int id, bool* launched) {
   if (b.inflight) {
     const cudaError_t q = cudaEventQuery(b.ev);
     if (q == cudaErrorNotReady) return EMT_OK;
-    if (q != cudaSuccess) return s->cuda_fail(q, "batch epoch");
+    if (q != cudaSuccess)
+      return give_up(s, b, id, EMT_ERR_CUDA, std::string("batch epoch: ") + cudaGetErrorString(q));
     b.inflight = false;
     b.completed = b.gens;
   }
   int rc;
   if (b.gens < s->generations) {
     const int g = std::min(s->epoch, s->generations - b.gens);
-    if ((rc = emt_run(b.h, g, b.stream)))
-      return s->fail(rc, "batch " + std::to_string(id) + ": " + emt_last_error(b.h));
+    if ((rc = emt_run(b.h, g, b.stream))) return give_up(s, b, id, rc, emt_last_error(b.h));
     const cudaError_t e = cudaEventRecord(b.ev, b.stream);
-    if (e != cudaSuccess) return s->cuda_fail(e, "batch event");
+    if (e != cudaSuccess)
+      return give_up(s, b, id, EMT_ERR_CUDA, std::string("batch event: ") + cudaGetErrorString(e));
     b.gens += g;
     b.inflight = true;
     *launched = true;
     return EMT_OK;
   }
   b.best.resize(b.desc.size());
-  if ((rc = emt_get_best_all(b.h, b.best.data())))
-    return s->fail(rc, "batch " + std::to_string(id) + ": " + emt_last_error(b.h));
+  if ((rc = emt_get_best_all(b.h, b.best.data()))) return give_up(s, b, id, rc, emt_last_error(b.h));
   emt_stats st;
-  if ((rc = emt_get_stats(b.h, &st)))
-    return s->fail(rc, "batch " + std::to_string(id) + ": " + emt_last_error(b.h));
+  if ((rc = emt_get_stats(b.h, &st))) return give_up(s, b, id, rc, emt_last_error(b.h));
   b.evals = st.evaluations;
   b.done = s->now();
   b.state = 2;
@@ -195,7 +206,7 @@ EMT_API int emt_service_step(emt_service_t* s, int32_t* active) {
       bool launched = false;
       if ((rc = advance(s, b, (int)i, &launched))) return rc;
     }
-    left += b.state != 2;
+    left += b.state == 0 || b.state == 1;
   }
   size_t fr = 0, tot = 0;
   if ((e = cudaMemGetInfo(&fr, &tot)) != cudaSuccess) return s->cuda_fail(e, "cudaMemGetInfo");
@@ -248,6 +259,7 @@ EMT_API int emt_service_batch(emt_service_t* s, int32_t batch, emt_service_batch
     info->done_ms = b.done;
   }
   if (best) {
+    if (b.state == 3) return s->fail(EMT_ERR_STATE, "the batch failed");
     if (b.state != 2) return s->fail(EMT_ERR_STATE, "the batch has not finished");
     std::copy(b.best.begin(), b.best.end(), best);
   }

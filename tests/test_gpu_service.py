@@ -64,3 +64,23 @@ def test_service_arguments(sgemtf):
         sgemtf.Service(sgemtf.Config(seed=1), generations=10, epoch=0)
     with pytest.raises(sgemtf.EngineError):
         svc.batch(7)
+
+
+def test_failed_batch_is_released_and_skipped(sgemtf):
+    """A batch that cannot be admitted (here a bad function id, caught by
+    emt_add_tasks) fails once: the round that met it returns the error, the
+    batch is marked failed, and the remaining batches are served."""
+    svc = sgemtf.Service(sgemtf.Config(seed=5), generations=20, epoch=10)
+    bad = svc.submit([sgemtf.TaskDesc(99, 10, 16)])
+    good = svc.submit(_batch(sgemtf, 0, 3))
+    with pytest.raises(sgemtf.EngineError) as e:
+        svc.drain()
+    assert e.value.status == sgemtf.ERR_INVALID_ARG
+    info, best = svc.batch(bad)
+    assert info["state"] == 3 and best is None
+    svc.drain()
+    info, best = svc.batch(good)
+    assert info["state"] == 2 and best.shape == (3,)
+    st = svc.stats()
+    assert st["batches_submitted"] == 2 and st["batches_done"] == 1 and st["tasks_done"] == 3
+    svc.close()
