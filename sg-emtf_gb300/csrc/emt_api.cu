@@ -112,7 +112,7 @@ struct emt_handle {
   CUtensorMap tmap;
   // large islands (any D > 128): HBM-resident pipeline (emt_large.cuh)
   bool large = false, large_tc = false;
-  int lKp = 0, lNq = 0, ldp = 4;
+  int lKp = 0, lNq = 0;
   int32_t lrot_grid = 1, ldecide_grid = 1;
   int64_t lrows = 0;
   size_t lsel_smem = 0;
@@ -321,7 +321,6 @@ int large_upload(emt_handle* h, int64_t pop, int32_t fit) {
     qrow[t] = (int64_t)t * h->lNq;
   }
   h->lrows = rows;
-  h->ldp = dpmax;
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
   emt_large_recheck_grids(sms, &h->lrot_grid, &h->ldecide_grid);  // persistent re-check grids

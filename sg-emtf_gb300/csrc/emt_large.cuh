@@ -724,6 +724,15 @@ __device__ __forceinline__ int sel_target(const LargeArgs& a, const TaskDev& td,
 constexpr int kRotJobs = 8;
 constexpr int kRotTile = 128;
 constexpr int kRotCols = 128;  // outputs per item: one per thread of a 128-thread CTA
+// work-item encodings: rotation items task << 16 | block << 12 | chunk, jobs
+// row | member << 16, tie jobs trial | (member + 1) << 16, decisions
+// task << 16 | tie (tasks < 2^15, checked on the host).  Rotation items per
+// task: blocks x chunks <= (1024 / 128) x ceil(2 NP / 8) <= 2 NP + 8, within
+// the host's 2 fit + 8 T allocation.
+static_assert((kMaxDimLarge + kRotCols - 1) / kRotCols <= 16, "column block in 4 bits");
+static_assert((2 * kMaxPop + kRotJobs - 1) / kRotJobs < 4096, "job chunk in 12 bits");
+static_assert(2 * kMaxPop + 1 < 0xFFFF, "job and tie indices in 16 bits");
+static_assert(kRotCols >= kRotJobs && kRotCols % 32 == 0, "row pointers set by the first threads");
 
 __global__ void __launch_bounds__(256) classify_kernel(const LargeArgs a, int mode) {
   const int task = blockIdx.x;
