@@ -63,6 +63,9 @@ METRIC = "fitness evals/s, 1000 rotated D=50 tasks: TC form vs FP32 form at rel 
 UNIT = "evals/s"
 TASKS, DIM, POP, GENS = 1000, 50, 64, 2000
 FLOPS_PER_EVAL = 2 * DIM * DIM  # rotation, unpadded D, one product counted
+# DRAM bytes (read + write) of one epoch launch of 304 tasks, 200 generations,
+# from the committed ncu captures; per launch the state moves once
+EPOCH_DRAM_BYTES_304 = {"fp32": 8.12e6, "tf32x3": 16.9e6}
 
 
 def parse():
@@ -76,8 +79,10 @@ def parse():
     p.add_argument("--gens", type=int, default=GENS)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-parity", action="store_true")
     p.add_argument("--workload", default="continuous",
-                   choices=["continuous", "cvrp", "uneven", "large", "quality", "service"])
+                   choices=["continuous", "cvrp", "uneven", "large", "quality", "service",
+                            "phases"])
     p.add_argument("--seeds", type=int, default=30)
     return p.parse_args()
 
@@ -182,15 +187,156 @@ def cpu_run(n_tasks, gens, threads, rank=0, seed=1):
     return n_tasks * POP * gens, secs
 
 
-def cpu_baseline(n_tasks, target_s=12.0):
+# The CPU legs time a sample of the workload that keeps its mix of work: a
+# subset of the tasks, 16 per function (so every host thread gets the same
+# share of each function), for ALL the generations, early and late alike --
+# the late generations of converged islands are the re-check-heavy ones.
+CPU_SAMPLE_TASKS = 16 * 7
+
+
+def cpu_sample_tasks(n_tasks):
+    """Task ids of the CPU sample: the first CPU_SAMPLE_TASKS of the
+    workload (function t mod 7, so 16 of each)."""
+    return list(range(min(n_tasks, CPU_SAMPLE_TASKS)))
+
+
+def cpu_baseline(n_tasks, gens):
     threads = os.cpu_count() or 1
-    ev, s = cpu_run(n_tasks, 2, threads)
-    rate = ev / max(s, 1e-9)
-    gens = int(max(2, min(400, target_s * rate / (n_tasks * POP))))
-    ev, s = cpu_run(n_tasks, gens, threads)
+    sample = cpu_sample_tasks(n_tasks)
+    ev, s = cpu_run(len(sample), gens, threads)
     return {"value": ev / s, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "%d tasks x %d generations (of %d), D=%d, NP=%d, %.1f s"
-                      % (n_tasks, gens, GENS, DIM, POP, s)}
+            "sample": "%d of the %d tasks (16 per function) x all %d generations, D=%d, NP=%d, "
+                      "%.1f s, %s" % (len(sample), n_tasks, gens, DIM, POP, s, cpu_model())}
+
+
+# Tasks of the D = 50 workload replayed against the oracle after the timed
+# steps: two per function (the first seven and the last seven task ids).
+PARITY_TASKS = 14
+
+
+def parity_ids(n):
+    k = min(n, PARITY_TASKS // 2)
+    return sorted(set(list(range(k)) + list(range(max(0, n - k), n))))
+
+
+def population_digest(eng, n, k):
+    """SHA-256 over every task's final population (the forms' FP32 fitness
+    values differ by their rounding; the populations must not), and the
+    populations of the parity tasks."""
+    import hashlib
+    h = hashlib.sha256()
+    sample = {}
+    ids = set(parity_ids(n))
+    for i in range(n):
+        x = eng.population(i)[0]
+        h.update(x.tobytes())
+        if i in ids:
+            sample[i] = x
+    return h.hexdigest(), sample
+
+
+def initial_sample(eng, k, stream):
+    """Initial populations and task parameters of the parity tasks (after a
+    reset, which restarts every task from generation 0)."""
+    eng.reset(stream)
+    eng.sync()
+    out = {}
+    for i in parity_ids(len(eng.tasks)):
+        Q, o = eng.task_params(i)
+        out[i] = (eng.population(i)[0], Q, o)
+    return out
+
+
+def parity_check(results, x0, n, gens, rank):
+    """Outside the timed region: the forms' final populations must hash
+    alike, and the parity tasks' final populations must equal the oracle's
+    replay of all the generations with every selection decided in FP64."""
+    import orc
+    import sgemtf
+    orc.build()
+    p = orc.params(seed=1)
+    ids = sorted(x0)
+    tasks, X, f32, f64 = [], [], [], []
+    for i in ids:
+        fid = (rank * n + i) % 7
+        lo, hi = sgemtf.function_box(fid)
+        x, Q, o = x0[i]
+        t = orc.OTask(fid, DIM, POP, lo, hi, Q, o, 0, i)
+        tasks.append(t)
+        X.append(x.copy())
+        v = np.array([t.eval64(r)[0] for r in x])
+        f64.append(v)
+        f32.append(v.astype(np.float32))
+    t0 = time.perf_counter()
+    orc.run_threads(p, tasks, X, f32, f64, 0, gens, 0, len(tasks))
+    secs = time.perf_counter() - t0
+    match = {k: all(np.array_equal(v["sample"][i], X[j]) for j, i in enumerate(ids))
+             for k, v in results.items()}
+    digests = {v["digest"] for v in results.values()}
+    return {"identical": len(digests) == 1 and all(match.values()),
+            "forms_identical": len(digests) == 1, "oracle_match": match,
+            "oracle_tasks": ids, "generations": gens, "oracle_s": secs,
+            "how": "final populations of all %d tasks hashed per form (SHA-256, after the last "
+                   "timed step); tasks %s replayed by the oracle from the same initial "
+                   "populations for all %d generations, every selection in FP64"
+                   % (n, ids, gens)}
+
+
+def epoch_roofline(head, results, n, gens, peaks, peak_kind):
+    """Roofline of the dominant kernel, the epoch launch (all generations),
+    against the resource that binds it.  Algorithmic work: 2 D^2 flop of
+    rotation per evaluation (unpadded D, one product counted).  The FP32 form
+    issues that work on the FP32 pipe, whose peak is derived (SMs x 128 FMA
+    lanes x 2 flop x the SM clock sampled during the timed steps); the
+    tensor-core form issues it as kind::tf32 MMAs, whose peak is half the
+    measured bf16 dense rate.  Both forms are issue-bound on CUDA cores
+    (function epilogue, trial builder, near-tie re-checks): the committed ncu
+    capture gives their issue-active share.  HBM stays a secondary figure:
+    the islands live in shared memory for the whole launch."""
+    import torch
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    evals_epoch = n * POP * gens
+    dp = (DIM + 3) // 4 * 4
+    state_bytes = n * (DIM * dp * 4 + dp * 4 + 2 * POP * dp * 4 + POP * 16 * 2)
+    out = {}
+    for k, v in results.items():
+        epoch_s = v["epoch_ms"] * 1e-3
+        mhz = v["clocks"].get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+        fp32_peak = sms * 128 * 2 * mhz * 1e6 / 1e12
+        tf32_peak = peaks["bf16_tflops"] / 2.0
+        tflops = FLOPS_PER_EVAL * evals_epoch / epoch_s / 1e12
+        gbs = state_bytes / epoch_s / 1e9
+        out[k] = {"rotation_tflops": tflops,
+                  "fp32_pipe": {"peak": fp32_peak, "frac": tflops / fp32_peak,
+                                "peak_kind": "derived: %d SMs x 128 x 2 flop x %.0f MHz" % (sms, mhz)},
+                  "tensor_tf32": {"peak": tf32_peak, "frac": tflops / tf32_peak,
+                                  "peak_kind": peak_kind + " bf16 dense / 2"},
+                  "hbm": {"achieved": gbs, "peak": peaks["hbm_gbs"], "frac": gbs / peaks["hbm_gbs"],
+                          "bytes": state_bytes}}
+    h = out[head]
+    pipe = "tensor_tf32" if head == "tf32x3" else "fp32_pipe"
+    return {"bound": "tensor" if head == "tf32x3" else "fp32",
+            "achieved": h["rotation_tflops"], "peak": h[pipe]["peak"], "unit": "TFLOP/s",
+            "frac": h[pipe]["frac"], "peak_kind": h[pipe]["peak_kind"],
+            # ncu dram bytes (read + write) of one epoch launch, scaled from the
+            # captured 304-task launch to the workload's tasks
+            "traffic": EPOCH_DRAM_BYTES_304.get(head, 0.0) * n / 304 or None,
+            "kernel": "epoch_kernel%s, %.2f ms per launch (CUDA events on the launching stream)"
+                      % ("_tc" if head == "tf32x3" else "", results[head]["epoch_ms"]),
+            "binding": "CUDA-core issue: the rotation is a small share of the instructions "
+                       "(function epilogue, trial builder, near-tie re-checks)",
+            "forms": out}
+
+
+def continuous_config(n, gens, world):
+    """The `config` object of the D = 50 workload, shared by both arms."""
+    return {"workload": "DE/rand/1/bin F=0.5 CR=0.9, %d tasks, D=%d, NP=%d, %d generations, "
+                        "functions t mod 7, seeded-QR rotation, FP64 near-tie re-check"
+                        % (n, DIM, POP, gens),
+            "tasks_per_gpu": n, "dim": DIM, "pop": POP, "generations": gens,
+            "evals_per_step_per_gpu": n * POP * (gens + 1),
+            "l2": "flushed (256 MB write) before every step",
+            "parallelism": "task-sharded x%d" % world}
 
 
 def cpu_model():
@@ -205,16 +351,20 @@ def cpu_model():
 
 
 def run_reference(args, rank, world):
-    """Reference arm: the CPU restatement on all host cores, rank 0 only."""
+    """Reference arm: the CPU restatement on all host cores, rank 0 only.
+    Each step runs the sample of cpu_sample_tasks (16 tasks per function)
+    through ALL the workload's generations from a fresh population, so the
+    step holds the same mix of early and late (re-check-heavy) generations
+    as the GPU arm's step; warm-up steps run 2 generations."""
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    gens_per_step = 8
+    sample = cpu_sample_tasks(args.tasks)
     for _ in range(args.warmup):
-        cpu_run(args.tasks, 2, threads)
+        cpu_run(len(sample), 2, threads)
     tot_ev, tot_s = 0, 0.0
     for _ in range(args.steps):
-        ev, s = cpu_run(args.tasks, gens_per_step, threads)
+        ev, s = cpu_run(len(sample), args.gens, threads)
         tot_ev += ev
         tot_s += s
     v = tot_ev / tot_s
@@ -222,14 +372,12 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * tot_s / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Philox tasks)",
-        "config": {"workload": "DE/rand/1/bin, %d tasks, D=%d, NP=%d, %d generations, seeded-QR "
-                               "rotation" % (args.tasks, DIM, POP, args.gens),
-                   "tasks": args.tasks, "dim": DIM, "pop": POP, "generations": args.gens,
-                   "sample_generations_per_step": gens_per_step},
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Philox tasks, seeded-QR rotations)",
+        "config": continuous_config(args.tasks, args.gens, world),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "%d tasks x %d generations per step, %s"
-                                   % (args.tasks, gens_per_step, cpu_model())},
+                         "sample": "per step %d of the %d tasks (16 per function) x all %d "
+                                   "generations, D=%d, NP=%d, %s"
+                                   % (len(sample), args.tasks, args.gens, DIM, POP, cpu_model())},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -730,9 +878,58 @@ def main_service(args, rank, world, local):
         "data": "synthetic (seeded tasks, seeded-QR rotations, seeded arrival schedule)"}))
 
 
+def main_phases(args, rank, world, local):
+    """--workload phases: where the D = 50 workload's epoch kernel spends its
+    cycles, per form, from the measurement build of the library (phase
+    clocks, sg-emtf_gb300/build.py --phases).  Each phase boundary adds a
+    barrier, so the timings are this build's own; the shares are the
+    Amdahl split (rotation against everything else)."""
+    if rank != 0:
+        return
+    os.environ["SGEMTF_PHASE_CLOCKS"] = "1"
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "sgemtf_build", os.path.join(ROOT, "sg-emtf_gb300", "build.py"))
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    b.build(phases=True)
+    import torch
+    import sgemtf
+    torch.cuda.set_device(local)
+    sp = torch.cuda.current_stream().cuda_stream
+    n, gens = args.tasks, args.gens
+    out = {}
+    for name, prec in (("fp32", sgemtf.ROT_FP32), ("tf32x3", sgemtf.ROT_TF32X3)):
+        eng = sgemtf.Engine(sgemtf.Config(seed=1, precision=prec, device=local))
+        eng.add_tasks([sgemtf.TaskDesc(f, DIM, POP, rotation=sgemtf.ROTATION_SEEDED_QR)
+                       for f in task_specs(n, rank)])
+        eng.reset(sp)
+        eng.run(gens, sp)
+        cyc = eng.phase_cycles()
+        st = eng.stats()
+        eng.close()
+        tot = float(sum(cyc.values()))
+        rot = cyc["rotate"] / tot
+        out[name] = {"cycles": cyc, "share": {k: v / tot for k, v in cyc.items()},
+                     "device_ms": st["device_ms"],
+                     # Amdahl: the step's speed-up if the rotation cost nothing
+                     "ceiling_if_rotation_free": 1.0 / (1.0 - rot) if rot < 1 else None}
+    f, t = out["fp32"]["cycles"], out["tf32x3"]["cycles"]
+    print(json.dumps({
+        "workload": "phases", "metric": "SM cycles per phase of the epoch kernel (CTA totals), "
+        "%d tasks, D=%d, NP=%d, %d generations" % (n, DIM, POP, gens),
+        "forms": out,
+        # the TC form can at most remove the FP32 form's rotation cycles
+        "tc_over_fp32_ceiling": sum(f.values()) / (sum(f.values()) - f["rotate"]),
+        "tc_over_fp32_cycles": sum(f.values()) / sum(t.values()),
+        "note": "measurement build: a barrier at every phase boundary"}), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.workload == "phases" and args.impl == "ours":
+        return main_phases(args, rank, world, local)
     if args.workload == "service" and args.impl == "ours":
         return main_service(args, rank, world, local)
     if args.workload == "quality" and args.impl == "ours":
@@ -817,12 +1014,18 @@ def main():
             t = torch.tensor([dev_ms], device="cuda")
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             dev_ms = float(t.item())
+        # outside the timed region: the last step's final state (a full run
+        # from reset), hashed, and the parity sample's populations
+        digest, sample = population_digest(eng, n, PARITY_TASKS)
         results[name] = {"ms": ms, "epoch_ms": float(np.mean(epoch_ms)), "dev_ms": dev_ms,
-                         "wall": wall, "stats": st,
+                         "wall": wall, "stats": st, "digest": digest, "sample": sample,
                          "clocks": clk.summary(), "precision_used": st["precision_used"]}
+        if "x0" not in results:
+            results["x0"] = initial_sample(eng, PARITY_TASKS, sp)
         eng.close()
     # headline: the faster of the forms that ran (both give identical
-    # populations; both are reported under "forms")
+    # populations, checked below; both are reported under "forms")
+    x0 = results.pop("x0")
     ran = [k for k, v in results.items() if k == "fp32" or v["precision_used"] == 1]
     head = min(ran, key=lambda k: results[k]["dev_ms"])
     r = results[head]
@@ -866,54 +1069,31 @@ def main():
 
     peaks, peak_kind = measured_peaks()
     ms_step = r["dev_ms"] / args.steps
-    # dominant kernel: the epoch launch (all generations), timed with events
-    # on the launching stream; algorithmic work = 2 D^2 flop per evaluation
-    epoch_s = r["epoch_ms"] * 1e-3
-    evals_epoch = n * POP * gens
-    dp = (DIM + 3) // 4 * 4
-    state_bytes = n * (DIM * dp * 4 + dp * 4 + 2 * POP * dp * 4 + POP * 16 * 2)
-    if head == "tf32x3":
-        achieved = FLOPS_PER_EVAL * evals_epoch / epoch_s / 1e12
-        roof = {"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"],
-                "unit": "TFLOP/s", "frac": achieved / peaks["bf16_tflops"],
-                # ncu dram read bytes of one epoch launch (16.9 MB for 304 tasks,
-                # scaled to the workload's tasks; the state is read once)
-                "traffic": 16.9e6 * n / 304,
-                "peak_kind": peak_kind + " bf16 dense (tf32 nominal is half of it)",
-                "note": "the tensor pipe is ~5% busy; the kernel is bound by CUDA-core "
-                        "issue (function epilogue, trial builder, near-tie re-checks)"}
-    else:
-        gbs = state_bytes / epoch_s / 1e9
-        roof = {"bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                # ncu dram read bytes of one epoch launch: 8.12 MB for 304 tasks
-                "frac": gbs / peaks["hbm_gbs"], "traffic": 8.12e6 * n / 304,
-                "peak_kind": peak_kind, "note": "state is resident in shared memory across "
-                "generations; the kernel is bound by CUDA-core issue, not HBM"}
+    roof = epoch_roofline(head, results, n, gens, peaks, peak_kind)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded Philox tasks, seeded-QR rotations)",
-        "config": {"workload": "DE/rand/1/bin F=0.5 CR=0.9, %d tasks, D=%d, NP=%d, %d generations, "
-                               "functions t mod 7, seeded-QR rotation, FP64 near-tie re-check"
-                               % (n, DIM, POP, gens),
-                   "tasks_per_gpu": n, "dim": DIM, "pop": POP, "generations": gens,
-                   "evals_per_step_per_gpu": evals_per_step, "l2": "flushed (256 MB write) "
-                   "before every step", "form": head, "parallelism": "task-sharded x%d" % world},
+        "config": continuous_config(n, gens, world),
+        "form": head,
         "forms": {k: {"value": total_evals / (v["dev_ms"] * 1e-3), "ms_per_step": v["dev_ms"] / args.steps,
                       "epoch_kernel_ms": v["epoch_ms"],
                       "rechecks": v["stats"]["rechecks"], "recheck_flips": v["stats"]["recheck_flips"],
                       "max_rel_err_vs_fp64": v["stats"]["max_rel_err"],
+                      "final_populations_sha256": v["digest"],
                       "precision_used": v["precision_used"]} for k, v in results.items()},
         "roofline": roof,
         "clocks": r["clocks"],
         "gpu_launches": 2 * args.steps,
         "wall_s_timed_region": r["wall"],
     }
+    if not args.no_parity:
+        line["parity"] = parity_check(results, x0, n, gens, rank)
     if e2e:
         line["e2e"] = e2e
     if not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(n)
+        line["cpu_baseline"] = cpu_baseline(n, gens)
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

@@ -79,9 +79,10 @@ typedef enum emt_algorithm {
 typedef enum emt_precision {
   EMT_ROT_FP32 = 0,   /* FP32 FMA on CUDA cores                          */
   EMT_ROT_TF32X3 = 1, /* tcgen05 tensor cores, hi/lo TF32 split of both
-                         operands, FP32 accumulation in tensor memory: 3
-                         products for islands of D <= 128; for larger ones
-                         both lo parts rounded to TF32 and all 4 products */
+                         operands (both parts rounded to nearest), FP32
+                         accumulation in tensor memory: hi.hi in one
+                         accumulator, hi.lo + lo.hi + lo.lo in a second,
+                         added in FP32                                     */
   EMT_ROT_AUTO = 2    /* the fastest form the device supports            */
 } emt_precision;
 
@@ -119,6 +120,10 @@ typedef enum emt_rotation {
                                                  rigorous 3^k conditioning bound */
 #define EMT_FLAG_NO_DIFF_RECHECK 0x40u        /* re-check near ties by FP64-class values
                                                  only, without the differential form */
+#define EMT_FLAG_TEST_LOST_COMPLETION 0x80u   /* test switch, tensor-core form: the
+                                                 rotation issues no MMA and no commit, so
+                                                 its bounded wait runs out; the epoch stops
+                                                 and emt_sync returns EMT_ERR_DEVICE_CHECK */
 
 typedef struct emt_config {
   int32_t algorithm;         /* emt_algorithm                                */
@@ -153,7 +158,11 @@ typedef struct emt_config {
   int32_t migration_interval; /* generations between migrations; 0 = none       */
   int32_t migration_count;    /* members each group sends; 0 = NP/subislands/8,
                                  at least 1; 2 * count <= NP / subislands       */
-  int32_t reserved[2];
+  int32_t wait_limit_ms;      /* limit of every bounded device-side wait (TMA and
+                                 MMA completion on mbarriers); 0 = 2000 ms.  A
+                                 wait that runs out sets the kernel's error word
+                                 (emt_sync: EMT_ERR_DEVICE_CHECK)              */
+  int32_t reserved;
 } emt_config;
 
 /* How emt_run launches an epoch's islands (results are identical).  The
@@ -258,11 +267,15 @@ EMT_API int emt_run(emt_handle_t* h, int32_t generations, void* stream);
  * over tasks of NP * round4(D) must not exceed EMT_NOALLOC_EXCHANGE_FLOATS,
  * else EMT_ERR_UNSUPPORTED and nothing runs.  The first call on a device
  * looks up the array's device address (cudaGetSymbolAddress) with that
- * device current; make that first call before any stream capture.  All
- * calls share the array and it keeps the last call's contents: calls that
- * overlap on the GPU (other handles, other streams) race on it.  Nothing in
- * it needs to start at zero: each call first copies in the exchange state
- * its handle carries.  Results are bit-identical to emt_run. */
+ * device current and keeps it for the life of the process; make that first
+ * call before any stream capture, and do not call it again on a device the
+ * process has reset with cudaDeviceReset (the kept address would be stale).
+ * All calls share the array and it keeps the last call's contents: calls
+ * that overlap on the GPU (other handles, other streams) race on it.
+ * Nothing in it needs to start at zero: each call first copies in the
+ * exchange state its handle carries.  Every epoch is one launch over all
+ * islands; the handle's schedule, use_graph and emt_tune choices do not
+ * apply here.  Results are bit-identical to emt_run. */
 #define EMT_NOALLOC_EXCHANGE_FLOATS (1 << 19)
 EMT_API int emt_run_noalloc(emt_handle_t* h, int32_t generations, void* stream);
 
@@ -283,6 +296,15 @@ EMT_API int emt_tune(emt_handle_t* h, int32_t generations, void* stream, int32_t
  * handles, whose rotation runs inside the epoch kernel.  No counterpart in
  * the reference. */
 EMT_API int emt_time_rotation(emt_handle_t* h, int32_t reps, void* stream, float* ms);
+
+/* Measurement hook: SM cycles the fused epoch kernel's CTAs spent per phase
+ * since emt_reset, summed over CTAs: [0] loading and writing back islands
+ * and transfer bookkeeping, [1] trial vectors, [2] rotation, [3] function
+ * epilogue, [4] FP32 selection, [5] near-tie re-checks.  Only the library's
+ * measurement build counts them (compiled with EMT_PHASE_CLOCKS, which adds
+ * a barrier at each phase boundary); the regular build returns
+ * EMT_ERR_UNSUPPORTED.  No counterpart in the reference. */
+EMT_API int emt_get_phase_cycles(emt_handle_t* h, uint64_t* cycles, int32_t n);
 
 /* Waits for the handle's work and reports a kernel's error word. */
 EMT_API int emt_sync(emt_handle_t* h);

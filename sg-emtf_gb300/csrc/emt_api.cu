@@ -536,7 +536,7 @@ int upload(emt_handle* h) {
           const float v = ht.Q[(size_t)r * ht.D + c];
           const float vh = tf32_hi(v);
           hi[(size_t)r * h->tc_kp + c] = vh;
-          lo[(size_t)r * h->tc_kp + c] = v - vh;
+          lo[(size_t)r * h->tc_kp + c] = tf32_hi(v - vh);  // rounded, as the A tiles are
         }
     }
     if ((e = h->d_qtc.ensure(hqc.size())) != cudaSuccess) return h->cuda_fail(e, "cudaMalloc");
@@ -593,6 +593,7 @@ emt::EpochArgs base_args(emt_handle* h, int mode) {
   a.subislands = h->cfg.subislands > 1 ? h->cfg.subislands : 1;
   a.mig_interval = h->cfg.migration_interval;
   a.mig_count = h->cfg.migration_count;
+  a.wait_ns = h->cfg.wait_limit_ms > 0 ? (uint64_t)h->cfg.wait_limit_ms * 1000000ull : 0ull;
   return a;
 }
 
@@ -717,6 +718,7 @@ emt::LargeArgs large_args(emt_handle* h) {
   a.subislands = h->cfg.subislands > 1 ? h->cfg.subislands : 1;
   a.mig_interval = h->cfg.migration_interval;
   a.mig_count = h->cfg.migration_count;
+  a.wait_ns = h->cfg.wait_limit_ms > 0 ? (uint64_t)h->cfg.wait_limit_ms * 1000000ull : 0ull;
   return a;
 }
 
@@ -949,7 +951,7 @@ int emt_create(const emt_config* cfg, emt_handle_t** out) {
       !(cfg->transfer_rate > 0.f && cfg->transfer_rate <= 1.f) ||
       !(cfg->transfer_mix >= 0.f && cfg->transfer_mix <= 1.f) || !(cfg->recheck_rel >= 0.0) ||
       cfg->subislands < 0 || cfg->subislands > EMT_MAX_POP / 4 || cfg->migration_interval < 0 ||
-      cfg->migration_count < 0)
+      cfg->migration_count < 0 || cfg->wait_limit_ms < 0)
     return EMT_ERR_INVALID_ARG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return EMT_ERR_CUDA;
@@ -1201,7 +1203,8 @@ static float* g_noalloc_ptr[256];  // device address of g_noalloc_exchange per o
 
 // Host code cannot use g_noalloc_exchange's name as a device address (it is a
 // host-side stand-in): look the address up once per device, with that device
-// current, and reuse it.
+// current, and reuse it for the life of the process (a cudaDeviceReset by the
+// caller would make it stale; the header says so).
 static int noalloc_scratch(emt_handle* h, float** out) {
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
   if (h->device < 0 || h->device >= 256) return h->fail(EMT_ERR_INVALID_ARG, "device ordinal");
@@ -1311,6 +1314,8 @@ int emt_sync(emt_handle_t* h) {
                                                (code == emt::CHECK_BAD_DESCRIPTOR ? " (bad task descriptor)"
                                                 : code == emt::CHECK_SMEM_TOO_SMALL ? " (shared memory too small)"
                                                 : code == emt::CHECK_BAD_PARTNER ? " (bad transfer partner)"
+                                                : code == emt::CHECK_TIMEOUT ? " (a bounded device wait ran out)"
+                                                : code == emt::CHECK_TC_SHAPE ? " (island outside the tensor-core form's limits)"
                                                                                  : ""));
     }
   }
@@ -1519,6 +1524,22 @@ int emt_get_stats(emt_handle_t* h, emt_stats* out) {
                                                           : (int32_t)h->tasks.size();
   }
   return EMT_OK;
+}
+
+int emt_get_phase_cycles(emt_handle_t* h, uint64_t* cycles, int32_t n) {
+  if (!h || !cycles || n < 0) return EMT_ERR_INVALID_ARG;
+#ifndef EMT_PHASE_CLOCKS
+  return h->fail(EMT_ERR_UNSUPPORTED, "phase clocks need the measurement build (EMT_PHASE_CLOCKS)");
+#else
+  if (!h->d_stats.p) return h->fail(EMT_ERR_STATE, "no run yet");
+  int rc = emt_sync(h);
+  if (rc) return rc;
+  unsigned long long s[emt::kStats];
+  cudaError_t e = cudaMemcpy(s, h->d_stats.p, sizeof(s), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return h->cuda_fail(e, "copy phase clocks");
+  for (int k = 0; k < n; ++k) cycles[k] = k < emt::kPhases ? (uint64_t)s[8 + k] : 0u;
+  return EMT_OK;
+#endif
 }
 
 // Checkpoint layout: magic, task count, generation counter, then per task

@@ -38,6 +38,10 @@ constexpr uint32_t FLAG_REF_ACKLEY_E = 0x4u;
 constexpr uint32_t FLAG_REF_BOXES = 0x8u;
 constexpr uint32_t FLAG_NO_RECHECK = 0x10u;
 constexpr uint32_t FLAG_RIGOROUS_WINDOW = 0x20u;
+// Test switch of the tensor-core form: the rotation issues no MMA and no
+// commit, so the first bounded wait on the MMA barrier runs out with nothing
+// in flight; the kernel reports CHECK_TIMEOUT and stops the epoch.
+constexpr uint32_t FLAG_TEST_LOST_COMPLETION = 0x80u;
 
 // Weierstrass terms k = 0..20 of one gene: sum of 0.5^k cos(2 pi 3^k (z + 1/2)).
 // cos(2 pi 3^k (z + 1/2)) = -cos(pi y_k) with y_k = 2 * 3^k * |z| (3^k is odd).

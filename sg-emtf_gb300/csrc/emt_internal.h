@@ -39,7 +39,18 @@ constexpr size_t kSmemLimit = 227 * 1024;
 
 enum Mode : int { MODE_EPOCH = 0, MODE_INIT = 1, MODE_EVAL = 2 };
 
-constexpr int kStats = 8;  // device counters, indexed as in EpochArgs::stats
+// device counters, indexed as in EpochArgs::stats; [8, 8 + kPhases) hold the
+// per-phase SM cycles of the phase-clock build (EMT_PHASE_CLOCKS)
+constexpr int kPhases = 6;
+constexpr int kStats = 8 + kPhases;
+enum Phase : int {
+  PH_OTHER = 0,    // loading and writing back islands, transfer bookkeeping, migration ranks
+  PH_BUILD = 1,    // trial vectors and the rotation operand
+  PH_ROTATE = 2,   // the rotation (FP32 tiles, or the MMAs and the TMEM drain)
+  PH_EVAL = 3,     // the function epilogue: f and its near-tie window
+  PH_SELECT = 4,   // FP32 decisions, anchors carried forward, copies of accepted trials
+  PH_RECHECK = 5   // near ties re-decided: differential form, FP64-class tiers
+};
 
 struct EpochArgs {
   const TaskDev* tasks;
@@ -80,6 +91,7 @@ struct EpochArgs {
   // sub-islands: groups per island (1 = none), migration interval and count
   int32_t subislands, mig_interval, mig_count;
   int32_t* queue;  // non-null: persistent grid taking islands from this counter
+  uint64_t wait_ns;  // limit of every bounded device wait (tensor-core form)
 };
 
 // Islands too large for one CTA's shared memory (D > kMaxDim, up to
@@ -135,6 +147,7 @@ struct LargeArgs {
   int32_t* err;
   size_t select_smem;    // dynamic shared memory of the selection kernel
   int32_t subislands, mig_interval, mig_count;  // sub-islands per island (1 = none)
+  uint64_t wait_ns;      // limit of every bounded device wait
 };
 
 namespace large {
@@ -203,15 +216,27 @@ EMT_HD Layout smem_layout(int D, int NP, bool qt_in_smem = true) {
   return L;
 }
 
-// Shared-memory carve-up of the tensor-core form.  The operand tiles come
-// first (1024-byte aligned): A = 2 (hi/lo) x nkb tiles of MA rows x 128 B,
-// B = 2 x nkb tiles of Np rows x 128 B.  With NP <= 64 the A tiles hold 64
-// rows and an M = 128 MMA reads the next 64 rows past each tile (finite data
-// whose output rows are ignored), so B (or slack) must follow A.  The FP32
-// rotated rows Z alias the A region once the MMAs have completed.
+// Shared-memory carve-up of the tensor-core form.  The first kTcHeader bytes
+// of the dynamic shared memory hold the CTA's own tensor-core state, at the
+// same place whatever island it works on (the persistent queue kernel runs
+// many): two mbarriers (MMA completion, TMA arrival), the TMEM base and the
+// "a bounded wait gave up" flag.  Then, 1024-byte aligned, the operand tiles:
+// A = 2 (hi/lo) x nkb tiles of MA rows x 128 B, B = 2 x nkb tiles of Np
+// rows x 128 B.  With NP <= 64 the A tiles hold 64 rows and an M = 128 MMA
+// reads the next 64 rows past each tile (finite data whose output rows are
+// ignored), so B (or slack) must follow A.  The FP32 rotated rows Z alias the
+// A region once the MMAs have completed.
+constexpr size_t kTcHeader = 64;
+struct TcHeader {
+  uint64_t mma_bar, tma_bar;
+  uint32_t tmem;
+  int32_t dead;
+};
+static_assert(sizeof(TcHeader) <= kTcHeader, "tensor-core header");
+
 struct TcLayout {
   int DP, Np, Kp, nkb, MA;
-  size_t A, B, fit64, z64, X, U, o, fit, tol, ftr, ttr, idx, flag, list, misc, bars, total;
+  size_t A, B, fit64, z64, X, U, o, fit, tol, ftr, ttr, idx, flag, list, misc, total;
 };
 
 EMT_HD TcLayout tc_layout(int D, int NP, int Np, int Kp) {
@@ -249,8 +274,8 @@ EMT_HD TcLayout tc_layout(int D, int NP, int Np, int Kp) {
   L.flag = off;  off = align16(off + sizeof(int) * NP);
   L.list = off;  off = align16(off + sizeof(int) * NP);
   L.misc = off;  off = align16(off + sizeof(int) * 8);
-  L.bars = off;  off = align16(off + 32);
-  L.total = off + 1024;  // the kernel aligns its base to 1024 bytes
+  // the header, then up to 1023 bytes to the 1024-byte aligned base
+  L.total = off + kTcHeader + 1024;
   return L;
 }
 

@@ -31,6 +31,46 @@
 
 namespace emt {
 
+// Phase clocks (build with -DEMT_PHASE_CLOCKS, the measurement build): thread
+// 0 of each CTA charges the SM cycles between CTA-wide barriers to the phase
+// the CTA was in (the Phase enum), and adds its totals to the stats array at
+// the end of the island.  mark() adds a barrier at boundaries that lack one.
+// The product build compiles every mark away.
+#ifdef EMT_PHASE_CLOCKS
+struct PhaseClock {
+  long long t0, acc[kPhases];
+  int cur;
+  __device__ __forceinline__ void begin() {
+    if (threadIdx.x == 0) {
+      t0 = clock64();
+      cur = PH_OTHER;
+      for (int k = 0; k < kPhases; ++k) acc[k] = 0;
+    }
+  }
+  __device__ __forceinline__ void mark(int next) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const long long t = clock64();
+      acc[cur] += t - t0;
+      t0 = t;
+      cur = next;
+    }
+  }
+  __device__ __forceinline__ void flush(unsigned long long* stats) {
+    mark(PH_OTHER);
+    if (threadIdx.x == 0 && stats)
+      for (int k = 0; k < kPhases; ++k) atomicAdd(stats + 8 + k, (unsigned long long)acc[k]);
+  }
+};
+#define EMT_PHASE(s, k) \
+  do {                      \
+    if ((s).ph) (s).ph->mark(k); \
+  } while (0)
+#else
+struct PhaseClock {};
+#define EMT_PHASE(s, k) ((void)0)
+#endif
+
 struct Smem {
   double *fit64, *z64;
   float *zc, *zcb;  // this task's anchor cache (global memory)
@@ -39,8 +79,24 @@ struct Smem {
   // tensor-core form
   unsigned char *A, *B;
   uint32_t a_saddr, b_saddr, mma_bar, tma_bar, tmem;
+  uint32_t acc2;  // TMEM column offset of the second accumulator
   int MA, nkb, Np, N, ksteps;
   uint32_t idesc;
+  int* dead;         // CTA-wide: a bounded wait gave up (the MMAs are skipped)
+  uint64_t wait_ns;  // limit of each bounded wait
+  bool lose_completion;  // test switch: issue no MMA and no commit
+  PhaseClock* ph;        // thread 0's phase clocks (measurement build only)
+};
+
+// The tensor-core state of one CTA, set up once per CTA: TMEM is allocated
+// once (the allocation permit is relinquished right after, so a CTA that
+// works on several islands, as the persistent queue kernel does, must not
+// allocate again), the mbarriers are initialised once and their phases run
+// on across islands.  Every thread keeps the same copy of the phases.
+struct TcCta {
+  TcHeader* hdr;
+  uint32_t tmem, ncols, mma_bar, tma_bar;
+  uint32_t mphase, tphase;  // parity each barrier completes next
 };
 
 __device__ __forceinline__ Smem carve_tc(unsigned char* base, const TcLayout& L) {
@@ -55,6 +111,7 @@ __device__ __forceinline__ Smem carve_tc(unsigned char* base, const TcLayout& L)
   s.Z = (float*)(base + L.A);  // rotated rows alias the A operand after the MMAs
   s.QT = nullptr;
   s.zc = s.zcb = nullptr;
+  s.ph = nullptr;
   s.o = (float*)(base + L.o);
   s.fit = (float*)(base + L.fit);
   s.tol = (float*)(base + L.tol);
@@ -66,8 +123,6 @@ __device__ __forceinline__ Smem carve_tc(unsigned char* base, const TcLayout& L)
   s.misc = (int*)(base + L.misc);
   s.a_saddr = tc::smem_addr(s.A);
   s.b_saddr = tc::smem_addr(s.B);
-  s.mma_bar = tc::smem_addr(base + L.bars);
-  s.tma_bar = s.mma_bar + 8;
   s.MA = L.MA;
   s.nkb = L.nkb;
   s.Np = L.Np;
@@ -84,6 +139,7 @@ __device__ __forceinline__ Smem carve(unsigned char* base, const Layout& L) {
   s.Z = (float*)(base + L.Z);
   s.QT = (float*)(base + L.QT);
   s.zc = s.zcb = nullptr;
+  s.ph = nullptr;
   s.o = (float*)(base + L.o);
   s.fit = (float*)(base + L.fit);
   s.tol = (float*)(base + L.tol);
@@ -143,13 +199,15 @@ __device__ void rotate_f32(const Smem& s, int D, int DP, int NPP, int nrows) {
 
 // Stores the rotation input s = x_j - o_j of row i: FP32 form into ST[j][i];
 // tensor-core form as a TF32 hi/lo pair into the swizzled A tiles
-// (hi = round-to-nearest TF32, lo = s - hi exactly; the MMA reads lo's top
-// 19 bits).
+// (hi = round-to-nearest TF32 of s, lo = round-to-nearest TF32 of s - hi, so
+// s = hi + lo + r with |r| <= 2^-22 |s| and r unbiased; a lo left for the
+// tensor core to truncate would carry a one-signed error that grows linearly
+// over K).
 template <bool TC>
 __device__ __forceinline__ void stage(const Smem& s, int i, int j, float v, int NPP) {
   if constexpr (TC) {
     const float hi = tc::tf32_round(v);
-    const float lo = v - hi;
+    const float lo = tc::tf32_round(v - hi);
     const uint32_t off = tc::sw128_offset(i, j & 31);
     unsigned char* t = s.A + (size_t)((j >> 5) * 2) * s.MA * 128;
     *reinterpret_cast<float*>(t + off) = hi;
@@ -167,10 +225,10 @@ template <bool TC>
 __device__ __forceinline__ void stage4(const Smem& s, int i, int b, float4 v, int NPP) {
   if constexpr (TC) {
     float4 hi, lo;
-    hi.x = tc::tf32_round(v.x); lo.x = v.x - hi.x;
-    hi.y = tc::tf32_round(v.y); lo.y = v.y - hi.y;
-    hi.z = tc::tf32_round(v.z); lo.z = v.z - hi.z;
-    hi.w = tc::tf32_round(v.w); lo.w = v.w - hi.w;
+    hi.x = tc::tf32_round(v.x); lo.x = tc::tf32_round(v.x - hi.x);
+    hi.y = tc::tf32_round(v.y); lo.y = tc::tf32_round(v.y - hi.y);
+    hi.z = tc::tf32_round(v.z); lo.z = tc::tf32_round(v.z - hi.z);
+    hi.w = tc::tf32_round(v.w); lo.w = tc::tf32_round(v.w - hi.w);
     const uint32_t off = (uint32_t)((i >> 3) * 1024 + (i & 7) * 128 + (((b & 7) ^ (i & 7)) << 4));
     unsigned char* t = s.A + (size_t)((b >> 3) * 2) * s.MA * 128 + off;
     *reinterpret_cast<float4*>(t) = hi;
@@ -200,10 +258,13 @@ __device__ void stage_differences(const Smem& s, const float* rows, int nrows, i
   }
 }
 
-// Tensor-core rotation of rows [0, nrows): three tcgen05 MMA passes
-// (hi.hi + hi.lo + lo.hi) over the K steps that cover D, one issuing
-// thread, completion on an mbarrier; then warps 0-3 drain the accumulator
-// (TMEM lane = row) into Z.  phase: the mbarrier parity this CTA expects.
+// Tensor-core rotation of rows [0, nrows): four tcgen05 MMA passes over the
+// K steps that cover D, one issuing thread, completion on an mbarrier.  hi.hi
+// accumulates alone in the first accumulator; hi.lo + lo.hi + lo.lo (each
+// about 2^-11 of it) in the second, so the large partial sums of hi.hi do
+// not swallow the small products (each MMA step rounds its accumulator to
+// FP32).  Warps 0-3 then drain both accumulators (TMEM lane = row), add them
+// in FP32 and store Z.  phase: the mbarrier parity this CTA expects next.
 __device__ void rotate_tc(const Smem& s, int D, int DP, int nrows, uint32_t& phase) {
   // Columns [D, Kp) of every staged row must hold finite values (they meet
   // the zero columns of Q): the FP64 re-check scratch shares this region, so
@@ -218,34 +279,42 @@ __device__ void rotate_tc(const Smem& s, int D, int DP, int nrows, uint32_t& pha
   }
   tc::fence_async_smem();  // generic-proxy operand writes -> async proxy
   __syncthreads();
-  const bool dead = s.misc[2] != 0;  // an earlier wait gave up: skip the MMAs
-  if (threadIdx.x == 0 && !dead) {
+  const bool dead = *s.dead != 0;  // an earlier wait gave up: skip the MMAs
+  if (threadIdx.x == 0 && !dead && !s.lose_completion) {
     tc::fence_after();
-    uint32_t acc = 0;
-    const int pa[3] = {0, 0, 1}, pb[3] = {0, 1, 0};
-    for (int p = 0; p < 3; ++p)
+    const int pa[4] = {0, 0, 1, 1}, pb[4] = {0, 1, 0, 1};
+    for (int p = 0; p < 4; ++p) {
+      const uint32_t d = s.tmem + (p ? s.acc2 : 0u);
       for (int st = 0; st < s.ksteps; ++st) {
         const int kb = st >> 2, ks = st & 3;
         const uint64_t ad =
             tc::sdesc_sw128(s.a_saddr + (uint32_t)((kb * 2 + pa[p]) * s.MA * 128 + ks * 32));
         const uint64_t bd =
             tc::sdesc_sw128(s.b_saddr + (uint32_t)((pb[p] * s.nkb + kb) * s.Np * 128 + ks * 32));
-        tc::mma_tf32(s.tmem, ad, bd, s.idesc, acc);
-        acc = 1;
+        tc::mma_tf32(d, ad, bd, s.idesc, (st > 0 || p > 1) ? 1u : 0u);
       }
+    }
     tc::mma_commit(s.mma_bar);
   }
   if (!dead) {
-    if (!tc::mbar_wait(s.mma_bar, phase) && threadIdx.x == 0) s.misc[2] = 1;
+    if (!tc::mbar_wait(s.mma_bar, phase, s.wait_ns)) atomicExch(s.dead, 1);
     phase ^= 1u;
   }
+  __syncthreads();
   tc::fence_after();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (warp < 4 && 32 * warp < nrows && !dead) {  // warp-uniform: the loads are .sync.aligned
+  if (*s.dead) {
+    // no valid accumulator: finite zeros, and the epoch stops at the end of
+    // this generation with CHECK_TIMEOUT reported
+    for (int it = threadIdx.x; it < nrows * DP; it += kThreads) s.Z[it] = 0.f;
+  } else if (warp < 4 && 32 * warp < nrows) {  // warp-uniform: the loads are .sync.aligned
     const int row = 32 * warp + lane;
     for (int c0 = 0; c0 < s.N; c0 += 16) {
-      float v[16];
+      float v[16], w[16];
       tc::tmem_ld16(s.tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, v);
+      tc::tmem_ld16(s.tmem + ((uint32_t)(32 * warp) << 16) + s.acc2 + (uint32_t)c0, w);
+#pragma unroll
+      for (int g = 0; g < 16; ++g) v[g] = __fadd_rn(v[g], w[g]);
       if (row < nrows)
 #pragma unroll
         for (int q = 0; q < 4; ++q)
@@ -263,12 +332,14 @@ __device__ void rotate_tc(const Smem& s, int D, int DP, int nrows, uint32_t& pha
 template <bool TC>
 __device__ void evaluate_rows(const Smem& s, const FnConst& fc, const float* rows, int nrows,
                               int DP, int NPP, float* fout, float* tout, uint32_t& phase) {
+  EMT_PHASE(s, PH_ROTATE);
   if constexpr (TC) {
     rotate_tc(s, fc.D, DP, nrows, phase);
   } else {
     rotate_f32(s, fc.D, DP, NPP, nrows);
     __syncthreads();
   }
+  EMT_PHASE(s, PH_EVAL);
   eval_rows_f32<kThreads>(fc, s.Z, rows, s.o, nrows, DP, fout, tout);
   __syncthreads();
 }
@@ -388,6 +459,7 @@ __device__ int select_and_replace(const Smem& s, const EpochArgs& a, const FnCon
   const bool recheck = !(a.flags & FLAG_NO_RECHECK);
   const bool anchors = recheck && s.zcb && !(a.flags & FLAG_NO_DIFF_RECHECK) &&
                        diff_pays(fc.fid);
+  EMT_PHASE(s, PH_SELECT);
   if (threadIdx.x == 0) s.misc[0] = s.misc[1] = 0;
   __syncthreads();
   // flag bits: 1 accept, 2 re-checked, 4 anchor carried forward
@@ -410,6 +482,7 @@ __device__ int select_and_replace(const Smem& s, const EpochArgs& a, const FnCon
   __syncthreads();
   const int nre = s.misc[0], nadv = s.misc[1];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  EMT_PHASE(s, PH_RECHECK);
   for (int r = warp; r < nre; r += kWarps) {
     const int c = s.list[r];
     const int m = target ? target[c] : c;
@@ -511,6 +584,7 @@ __device__ int select_and_replace(const Smem& s, const EpochArgs& a, const FnCon
     if (lane == 0) s.zcb[2 * m] = ez;  // refreshed on its next use if above the limit
     __syncwarp();
   }
+  EMT_PHASE(s, PH_SELECT);
   __syncthreads();
   // copy accepted candidates into the population
   const int nq = DP >> 2;
@@ -603,7 +677,7 @@ __device__ __forceinline__ int transfer_k(float rate, int NP) {
 
 template <bool TC>
 __device__ __forceinline__ void epoch_body(const EpochArgs& a, const void* tmap,
-                                           unsigned char* smem_raw, int task) {
+                                           unsigned char* smem_raw, int task, TcCta& cta) {
   if (task < 0 || task >= a.n_tasks) {
     if (threadIdx.x == 0) report(a.err, CHECK_BAD_DESCRIPTOR);
     return;
@@ -616,7 +690,6 @@ __device__ __forceinline__ void epoch_body(const EpochArgs& a, const void* tmap,
   const int D = td.D, NP = td.NP;
   Smem s;
   int DP, NPP;
-  uint32_t ncols = 0;
   if constexpr (TC) {
     if (NP > 128 || round16(D) > a.tc_np || round32(D) > a.tc_kp) {
       if (threadIdx.x == 0) report(a.err, CHECK_TC_SHAPE);
@@ -627,32 +700,30 @@ __device__ __forceinline__ void epoch_body(const EpochArgs& a, const void* tmap,
       if (threadIdx.x == 0) report(a.err, CHECK_SMEM_TOO_SMALL);
       return;
     }
-    unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    unsigned char* base =
+        (unsigned char*)(((uintptr_t)smem_raw + kTcHeader + 1023) & ~(uintptr_t)1023);
     s = carve_tc(base, L);
+    s.mma_bar = cta.mma_bar;
+    s.tma_bar = cta.tma_bar;
+    s.tmem = cta.tmem;
+    s.acc2 = cta.ncols / 2;
+    s.dead = &cta.hdr->dead;
+    s.wait_ns = a.wait_ns ? a.wait_ns : tc::kWaitLimitNs;
+    s.lose_completion = (a.flags & FLAG_TEST_LOST_COMPLETION) != 0;
     s.QT = const_cast<float*>(a.qt + td.q_off);  // FP32 Q^T for the re-checks
     DP = L.DP;
     NPP = round4(NP);
     s.N = round16(D);
     s.ksteps = (D + 7) >> 3;
     s.idesc = tc::idesc_tf32(128, s.N);
-    ncols = 32;
-    while (ncols < (uint32_t)a.tc_np) ncols <<= 1;
     // zero the operand tiles once: padded K columns meet zero Q columns, so
     // they only need to hold finite values
     for (size_t it = threadIdx.x; it < (L.B - L.A) / 16; it += kThreads)
       reinterpret_cast<float4*>(s.A)[it] = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (threadIdx.x == 0) {
-      tc::mbar_init(s.mma_bar, 1);
-      tc::mbar_init(s.tma_bar, 1);
-      s.misc[2] = 0;
-    }
-    if ((threadIdx.x >> 5) == 0) tc::tmem_alloc(reinterpret_cast<uint32_t*>(s.misc + 4), ncols);
-    tc::fence_before();
-    __syncthreads();
-    tc::fence_after();
-    s.tmem = *reinterpret_cast<volatile uint32_t*>(s.misc + 4);
     // B operand: Q hi/lo tiles of this task by TMA (box 32 x Np x 1 per tile)
-    if (threadIdx.x == 0) {
+    // into the B region, which no MMA reads any more (the previous island's
+    // last MMAs completed before its selection)
+    if (threadIdx.x == 0 && !*s.dead) {
       tc::mbar_expect_tx(s.tma_bar, (uint32_t)(2 * s.nkb * s.Np * 128));
       for (int h = 0; h < 2; ++h)
         for (int kb = 0; kb < s.nkb; ++kb)
@@ -682,7 +753,12 @@ __device__ __forceinline__ void epoch_body(const EpochArgs& a, const void* tmap,
     s.zc = a.zc + 2 * td.pop_off;
     s.zcb = a.zcb + 2 * (size_t)td.fit_off;
   }
-  uint32_t phase = 0;
+  uint32_t phase = TC ? cta.mphase : 0u;
+#ifdef EMT_PHASE_CLOCKS
+  PhaseClock ph;
+  ph.begin();
+  s.ph = &ph;
+#endif
 
   // ---- load the task into shared memory ----
   const float* gq = a.qt + td.q_off;
@@ -718,7 +794,10 @@ __device__ __forceinline__ void epoch_body(const EpochArgs& a, const void* tmap,
   }
   for (int it = threadIdx.x; it < NP * DP; it += kThreads) s.U[it] = 0.f;
   if constexpr (TC) {
-    if (!tc::mbar_wait(s.tma_bar, 0) && threadIdx.x == 0) s.misc[2] = 1;
+    if (!*s.dead) {
+      if (!tc::mbar_wait(s.tma_bar, cta.tphase, s.wait_ns)) atomicExch(s.dead, 1);
+      cta.tphase ^= 1u;
+    }
   }
   __syncthreads();
 
@@ -783,10 +862,15 @@ __device__ __forceinline__ void epoch_body(const EpochArgs& a, const void* tmap,
       if (a.subislands > 1 && a.mig_interval > 0 && G > 1u &&
           (G - 1u) % (uint32_t)a.mig_interval == 0u)
         migrate(s, a, fc, NP, DP, st_re, st_fl);
+      EMT_PHASE(s, PH_BUILD);
       build_trials<TC>(s, a, td, task, G, DP, NPP);
       __syncthreads();
       evaluate_rows<TC>(s, fc, s.U, NP, DP, NPP, s.ftr, s.ttr, phase);
       select_and_replace(s, a, fc, NP, nullptr, false, DP, st_re, st_fl);
+      EMT_PHASE(s, PH_OTHER);
+      if constexpr (TC) {
+        if (*s.dead) break;  // read after the selection's barrier: CTA-uniform
+      }
     }
     if (threadIdx.x == 0) {
       a.gen[task] = gen0 + (uint32_t)a.gens;
@@ -814,13 +898,44 @@ __device__ __forceinline__ void epoch_body(const EpochArgs& a, const void* tmap,
     a.tol32[td.fit_off + i] = s.tol[i];
     a.fit64[td.fit_off + i] = s.fit64[i];
   }
-  if constexpr (TC) {
-    if (threadIdx.x == 0 && s.misc[2]) report(a.err, CHECK_TIMEOUT);
-    tc::fence_before();
-    __syncthreads();
-    tc::fence_after();
-    if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(s.tmem, ncols);
+#ifdef EMT_PHASE_CLOCKS
+  ph.flush(a.stats);
+#endif
+  if constexpr (TC) cta.mphase = phase;
+}
+
+// Sets up the CTA's tensor-core state in the header of its dynamic shared
+// memory: both mbarriers, the flag, and 2 x pow2(tc_np) TMEM columns (two
+// accumulators of the rotation).
+__device__ __forceinline__ void tc_cta_begin(const EpochArgs& a, unsigned char* smem_raw,
+                                             TcCta& cta) {
+  cta.hdr = reinterpret_cast<TcHeader*>(smem_raw);
+  cta.mma_bar = tc::smem_addr(&cta.hdr->mma_bar);
+  cta.tma_bar = tc::smem_addr(&cta.hdr->tma_bar);
+  uint32_t half = 32;
+  while (half < (uint32_t)a.tc_np) half <<= 1;
+  cta.ncols = 2 * half;
+  cta.mphase = cta.tphase = 0;
+  if (threadIdx.x == 0) {
+    tc::mbar_init(cta.mma_bar, 1);
+    tc::mbar_init(cta.tma_bar, 1);
+    cta.hdr->dead = 0;
   }
+  if ((threadIdx.x >> 5) == 0) tc::tmem_alloc(&cta.hdr->tmem, cta.ncols);
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  cta.tmem = *reinterpret_cast<volatile uint32_t*>(&cta.hdr->tmem);
+}
+
+// Reports a wait that gave up and frees the CTA's TMEM (no MMA is in
+// flight: every commit issued was waited for, or none was issued).
+__device__ __forceinline__ void tc_cta_end(const EpochArgs& a, TcCta& cta) {
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  if (threadIdx.x == 0 && cta.hdr->dead) report(a.err, CHECK_TIMEOUT);
+  if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(cta.tmem, cta.ncols);
 }
 
 // One island per CTA (order[blockIdx.x], or single_task), or (QUEUE) a
@@ -830,10 +945,13 @@ __device__ __forceinline__ void epoch_body(const EpochArgs& a, const void* tmap,
 template <bool TC, bool QUEUE>
 __device__ __forceinline__ void epoch_entry(const EpochArgs& a, const void* tmap,
                                             unsigned char* smem_raw) {
+  TcCta cta{};
+  if constexpr (TC) tc_cta_begin(a, smem_raw, cta);
   if constexpr (!QUEUE) {
     epoch_body<TC>(a, tmap, smem_raw,
                    a.single_task >= 0 ? a.single_task
-                                      : (a.order ? a.order[blockIdx.x] : (int)blockIdx.x));
+                                      : (a.order ? a.order[blockIdx.x] : (int)blockIdx.x),
+                   cta);
   } else {
     __shared__ int item;
     for (;;) {
@@ -841,10 +959,14 @@ __device__ __forceinline__ void epoch_entry(const EpochArgs& a, const void* tmap
       if (threadIdx.x == 0) item = atomicAdd(a.queue, 1);
       __syncthreads();
       const int i = item;
-      if (i >= a.n_tasks) return;
-      epoch_body<TC>(a, tmap, smem_raw, a.order ? a.order[i] : i);
+      if (i >= a.n_tasks) break;
+      if constexpr (TC) {
+        if (cta.hdr->dead) break;  // written before the barrier above: CTA-uniform
+      }
+      epoch_body<TC>(a, tmap, smem_raw, a.order ? a.order[i] : i, cta);
     }
   }
+  if constexpr (TC) tc_cta_end(a, cta);
 }
 
 // FP32 form: three islands of D = 50, NP = 64 share an SM (~68 KB each).

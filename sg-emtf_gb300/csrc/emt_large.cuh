@@ -370,11 +370,12 @@ __global__ void __launch_bounds__(192, 1)
   tc::fence_after();
   const uint32_t tmem = *tslot;
   const int64_t srow = a.srow[task] + m0, qrow = a.qrow[task] + n0;
+  const uint64_t wait_ns = a.wait_ns ? a.wait_ns : tc::kWaitLimitNs;
 
   if (warp == 0 && lane == 0) {  // producer
     for (int kb = 0; kb < nkb; ++kb) {
       const int s = kb % kTcStages;
-      if (kb >= kTcStages && !tc::mbar_wait(empty0 + 8 * s, ((kb / kTcStages) - 1) & 1)) {
+      if (kb >= kTcStages && !tc::mbar_wait(empty0 + 8 * s, ((kb / kTcStages) - 1) & 1, wait_ns)) {
         atomicExch(&ctl[0], 1);
         break;
       }
@@ -392,7 +393,7 @@ __global__ void __launch_bounds__(192, 1)
     int kb = 0;
     for (; kb < nkb; ++kb) {
       const int s = kb % kTcStages;
-      if (!tc::mbar_wait(full0 + 8 * s, (kb / kTcStages) & 1)) {
+      if (!tc::mbar_wait(full0 + 8 * s, (kb / kTcStages) & 1, wait_ns)) {
         atomicExch(&ctl[0], 1);
         break;
       }
@@ -416,7 +417,7 @@ __global__ void __launch_bounds__(192, 1)
     }
     if (kb == nkb) tc::mma_commit(done);
   } else if (warp >= 2) {  // epilogue
-    const bool ok = tc::mbar_wait(done, 0);
+    const bool ok = tc::mbar_wait(done, 0, wait_ns);
     if (!ok && lane == 0) atomicExch(&ctl[0], 1);
     tc::fence_after();
     const int q = warp & 3;

@@ -113,9 +113,13 @@ __device__ __forceinline__ uint64_t globaltimer() {
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
-// Waits for phase `parity` of the barrier; gives up after ~2 s and returns
-// false, so a lost completion can never hang the GPU.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+// Default limit of a bounded wait: 2 s of %globaltimer.
+constexpr uint64_t kWaitLimitNs = 2000000000ull;
+
+// Waits for phase `parity` of the barrier; gives up after limit_ns and
+// returns false, so a lost completion can never hang the GPU.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity,
+                                          uint64_t limit_ns = kWaitLimitNs) {
   const uint64_t t0 = globaltimer();
   for (uint32_t it = 0;; ++it) {
     uint32_t ok;
@@ -125,7 +129,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
         : "r"(bar), "r"(parity)
         : "memory");
     if (ok) return true;
-    if ((it & 63) == 63 && globaltimer() - t0 > 2000000000ull) return false;
+    if ((it & 63) == 63 && globaltimer() - t0 > limit_ns) return false;
   }
 }
 

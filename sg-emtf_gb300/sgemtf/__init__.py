@@ -16,6 +16,8 @@ import numpy as np
 
 PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(PKG_DIR, "_build", "libsgemtf.so")
+# the measurement build (phase clocks), loaded instead when SGEMTF_PHASE_CLOCKS=1
+PHASES_LIB_PATH = os.path.join(PKG_DIR, "_build", "libsgemtf_phases.so")
 
 # ---- enums (include/sgemtf.h) ----
 OK, ERR_INVALID_ARG, ERR_OUT_OF_MEMORY, ERR_CUDA, ERR_DEVICE_TIMEOUT, ERR_STATE, \
@@ -33,6 +35,7 @@ FLAG_REF_BOXES = 0x8
 FLAG_NO_RECHECK = 0x10
 FLAG_RIGOROUS_WINDOW = 0x20
 FLAG_NO_DIFF_RECHECK = 0x40
+FLAG_TEST_LOST_COMPLETION = 0x80
 SCHEDULE_AUTO, SCHEDULE_SINGLE, SCHEDULE_BUCKETS, SCHEDULE_PER_TASK, SCHEDULE_QUEUE = 0, 1, 2, 3, 4
 MAX_DIM, MAX_POP = 128, 256
 NOALLOC_EXCHANGE_FLOATS = 1 << 19
@@ -40,6 +43,7 @@ NOALLOC_EXCHANGE_FLOATS = 1 << 19
 EXPORTED = [
     "emt_config_default", "emt_function_from_reference", "emt_function_box", "emt_create",
     "emt_add_tasks", "emt_reset", "emt_run", "emt_run_noalloc", "emt_tune", "emt_time_rotation",
+    "emt_get_phase_cycles",
     "emt_sync", "emt_get_best", "emt_get_best_all",
     "emt_get_population", "emt_set_population", "emt_get_task_info", "emt_get_task_params",
     "emt_evaluate", "emt_get_stats", "emt_snapshot_size", "emt_snapshot", "emt_restore",
@@ -64,7 +68,7 @@ class Config(ctypes.Structure):
                 ("device", ctypes.c_int32), ("schedule", ctypes.c_int32),
                 ("use_graph", ctypes.c_int32), ("subislands", ctypes.c_int32),
                 ("migration_interval", ctypes.c_int32), ("migration_count", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 2)]
+                ("wait_limit_ms", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
     def __init__(self, **kw):
         super().__init__()
@@ -167,10 +171,11 @@ def lib():
     fallback implementation."""
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB_PATH):
-            raise RuntimeError("libsgemtf.so not built: run `python sg-emtf_gb300/build.py` "
-                               "(or __graft_entry__.build())")
-        L = ctypes.CDLL(LIB_PATH)
+        path = PHASES_LIB_PATH if os.environ.get("SGEMTF_PHASE_CLOCKS") == "1" else LIB_PATH
+        if not os.path.exists(path):
+            raise RuntimeError("%s not built: run `python sg-emtf_gb300/build.py` "
+                               "(--phases for the measurement build)" % os.path.basename(path))
+        L = ctypes.CDLL(path)
         vp = ctypes.c_void_p
         i32 = ctypes.c_int32
         f32p = ctypes.POINTER(ctypes.c_float)
@@ -186,6 +191,7 @@ def lib():
         L.emt_run_noalloc.argtypes = [vp, i32, vp]
         L.emt_tune.argtypes = [vp, i32, vp, ctypes.POINTER(ctypes.c_int32)]
         L.emt_time_rotation.argtypes = [vp, i32, vp, ctypes.POINTER(ctypes.c_float)]
+        L.emt_get_phase_cycles.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64), i32]
         L.emt_sync.argtypes = [vp]
         L.emt_get_best.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_double), f32p]
         L.emt_get_best_all.argtypes = [vp, f32p]
@@ -331,6 +337,15 @@ class Engine:
 
     def sync(self):
         self._check(lib().emt_sync(self._h), "emt_sync")
+
+    PHASES = ["other", "build", "rotate", "eval", "select", "recheck"]
+
+    def phase_cycles(self):
+        """emt_get_phase_cycles (measurement build only): SM cycles per phase."""
+        out = (ctypes.c_uint64 * len(self.PHASES))()
+        self._check(lib().emt_get_phase_cycles(self._h, out, len(self.PHASES)),
+                    "emt_get_phase_cycles")
+        return dict(zip(self.PHASES, [int(v) for v in out]))
 
     def _dim(self, task):
         if 0 <= task < len(self.tasks):
