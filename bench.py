@@ -66,6 +66,7 @@ FLOPS_PER_EVAL = 2 * DIM * DIM  # rotation, unpadded D, one product counted
 # DRAM bytes (read + write) of one epoch launch of 304 tasks, 200 generations,
 # from the committed ncu captures; per launch the state moves once
 EPOCH_DRAM_BYTES_304 = {"fp32": 8.12e6, "tf32x3": 16.9e6}
+TC_FORMS = ("tf32x3", "bf16x3")
 
 
 def parse():
@@ -74,7 +75,7 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--precision", default="auto", choices=["fp32", "tf32x3", "auto"])
+    p.add_argument("--precision", default="auto", choices=["fp32", "tf32x3", "bf16x3", "auto"])
     p.add_argument("--tasks", type=int, default=TASKS)
     p.add_argument("--gens", type=int, default=GENS)
     p.add_argument("--no-e2e", action="store_true")
@@ -288,8 +289,9 @@ def epoch_roofline(head, results, n, gens, peaks, peak_kind):
     rotation per evaluation (unpadded D, one product counted).  The FP32 form
     issues that work on the FP32 pipe, whose peak is derived (SMs x 128 FMA
     lanes x 2 flop x the SM clock sampled during the timed steps); the
-    tensor-core form issues it as kind::tf32 MMAs, whose peak is half the
-    measured bf16 dense rate.  Both forms are issue-bound on CUDA cores
+    tensor-core forms issue it as kind::tf32 MMAs, whose peak is half the
+    measured bf16 dense rate, or as kind::f16 MMAs on BF16 parts, whose peak
+    is the measured bf16 dense rate.  Both forms are issue-bound on CUDA cores
     (function epilogue, trial builder, near-tie re-checks): the committed ncu
     capture gives their issue-active share.  HBM stays a secondary figure:
     the islands live in shared memory for the whole launch."""
@@ -303,26 +305,27 @@ def epoch_roofline(head, results, n, gens, peaks, peak_kind):
         epoch_s = v["epoch_ms"] * 1e-3
         mhz = v["clocks"].get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
         fp32_peak = sms * 128 * 2 * mhz * 1e6 / 1e12
-        tf32_peak = peaks["bf16_tflops"] / 2.0
+        tc_peak = peaks["bf16_tflops"] / (2.0 if k == "tf32x3" else 1.0)
         tflops = FLOPS_PER_EVAL * evals_epoch / epoch_s / 1e12
         gbs = state_bytes / epoch_s / 1e9
         out[k] = {"rotation_tflops": tflops,
                   "fp32_pipe": {"peak": fp32_peak, "frac": tflops / fp32_peak,
                                 "peak_kind": "derived: %d SMs x 128 x 2 flop x %.0f MHz" % (sms, mhz)},
-                  "tensor_tf32": {"peak": tf32_peak, "frac": tflops / tf32_peak,
-                                  "peak_kind": peak_kind + " bf16 dense / 2"},
+                  "tensor": {"peak": tc_peak, "frac": tflops / tc_peak,
+                             "peak_kind": peak_kind + " bf16 dense" +
+                                          (" / 2 (kind::tf32)" if k == "tf32x3" else "")},
                   "hbm": {"achieved": gbs, "peak": peaks["hbm_gbs"], "frac": gbs / peaks["hbm_gbs"],
                           "bytes": state_bytes}}
     h = out[head]
-    pipe = "tensor_tf32" if head == "tf32x3" else "fp32_pipe"
-    return {"bound": "tensor" if head == "tf32x3" else "fp32",
+    pipe = "tensor" if head in TC_FORMS else "fp32_pipe"
+    return {"bound": "tensor" if head in TC_FORMS else "fp32",
             "achieved": h["rotation_tflops"], "peak": h[pipe]["peak"], "unit": "TFLOP/s",
             "frac": h[pipe]["frac"], "peak_kind": h[pipe]["peak_kind"],
             # ncu dram bytes (read + write) of one epoch launch, scaled from the
             # captured 304-task launch to the workload's tasks
             "traffic": EPOCH_DRAM_BYTES_304.get(head, 0.0) * n / 304 or None,
             "kernel": "epoch_kernel%s, %.2f ms per launch (CUDA events on the launching stream)"
-                      % ("_tc" if head == "tf32x3" else "", results[head]["epoch_ms"]),
+                      % ("_tc" if head in TC_FORMS else "", results[head]["epoch_ms"]),
             "binding": "CUDA-core issue: the rotation is a small share of the instructions "
                        "(function epilogue, trial builder, near-tie re-checks)",
             "forms": out}
@@ -899,7 +902,8 @@ def main_phases(args, rank, world, local):
     sp = torch.cuda.current_stream().cuda_stream
     n, gens = args.tasks, args.gens
     out = {}
-    for name, prec in (("fp32", sgemtf.ROT_FP32), ("tf32x3", sgemtf.ROT_TF32X3)):
+    for name, prec in (("fp32", sgemtf.ROT_FP32), ("tf32x3", sgemtf.ROT_TF32X3),
+                       ("bf16x3", sgemtf.ROT_BF16X3)):
         eng = sgemtf.Engine(sgemtf.Config(seed=1, precision=prec, device=local))
         eng.add_tasks([sgemtf.TaskDesc(f, DIM, POP, rotation=sgemtf.ROTATION_SEEDED_QR)
                        for f in task_specs(n, rank)])
@@ -914,14 +918,15 @@ def main_phases(args, rank, world, local):
                      "device_ms": st["device_ms"],
                      # Amdahl: the step's speed-up if the rotation cost nothing
                      "ceiling_if_rotation_free": 1.0 / (1.0 - rot) if rot < 1 else None}
-    f, t = out["fp32"]["cycles"], out["tf32x3"]["cycles"]
+    f = out["fp32"]["cycles"]
     print(json.dumps({
         "workload": "phases", "metric": "SM cycles per phase of the epoch kernel (CTA totals), "
         "%d tasks, D=%d, NP=%d, %d generations" % (n, DIM, POP, gens),
         "forms": out,
-        # the TC form can at most remove the FP32 form's rotation cycles
+        # a tensor-core form can at most remove the FP32 form's rotation cycles
         "tc_over_fp32_ceiling": sum(f.values()) / (sum(f.values()) - f["rotate"]),
-        "tc_over_fp32_cycles": sum(f.values()) / sum(t.values()),
+        "fp32_over_tc_cycles": {k: sum(f.values()) / sum(out[k]["cycles"].values())
+                                for k in TC_FORMS},
         "note": "measurement build: a barrier at every phase boundary"}), flush=True)
 
 
@@ -961,7 +966,8 @@ def main():
         if world > 1:
             dist.barrier()
 
-    prec = {"fp32": sgemtf.ROT_FP32, "tf32x3": sgemtf.ROT_TF32X3, "auto": sgemtf.ROT_AUTO}
+    prec = {"fp32": sgemtf.ROT_FP32, "tf32x3": sgemtf.ROT_TF32X3, "bf16x3": sgemtf.ROT_BF16X3,
+            "auto": sgemtf.ROT_AUTO}
     n, gens = args.tasks, args.gens
     fids = task_specs(n, rank)
     stream = torch.cuda.current_stream()
@@ -992,7 +998,7 @@ def main():
 
     evals_per_step = n * POP * (gens + 1)
     results = {}
-    for name in (["fp32", "tf32x3"] if args.precision == "auto" else [args.precision]):
+    for name in (["fp32", "tf32x3", "bf16x3"] if args.precision == "auto" else [args.precision]):
         try:
             eng = make_engine(prec[name])
         except sgemtf.EngineError as e:
@@ -1026,7 +1032,7 @@ def main():
     # headline: the faster of the forms that ran (both give identical
     # populations, checked below; both are reported under "forms")
     x0 = results.pop("x0")
-    ran = [k for k, v in results.items() if k == "fp32" or v["precision_used"] == 1]
+    ran = [k for k, v in results.items() if v["precision_used"] == prec[k]]
     head = min(ran, key=lambda k: results[k]["dev_ms"])
     r = results[head]
     total_evals = evals_per_step * args.steps * world

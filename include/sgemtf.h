@@ -78,12 +78,19 @@ typedef enum emt_algorithm {
 /* Arithmetic of the rotation z = Q (x - o) behind every evaluation. */
 typedef enum emt_precision {
   EMT_ROT_FP32 = 0,   /* FP32 FMA on CUDA cores                          */
-  EMT_ROT_TF32X3 = 1, /* tcgen05 tensor cores, hi/lo TF32 split of both
-                         operands (both parts rounded to nearest), FP32
-                         accumulation in tensor memory: hi.hi in one
+  EMT_ROT_TF32X3 = 1, /* tcgen05 tensor cores, kind::tf32: hi/lo TF32 split
+                         of both operands (both parts rounded to nearest),
+                         FP32 accumulation in tensor memory: hi.hi in one
                          accumulator, hi.lo + lo.hi + lo.lo in a second,
                          added in FP32                                     */
-  EMT_ROT_AUTO = 2    /* the fastest form the device supports            */
+  EMT_ROT_AUTO = 2,   /* the tensor-core form when the device and the
+                         islands allow it (BF16X3), else FP32              */
+  EMT_ROT_BF16X3 = 3  /* tcgen05 tensor cores, kind::f16: each operand split
+                         exactly into three BF16 parts (x = x0 + x1 + x2), all
+                         nine products of parts, so every product is exact;
+                         x0.y0 in one FP32 tensor-memory accumulator, the
+                         other eight in a second.  Islands of D <= 128; a
+                         large-island handle runs TF32X3 instead            */
 } emt_precision;
 
 typedef enum emt_function {

@@ -6,6 +6,7 @@
  * explicit fmaf() here and the file is compiled with -ffp-contract=off, so
  * trial vectors agree with the device bit for bit on x86 and on Arm.
  */
+#define __STDC_WANT_IEC_60559_TYPES_EXT__ 1
 #include "emt_oracle.h"
 
 #include <math.h>
@@ -272,6 +273,111 @@ static double fvalue64(int fid, uint32_t flags, int D, const double* z, double* 
   }
   if (scale) *scale = s;
   return f;
+}
+
+/* ------------------------------------------------------------------ */
+/* _Float128 evaluation: the replay's arbiter of near ties              */
+/* ------------------------------------------------------------------ */
+/* Near its optimum a function value can be the small difference of large
+ * terms (Ackley: 20 + e - 20 exp(-0.2 r) - exp(B / D); Schwefel:
+ * 418.9829 D - sum z sin sqrt|z|), so two FP64 evaluations may tie although
+ * the exact values differ (observed: Ackley, f = 3.1e-6, exact gap 2.7e-15,
+ * FP64 gap 0).  The replay's decision is the exact one: FP64 values decide
+ * when they differ by more than 1e-10 of the scale (every FP64 form here
+ * is far more accurate than that), and IEEE binary128 evaluations (113-bit
+ * significand; the rotation's FP32 x FP32 products are exact in it; glibc's
+ * *f128 functions) decide the rest. */
+typedef _Float128 q128;
+static const q128 kPiQ = 3.14159265358979323846264338327950288q;
+
+static void rotate128(const orc_task* t, const float* x, q128* z) {
+  int D = t->D;
+  for (int n = 0; n < D; ++n) {
+    if (!t->Q) { z[n] = (q128)x[n] - (q128)t->o[n]; continue; }
+    q128 acc = 0;
+    for (int k = 0; k < D; ++k)
+      acc += (q128)t->Q[(size_t)n * D + k] * ((q128)x[k] - (q128)t->o[k]);
+    z[n] = acc;
+  }
+}
+
+static q128 cospi128(q128 x) {
+  q128 r = fmodf128(fabsf128(x), 2); /* exact */
+  if (r > 1) r = 2 - r;
+  return cosf128(kPiQ * r);
+}
+
+static q128 fvalue128(int fid, uint32_t flags, int D, const q128* z) {
+  q128 f = 0;
+  switch (fid) {
+    case ORC_SPHERE:
+      for (int j = 0; j < D; ++j) f += z[j] * z[j];
+      break;
+    case ORC_RASTRIGIN:
+      for (int j = 0; j < D; ++j) f += z[j] * z[j] - 10 * cospi128(2 * z[j]) + 10;
+      break;
+    case ORC_ACKLEY: {
+      q128 a = 0, b = 0;
+      for (int j = 0; j < D; ++j) { a += z[j] * z[j]; b += cospi128(2 * z[j]); }
+      q128 e = (flags & ORC_FLAG_REF_ACKLEY_E) ? (q128)2.718282 : expf128(1);
+      f = -20 * expf128(-(q128)0.2q * sqrtf128(a / D)) - expf128(b / D) + 20 + e;
+      break;
+    }
+    case ORC_GRIEWANK: {
+      q128 a = 0, p = 1;
+      for (int j = 0; j < D; ++j) {
+        a += z[j] * z[j];
+        if (!(flags & ORC_FLAG_REF_GRIEWANK_NO_PRODUCT)) p *= cosf128(z[j] / sqrtf128((q128)(j + 1)));
+      }
+      f = 1 + a / 4000 - p;
+      break;
+    }
+    case ORC_ROSENBROCK:
+      for (int j = 0; j + 1 < D; ++j) {
+        q128 a = z[j] * z[j] - z[j + 1], b = z[j] - 1;
+        f += 100 * a * a + b * b;
+      }
+      break;
+    case ORC_SCHWEFEL: {
+      q128 a = 0;
+      for (int j = 0; j < D; ++j) a += z[j] * sinf128(sqrtf128(fabsf128(z[j])));
+      f = (q128)418.9829 * D - a;
+      break;
+    }
+    case ORC_WEIERSTRASS: {
+      for (int j = 0; j < D; ++j) {
+        q128 ak = 1, bk = 1;
+        for (int k = 0; k <= 20; ++k) {
+          f += ak * cospi128(2 * bk * (z[j] + (q128)0.5q));
+          ak *= (q128)0.5q;
+          bk *= 3;
+        }
+      }
+      f += (q128)weier_offset(flags, D);
+      break;
+    }
+    default:
+      f = NAN;
+  }
+  return f;
+}
+
+static q128 eval128(const orc_task* t, const float* x) {
+  q128 zb[1024];
+  rotate128(t, x, zb);
+  return fvalue128(t->fid, t->flags, t->D, zb);
+}
+
+/* Whether u replaces x in the replay (mode 0): f(u) <= f(x), or f(u) < f(x)
+ * when strict.  fu, fx: FP64 values; su: u's FP64 scale.  Identical vectors
+ * tie. */
+static int decide_exact(const orc_task* t, const float* u, double fu, double su,
+                        const float* x, double fx, int strict) {
+  if (memcmp(u, x, sizeof(float) * (size_t)t->D) == 0) return !strict;
+  if (!(fabs(fu - fx) <= 1e-10 * (su + fabs(fu) + fabs(fx))))
+    return strict ? fu < fx : fu <= fx;
+  const q128 qu = eval128(t, u), qx = eval128(t, x);
+  return strict ? qu < qx : qu <= qx;
 }
 
 double orc_eval64(const orc_task* t, const float* x, double* scale, double* zout) {
@@ -613,9 +719,10 @@ int orc_generation(const orc_params* p, const orc_task* t, float* X, float* fit3
     double ft64 = NAN;
     float ft32 = NAN;
     if (mode == 0) {
-      ft64 = orc_eval64(t, u, NULL, NULL);
+      double su;
+      ft64 = orc_eval64(t, u, &su, NULL);
       if (isnan(fit64[i])) fit64[i] = orc_eval64(t, xi, NULL, NULL);
-      acc = ft64 <= fit64[i];
+      acc = decide_exact(t, u, ft64, su, xi, fit64[i], 0);
     } else {
       float st, sp;
       ft32 = orc_eval32(t, u, &st);
@@ -706,9 +813,10 @@ int orc_transfer_in(const orc_params* p, const orc_task* t, const orc_task* pt,
     double f64 = NAN;
     float f32 = NAN;
     if (mode == 0) {
-      f64 = orc_eval64(t, cv, NULL, NULL);
+      double sc;
+      f64 = orc_eval64(t, cv, &sc, NULL);
       if (isnan(fit64[m])) fit64[m] = orc_eval64(t, xm, NULL, NULL);
-      acc = f64 < fit64[m];
+      acc = decide_exact(t, cv, f64, sc, xm, fit64[m], 1);
     } else {
       float sc, sm;
       f32 = orc_eval32(t, cv, &sc);
@@ -780,9 +888,10 @@ int orc_migrate(const orc_params* p, const orc_task* t, float* X, float* fit32, 
     double f64 = NAN;
     float f32 = NAN;
     if (mode == 0) {
-      f64 = orc_eval64(t, cv, NULL, NULL);
+      double sc;
+      f64 = orc_eval64(t, cv, &sc, NULL);
       if (isnan(fit64[tm])) fit64[tm] = orc_eval64(t, xm, NULL, NULL);
-      acc = f64 < fit64[tm];
+      acc = decide_exact(t, cv, f64, sc, xm, fit64[tm], 1);
     } else {
       float sc, sm;
       f32 = orc_eval32(t, cv, &sc);

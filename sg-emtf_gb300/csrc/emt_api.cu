@@ -107,6 +107,7 @@ struct emt_handle {
   int queue_grid = 1;  // persistent grid of EMT_SCHEDULE_QUEUE: SMs x resident CTAs
   // tensor-core form: Q hi/lo tiles [task][2][Np][Kp] and their TMA map
   bool use_tc = false;
+  bool tc_bf16 = false;  // exact 3 x BF16 split (else TF32 hi/lo)
   int tc_np = 0, tc_kp = 0;
   DevBuf<float> d_qtc;
   CUtensorMap tmap;
@@ -235,6 +236,20 @@ float tf32_hi(float x) {
   return r;
 }
 
+// BF16 round to nearest even (what cvt.rn.bf16.f32 computes), and back.
+uint16_t bf16_rn(float x) {
+  uint32_t b;
+  std::memcpy(&b, &x, 4);
+  b += 0x7FFFu + ((b >> 16) & 1u);
+  return (uint16_t)(b >> 16);
+}
+float bf16_value(uint16_t h) {
+  const uint32_t b = (uint32_t)h << 16;
+  float r;
+  std::memcpy(&r, &b, 4);
+  return r;
+}
+
 bool device_has_tcgen05(int device) {
   int major = 0;
   if (cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device) != cudaSuccess)
@@ -243,14 +258,15 @@ bool device_has_tcgen05(int device) {
 }
 
 // Whether every island fits the tensor-core form (NP <= 128, one 128-row MMA
-// tile; operands and state within the shared-memory limit).
-bool tc_fits(const std::vector<HostTask>& tasks, int& np, int& kp) {
+// tile; operands and state within the shared-memory limit).  np: rows of the
+// B tiles, kp: their K extent in elements.
+bool tc_fits(const std::vector<HostTask>& tasks, bool bf16, int& np, int& kp) {
   int dmax = 1;
   for (const auto& t : tasks) dmax = std::max(dmax, t.D);
-  np = emt::round16(dmax);
-  kp = emt::round32(dmax);
+  np = emt::round8(dmax);
+  kp = bf16 ? emt::round64(dmax) : emt::round32(dmax);
   for (const auto& t : tasks)
-    if (t.NP > 128 || emt::tc_layout(t.D, t.NP, np, kp).total > emt::kSmemLimit) return false;
+    if (t.NP > 128 || emt::tc_layout(t.D, t.NP, np, kp, bf16).total > emt::kSmemLimit) return false;
   return true;
 }
 
@@ -259,8 +275,9 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
-// Tensor map over the Q tiles: dims (Kp, Np, 2 * tasks) FP32, box (32, Np, 1),
-// 128-byte swizzle, i.e. one K-major B tile of one task per TMA load.
+// Tensor map over the Q tiles: dims (Kp, Np, planes * tasks), FP32 (TF32
+// parts) or BF16, box (one 128-byte row, Np, 1), 128-byte swizzle, i.e. one
+// K-major B tile of one part of one task per TMA load.
 int encode_qtc_map(emt_handle* h) {
   void* fn = nullptr;
   cudaDriverEntryPointQueryResult q;
@@ -268,12 +285,16 @@ int encode_qtc_map(emt_handle* h) {
                                                    cudaEnableDefault, &q);
   if (e != cudaSuccess || !fn || q != cudaDriverEntryPointSuccess)
     return h->fail(EMT_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  const int planes = h->tc_bf16 ? 3 : 2, esz = h->tc_bf16 ? 2 : 4;
   const cuuint64_t dims[3] = {(cuuint64_t)h->tc_kp, (cuuint64_t)h->tc_np,
-                              (cuuint64_t)(2 * h->tasks.size())};
-  const cuuint64_t strides[2] = {(cuuint64_t)h->tc_kp * 4, (cuuint64_t)h->tc_kp * h->tc_np * 4};
-  const cuuint32_t box[3] = {32, (cuuint32_t)h->tc_np, 1};
+                              (cuuint64_t)(planes * h->tasks.size())};
+  const cuuint64_t strides[2] = {(cuuint64_t)h->tc_kp * esz,
+                                 (cuuint64_t)h->tc_kp * h->tc_np * esz};
+  const cuuint32_t box[3] = {(cuuint32_t)(128 / esz), (cuuint32_t)h->tc_np, 1};
   const cuuint32_t estr[3] = {1, 1, 1};
-  CUresult r = ((EncodeTiledFn)fn)(&h->tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, h->d_qtc.p, dims,
+  CUresult r = ((EncodeTiledFn)fn)(&h->tmap, h->tc_bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
+                                                        : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                                   3, h->d_qtc.p, dims,
                                    strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                                    CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -404,28 +425,33 @@ int upload(emt_handle* h) {
     smem = std::max(smem, emt::smem_layout(ht.D, ht.NP, d.qt_in_smem != 0).total);
   }
   h->use_tc = false;
+  h->tc_bf16 = false;
   h->large = false;
   for (const auto& t : h->tasks) h->large |= t.D > emt::kMaxDim;
   if (h->large) {
     // the pipeline's work items carry the task index in 15 bits
     if (h->tasks.size() > 32767)
       return h->fail(EMT_ERR_UNSUPPORTED, "a handle with islands of D > 128 holds at most 32767 tasks");
+    // (large islands run the TF32 hi/lo GEMM for either tensor-core form)
     h->large_tc = h->cfg.precision != EMT_ROT_FP32 && device_has_tcgen05(h->device);
-    if (!h->large_tc && h->cfg.precision == EMT_ROT_TF32X3)
+    if (!h->large_tc && (h->cfg.precision == EMT_ROT_TF32X3 || h->cfg.precision == EMT_ROT_BF16X3))
       return h->fail(EMT_ERR_UNSUPPORTED, "tensor-core form needs an sm_10x device");
     smem = 0;
   } else if (h->cfg.precision != EMT_ROT_FP32) {
     int np = 0, kp = 0;
-    const bool ok = device_has_tcgen05(h->device) && tc_fits(h->tasks, np, kp);
-    if (!ok && h->cfg.precision == EMT_ROT_TF32X3)
+    const bool bf16 = h->cfg.precision != EMT_ROT_TF32X3;  // BF16X3, and AUTO's choice
+    const bool ok = device_has_tcgen05(h->device) && tc_fits(h->tasks, bf16, np, kp);
+    if (!ok && h->cfg.precision != EMT_ROT_AUTO)
       return h->fail(EMT_ERR_UNSUPPORTED, "tensor-core form needs an sm_10x device and islands "
                                           "with NP <= 128 whose tiles fit in shared memory");
     if (ok) {
       h->use_tc = true;
+      h->tc_bf16 = bf16;
       h->tc_np = np;
       h->tc_kp = kp;
       smem = 0;
-      for (const auto& t : h->tasks) smem = std::max(smem, emt::tc_layout(t.D, t.NP, np, kp).total);
+      for (const auto& t : h->tasks)
+        smem = std::max(smem, emt::tc_layout(t.D, t.NP, np, kp, bf16).total);
     }
   }
   h->smem_bytes = smem;
@@ -449,7 +475,7 @@ int upload(emt_handle* h) {
   std::map<size_t, int> occ_of;  // one occupancy query per distinct shared-memory size
   for (int t = 0; t < n && !h->large; ++t) {
     const HostTask& ht = h->tasks[t];
-    h->task_smem[t] = h->use_tc ? emt::tc_layout(ht.D, ht.NP, h->tc_np, h->tc_kp).total
+    h->task_smem[t] = h->use_tc ? emt::tc_layout(ht.D, ht.NP, h->tc_np, h->tc_kp, h->tc_bf16).total
                                 : emt::smem_layout(ht.D, ht.NP, h->table[t].qt_in_smem != 0).total;
     auto it = occ_of.find(h->task_smem[t]);
     if (it == occ_of.end())
@@ -525,22 +551,36 @@ int upload(emt_handle* h) {
       (e = cudaMemset(h->d_err.p, 0, sizeof(int32_t))))
     return h->cuda_fail(e, "upload");
   if (h->use_tc) {
-    const size_t per = (size_t)2 * h->tc_np * h->tc_kp;
-    std::vector<float> hqc(per * n, 0.f);
+    // Q's split parts, part-major per task: TF32 hi and lo (both rounded to
+    // nearest, as the A tiles are), or the exact three BF16 parts
+    const size_t plane = (size_t)h->tc_np * h->tc_kp;
+    const size_t per = (h->tc_bf16 ? 3 : 2) * plane;
+    const size_t esz = h->tc_bf16 ? sizeof(uint16_t) : sizeof(float);
+    std::vector<unsigned char> hqc(per * n * esz, 0);
     for (int t = 0; t < n; ++t) {
       const HostTask& ht = h->tasks[t];
-      float* hi = hqc.data() + per * t;
-      float* lo = hi + (size_t)h->tc_np * h->tc_kp;
       for (int r = 0; r < ht.D; ++r)
         for (int c = 0; c < ht.D; ++c) {
           const float v = ht.Q[(size_t)r * ht.D + c];
-          const float vh = tf32_hi(v);
-          hi[(size_t)r * h->tc_kp + c] = vh;
-          lo[(size_t)r * h->tc_kp + c] = tf32_hi(v - vh);  // rounded, as the A tiles are
+          const size_t at = per * t + (size_t)r * h->tc_kp + c;
+          if (h->tc_bf16) {
+            uint16_t* q = reinterpret_cast<uint16_t*>(hqc.data());
+            const uint16_t p0 = bf16_rn(v);
+            const float r1 = v - bf16_value(p0);
+            const uint16_t p1 = bf16_rn(r1);
+            q[at] = p0;
+            q[at + plane] = p1;
+            q[at + 2 * plane] = bf16_rn(r1 - bf16_value(p1));
+          } else {
+            float* q = reinterpret_cast<float*>(hqc.data());
+            const float vh = tf32_hi(v);
+            q[at] = vh;
+            q[at + plane] = tf32_hi(v - vh);
+          }
         }
     }
-    if ((e = h->d_qtc.ensure(hqc.size())) != cudaSuccess) return h->cuda_fail(e, "cudaMalloc");
-    if ((e = cudaMemcpy(h->d_qtc.p, hqc.data(), sizeof(float) * hqc.size(), cudaMemcpyHostToDevice)))
+    if ((e = h->d_qtc.ensure((hqc.size() + 3) / 4)) != cudaSuccess) return h->cuda_fail(e, "cudaMalloc");
+    if ((e = cudaMemcpy(h->d_qtc.p, hqc.data(), hqc.size(), cudaMemcpyHostToDevice)))
       return h->cuda_fail(e, "upload");
     int rc = encode_qtc_map(h);
     if (rc) return rc;
@@ -590,6 +630,7 @@ emt::EpochArgs base_args(emt_handle* h, int mode) {
   a.smem_bytes = h->smem_bytes;
   a.tc_np = h->tc_np;
   a.tc_kp = h->tc_kp;
+  a.tc_bf16 = h->tc_bf16 ? 1 : 0;
   a.subislands = h->cfg.subislands > 1 ? h->cfg.subislands : 1;
   a.mig_interval = h->cfg.migration_interval;
   a.mig_count = h->cfg.migration_count;
@@ -944,7 +985,7 @@ int emt_create(const emt_config* cfg, emt_handle_t** out) {
   if (!cfg || !out) return EMT_ERR_INVALID_ARG;
   *out = nullptr;
   if (cfg->algorithm < EMT_DE_RAND1_BIN || cfg->algorithm > EMT_GA_SBX_PM) return EMT_ERR_INVALID_ARG;
-  if (cfg->precision < EMT_ROT_FP32 || cfg->precision > EMT_ROT_AUTO) return EMT_ERR_INVALID_ARG;
+  if (cfg->precision < EMT_ROT_FP32 || cfg->precision > EMT_ROT_BF16X3) return EMT_ERR_INVALID_ARG;
   if (!(cfg->CR >= 0.f && cfg->CR <= 1.f) || !(cfg->p_c >= 0.f && cfg->p_c <= 1.f) ||
       !(cfg->eta_c >= 0.f) || !(cfg->eta_m >= 0.f) || !(cfg->p_m <= 1.f) ||
       !std::isfinite(cfg->F) || cfg->transfer_interval < 0 ||
@@ -1316,6 +1357,7 @@ int emt_sync(emt_handle_t* h) {
                                                 : code == emt::CHECK_BAD_PARTNER ? " (bad transfer partner)"
                                                 : code == emt::CHECK_TIMEOUT ? " (a bounded device wait ran out)"
                                                 : code == emt::CHECK_TC_SHAPE ? " (island outside the tensor-core form's limits)"
+                                                : code == emt::CHECK_SMEM_ALIGN ? " (shared memory not 1024-byte aligned)"
                                                                                  : ""));
     }
   }
@@ -1484,7 +1526,8 @@ int emt_get_stats(emt_handle_t* h, emt_stats* out) {
   if (!h || !out) return EMT_ERR_INVALID_ARG;
   std::memset(out, 0, sizeof(*out));
   out->n_tasks = (int32_t)h->tasks.size();
-  out->precision_used = h->use_tc ? EMT_ROT_TF32X3 : EMT_ROT_FP32;
+  out->precision_used = h->use_tc ? (h->tc_bf16 ? EMT_ROT_BF16X3 : EMT_ROT_TF32X3)
+                       : (h->large && h->large_tc) ? EMT_ROT_TF32X3 : EMT_ROT_FP32;
   if (h->d_stats.p) {
     int rc = emt_sync(h);
     if (rc) return rc;

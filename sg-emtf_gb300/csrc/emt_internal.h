@@ -87,7 +87,8 @@ struct EpochArgs {
   float* zcb;
   int32_t* err;               // first kernel-side check that fired (0 = none)
   size_t smem_bytes;          // dynamic shared memory the launch provides
-  int32_t tc_np, tc_kp;       // tensor-core form: padded N and K of the B tiles
+  int32_t tc_np, tc_kp;       // tensor-core form: padded N and K (elements) of the B tiles
+  int32_t tc_bf16;            // 1: exact 3 x BF16 split (kind::f16); 0: TF32 hi/lo
   // sub-islands: groups per island (1 = none), migration interval and count
   int32_t subislands, mig_interval, mig_count;
   int32_t* queue;  // non-null: persistent grid taking islands from this counter
@@ -183,6 +184,8 @@ struct EvalArgs {
 EMT_HD int round4(int v) { return (v + 3) & ~3; }
 EMT_HD size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
 
+constexpr size_t kQueueSlot = 16;
+
 struct Layout {
   int DP, NPP;
   size_t fit64, z64, X, U, ST, Z, QT, o, fit, tol, ftr, ttr, idx, flag, list, misc, total;
@@ -212,45 +215,54 @@ EMT_HD Layout smem_layout(int D, int NP, bool qt_in_smem = true) {
   L.flag = off;  off = align16(off + sizeof(int) * NP);
   L.list = off;  off = align16(off + sizeof(int) * NP);
   L.misc = off;  off = align16(off + sizeof(int) * 8);
-  L.total = off;
+  // the last kQueueSlot bytes of a launch's allocation: the persistent queue
+  // kernel's island slot (at the same place whatever island a CTA works on)
+  L.total = off + kQueueSlot;
   return L;
 }
 
-// Shared-memory carve-up of the tensor-core form.  The first kTcHeader bytes
-// of the dynamic shared memory hold the CTA's own tensor-core state, at the
-// same place whatever island it works on (the persistent queue kernel runs
-// many): two mbarriers (MMA completion, TMA arrival), the TMEM base and the
-// "a bounded wait gave up" flag.  Then, 1024-byte aligned, the operand tiles:
-// A = 2 (hi/lo) x nkb tiles of MA rows x 128 B, B = 2 x nkb tiles of Np
-// rows x 128 B.  With NP <= 64 the A tiles hold 64 rows and an M = 128 MMA
-// reads the next 64 rows past each tile (finite data whose output rows are
-// ignored), so B (or slack) must follow A.  The FP32 rotated rows Z alias the
-// A region once the MMAs have completed.
+// Shared-memory carve-up of the tensor-core form.  The dynamic shared memory
+// starts 1024-byte aligned (the kernel checks it) with the operand tiles,
+// `planes` split parts of each operand (TF32: hi, lo; BF16: three parts),
+// each part nkb tiles of 128-byte rows (32 TF32 or 64 BF16 values per row):
+// A = planes x nkb tiles of MA rows, B = planes x nkb tiles of Np rows.  With
+// NP <= 64 the A tiles hold 64 rows and an M = 128 MMA reads the next 64
+// rows past each tile (data whose output rows are ignored), so B (or slack)
+// must follow A.  B holds Np = round8(D) rows of Q: an MMA of N = round16(D)
+// columns reads up to 8 rows past a part, whose output columns (>= D) are
+// never used.  The FP32 rotated rows Z alias the A region once the MMAs have
+// completed.  The last kTcHeader bytes of the launch's allocation hold the
+// CTA's own tensor-core state, at the same place whatever island it works on
+// (the persistent queue kernel runs many): two mbarriers (MMA completion, TMA
+// arrival), the TMEM base and the "a bounded wait gave up" flag.
 constexpr size_t kTcHeader = 64;
 struct TcHeader {
   uint64_t mma_bar, tma_bar;
   uint32_t tmem;
   int32_t dead;
+  int32_t item;  // the persistent queue kernel's current island
 };
 static_assert(sizeof(TcHeader) <= kTcHeader, "tensor-core header");
 
 struct TcLayout {
-  int DP, Np, Kp, nkb, MA;
+  int DP, Np, Kp, nkb, MA, planes, epr;
   size_t A, B, fit64, z64, X, U, o, fit, tol, ftr, ttr, idx, flag, list, misc, total;
 };
 
-EMT_HD TcLayout tc_layout(int D, int NP, int Np, int Kp) {
+EMT_HD TcLayout tc_layout(int D, int NP, int Np, int Kp, bool bf16) {
   TcLayout L;
   L.DP = round4(D);
   L.Np = Np;
   L.Kp = Kp;
-  L.nkb = Kp / 32;
+  L.planes = bf16 ? 3 : 2;
+  L.epr = bf16 ? 64 : 32;
+  L.nkb = Kp / L.epr;
   L.MA = NP <= 64 ? 64 : 128;
   size_t off = 0;
   L.A = off;
-  off += (size_t)2 * L.nkb * L.MA * 128;
+  off += (size_t)L.planes * L.nkb * L.MA * 128;
   L.B = off;
-  const size_t bsz = (size_t)2 * L.nkb * Np * 128, slack = (size_t)(128 - L.MA) * 128;
+  const size_t bsz = (size_t)L.planes * L.nkb * Np * 128, slack = (size_t)(128 - L.MA) * 128;
   off += bsz > slack ? bsz : slack;
   L.fit64 = off; off = align16(off + sizeof(double) * NP);
   // FP64 re-check scratch: idle A-region space past Z (the re-checks run
@@ -274,13 +286,14 @@ EMT_HD TcLayout tc_layout(int D, int NP, int Np, int Kp) {
   L.flag = off;  off = align16(off + sizeof(int) * NP);
   L.list = off;  off = align16(off + sizeof(int) * NP);
   L.misc = off;  off = align16(off + sizeof(int) * 8);
-  // the header, then up to 1023 bytes to the 1024-byte aligned base
-  L.total = off + kTcHeader + 1024;
+  L.total = off + kTcHeader;  // the header closes the allocation
   return L;
 }
 
+EMT_HD int round8(int v) { return (v + 7) & ~7; }
 EMT_HD int round16(int v) { return (v + 15) & ~15; }
 EMT_HD int round32(int v) { return (v + 31) & ~31; }
+EMT_HD int round64(int v) { return (v + 63) & ~63; }
 
 // Error codes written to EpochArgs::err by the kernels' own checks.
 enum DeviceCheck : int32_t {
@@ -289,7 +302,8 @@ enum DeviceCheck : int32_t {
   CHECK_SMEM_TOO_SMALL = 2,
   CHECK_BAD_PARTNER = 3,
   CHECK_TIMEOUT = 4,      // a bounded mbarrier wait gave up
-  CHECK_TC_SHAPE = 5      // island outside the tensor-core form's limits
+  CHECK_TC_SHAPE = 5,     // island outside the tensor-core form's limits
+  CHECK_SMEM_ALIGN = 6    // dynamic shared memory not 1024-byte aligned (tensor-core form)
 };
 
 // Arguments of the best-member kernel (popSort + messageTransfer,

@@ -81,6 +81,8 @@ struct Smem {
   uint32_t a_saddr, b_saddr, mma_bar, tma_bar, tmem;
   uint32_t acc2;  // TMEM column offset of the second accumulator
   int MA, nkb, Np, N, ksteps;
+  int planes;     // split parts per operand: 2 (TF32 hi/lo) or 3 (BF16)
+  bool bf16;      // exact 3 x BF16 split, kind::f16 MMAs
   uint32_t idesc;
   int* dead;         // CTA-wide: a bounded wait gave up (the MMAs are skipped)
   uint64_t wait_ns;  // limit of each bounded wait
@@ -124,6 +126,8 @@ __device__ __forceinline__ Smem carve_tc(unsigned char* base, const TcLayout& L)
   s.a_saddr = tc::smem_addr(s.A);
   s.b_saddr = tc::smem_addr(s.B);
   s.MA = L.MA;
+  s.planes = L.planes;
+  s.bf16 = L.planes == 3;
   s.nkb = L.nkb;
   s.Np = L.Np;
   return s;
@@ -198,41 +202,67 @@ __device__ void rotate_f32(const Smem& s, int D, int DP, int NPP, int nrows) {
 }
 
 // Stores the rotation input s = x_j - o_j of row i: FP32 form into ST[j][i];
-// tensor-core form as a TF32 hi/lo pair into the swizzled A tiles
-// (hi = round-to-nearest TF32 of s, lo = round-to-nearest TF32 of s - hi, so
-// s = hi + lo + r with |r| <= 2^-22 |s| and r unbiased; a lo left for the
-// tensor core to truncate would carry a one-signed error that grows linearly
-// over K).
+// tensor-core form as its split parts in the swizzled A tiles:
+//   TF32: hi = round-to-nearest TF32 of s, lo = round-to-nearest TF32 of
+//         s - hi, so s = hi + lo + r with |r| <= 2^-22 |s| and r unbiased (a
+//         lo left for the tensor core to truncate would carry a one-signed
+//         error that grows linearly over K);
+//   BF16: three round-to-nearest BF16 parts with s = p0 + p1 + p2 exactly.
 template <bool TC>
 __device__ __forceinline__ void stage(const Smem& s, int i, int j, float v, int NPP) {
   if constexpr (TC) {
-    const float hi = tc::tf32_round(v);
-    const float lo = tc::tf32_round(v - hi);
-    const uint32_t off = tc::sw128_offset(i, j & 31);
-    unsigned char* t = s.A + (size_t)((j >> 5) * 2) * s.MA * 128;
-    *reinterpret_cast<float*>(t + off) = hi;
-    *reinterpret_cast<float*>(t + (size_t)s.MA * 128 + off) = lo;
+    if (s.bf16) {
+      uint32_t p0, p1, p2;
+      tc::split3_bf16x2(v, 0.f, p0, p1, p2);
+      const uint32_t off = tc::sw128_offset_b16(i, j & 63);
+      unsigned char* t = s.A + (size_t)((j >> 6) * 3) * s.MA * 128 + off;
+      const size_t pl = (size_t)s.MA * 128;
+      *reinterpret_cast<uint16_t*>(t) = (uint16_t)p0;
+      *reinterpret_cast<uint16_t*>(t + pl) = (uint16_t)p1;
+      *reinterpret_cast<uint16_t*>(t + 2 * pl) = (uint16_t)p2;
+    } else {
+      const float hi = tc::tf32_round(v);
+      const float lo = tc::tf32_round(v - hi);
+      const uint32_t off = tc::sw128_offset(i, j & 31);
+      unsigned char* t = s.A + (size_t)((j >> 5) * 2) * s.MA * 128;
+      *reinterpret_cast<float*>(t + off) = hi;
+      *reinterpret_cast<float*>(t + (size_t)s.MA * 128 + off) = lo;
+    }
   } else {
     s.ST[j * NPP + i] = v;
   }
 }
 
-// Four consecutive inputs s_{4b..4b+3} of row i (zeros beyond D).  In the
-// tensor-core form they fill one 16-byte chunk of the swizzled tile, so a
+// Four consecutive inputs s_{4b..4b+3} of row i (zeros beyond D).  TF32:
+// they fill one 16-byte chunk of each part's swizzled tile, so a
 // quarter-warp on 8 consecutive rows writes 8 distinct chunks (no bank
-// conflicts).
+// conflicts).  BF16: half a chunk of each part; item_ib below hands a
+// half-warp 8 rows x 2 neighbouring blocks, which covers the 32 banks once.
 template <bool TC>
 __device__ __forceinline__ void stage4(const Smem& s, int i, int b, float4 v, int NPP) {
   if constexpr (TC) {
-    float4 hi, lo;
-    hi.x = tc::tf32_round(v.x); lo.x = tc::tf32_round(v.x - hi.x);
-    hi.y = tc::tf32_round(v.y); lo.y = tc::tf32_round(v.y - hi.y);
-    hi.z = tc::tf32_round(v.z); lo.z = tc::tf32_round(v.z - hi.z);
-    hi.w = tc::tf32_round(v.w); lo.w = tc::tf32_round(v.w - hi.w);
-    const uint32_t off = (uint32_t)((i >> 3) * 1024 + (i & 7) * 128 + (((b & 7) ^ (i & 7)) << 4));
-    unsigned char* t = s.A + (size_t)((b >> 3) * 2) * s.MA * 128 + off;
-    *reinterpret_cast<float4*>(t) = hi;
-    *reinterpret_cast<float4*>(t + (size_t)s.MA * 128) = lo;
+    if (s.bf16) {
+      uint2 p0, p1, p2;
+      tc::split3_bf16x2(v.x, v.y, p0.x, p1.x, p2.x);
+      tc::split3_bf16x2(v.z, v.w, p0.y, p1.y, p2.y);
+      const uint32_t off = (uint32_t)((i >> 3) * 1024 + (i & 7) * 128 +
+                                      ((((b >> 1) & 7) ^ (i & 7)) << 4) + ((b & 1) << 3));
+      unsigned char* t = s.A + (size_t)((b >> 4) * 3) * s.MA * 128 + off;
+      const size_t pl = (size_t)s.MA * 128;
+      *reinterpret_cast<uint2*>(t) = p0;
+      *reinterpret_cast<uint2*>(t + pl) = p1;
+      *reinterpret_cast<uint2*>(t + 2 * pl) = p2;
+    } else {
+      float4 hi, lo;
+      hi.x = tc::tf32_round(v.x); lo.x = tc::tf32_round(v.x - hi.x);
+      hi.y = tc::tf32_round(v.y); lo.y = tc::tf32_round(v.y - hi.y);
+      hi.z = tc::tf32_round(v.z); lo.z = tc::tf32_round(v.z - hi.z);
+      hi.w = tc::tf32_round(v.w); lo.w = tc::tf32_round(v.w - hi.w);
+      const uint32_t off = (uint32_t)((i >> 3) * 1024 + (i & 7) * 128 + (((b & 7) ^ (i & 7)) << 4));
+      unsigned char* t = s.A + (size_t)((b >> 3) * 2) * s.MA * 128 + off;
+      *reinterpret_cast<float4*>(t) = hi;
+      *reinterpret_cast<float4*>(t + (size_t)s.MA * 128) = lo;
+    }
   } else {
     s.ST[(4 * b + 0) * NPP + i] = v.x;
     s.ST[(4 * b + 1) * NPP + i] = v.y;
@@ -241,86 +271,152 @@ __device__ __forceinline__ void stage4(const Smem& s, int i, int b, float4 v, in
   }
 }
 
+// Work item `it` of a loop over (row i < nrows, 4-gene block b < nb): row
+// fastest (consecutive threads on consecutive rows), or, for the BF16
+// staging, 16 consecutive items on 8 rows x 2 neighbouring blocks.  Returns
+// false for the padding items of the BF16 order.  The order of the items
+// changes nothing but which thread does which.
+__device__ __forceinline__ bool item_ib(int it, int nrows, int nb, bool pairs, int& i, int& b) {
+  if (!pairs) {
+    b = it / nrows;
+    i = it - b * nrows;
+    return true;
+  }
+  const int r8 = (nrows + 7) >> 3, g = it >> 4, l = it & 15;
+  const int bp = g / r8, ro = g - bp * r8;
+  i = 8 * ro + (l & 7);
+  b = 2 * bp + (l >> 3);
+  return i < nrows && b < nb;
+}
+
+__device__ __forceinline__ int items_ib(int nrows, int nb, bool pairs) {
+  return pairs ? ((nrows + 7) >> 3) * ((nb + 1) >> 1) * 16 : nrows * nb;
+}
+
+// 4-gene blocks a staging loop covers: the row's DP / 4, and in the
+// tensor-core form every block up to the operand tiles' K extent, so that
+// the pad columns [D, Kp) are written (as zeros) with the rest of the row.
+template <bool TC>
+__device__ __forceinline__ int staged_blocks(const Smem& s, int DP) {
+  if constexpr (TC) return (s.nkb * (s.bf16 ? 64 : 32)) >> 2;
+  return DP >> 2;
+}
+
 template <bool TC>
 __device__ void stage_differences(const Smem& s, const float* rows, int nrows, int D, int DP,
                                   int NPP) {
-  const int nb = DP >> 2;
-  for (int it = threadIdx.x; it < nrows * nb; it += kThreads) {
-    const int b = it / nrows, i = it - b * nrows;
-    const float4 x = reinterpret_cast<const float4*>(rows + i * DP)[b];
-    const float4 o = reinterpret_cast<const float4*>(s.o)[b];
-    float4 v;
-    v.x = 4 * b + 0 < D ? fsub(x.x, o.x) : 0.f;
-    v.y = 4 * b + 1 < D ? fsub(x.y, o.y) : 0.f;
-    v.z = 4 * b + 2 < D ? fsub(x.z, o.z) : 0.f;
-    v.w = 4 * b + 3 < D ? fsub(x.w, o.w) : 0.f;
+  const int nb = staged_blocks<TC>(s, DP), nbx = DP >> 2;
+  const bool pairs = TC && s.bf16;
+  const int nit = items_ib(nrows, nb, pairs);
+  for (int it = threadIdx.x; it < nit; it += kThreads) {
+    int i, b;
+    if (!item_ib(it, nrows, nb, pairs, i, b)) continue;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (b < nbx) {
+      const float4 x = reinterpret_cast<const float4*>(rows + i * DP)[b];
+      const float4 o = reinterpret_cast<const float4*>(s.o)[b];
+      v.x = 4 * b + 0 < D ? fsub(x.x, o.x) : 0.f;
+      v.y = 4 * b + 1 < D ? fsub(x.y, o.y) : 0.f;
+      v.z = 4 * b + 2 < D ? fsub(x.z, o.z) : 0.f;
+      v.w = 4 * b + 3 < D ? fsub(x.w, o.w) : 0.f;
+    }
     stage4<TC>(s, i, b, v, NPP);
   }
 }
 
-// Tensor-core rotation of rows [0, nrows): four tcgen05 MMA passes over the
-// K steps that cover D, one issuing thread, completion on an mbarrier.  hi.hi
-// accumulates alone in the first accumulator; hi.lo + lo.hi + lo.lo (each
-// about 2^-11 of it) in the second, so the large partial sums of hi.hi do
-// not swallow the small products (each MMA step rounds its accumulator to
-// FP32).  Warps 0-3 then drain both accumulators (TMEM lane = row), add them
-// in FP32 and store Z.  phase: the mbarrier parity this CTA expects next.
-__device__ void rotate_tc(const Smem& s, int D, int DP, int nrows, uint32_t& phase) {
-  // Columns [D, Kp) of every staged row must hold finite values (they meet
-  // the zero columns of Q): the FP64 re-check scratch shares this region, so
-  // clear them here, whatever path staged the row.
-  const int kp = s.nkb * 32, npad = kp - D;
+// Zeros in the pad columns [D, Kp) of the tensor-core operand rows [0,
+// nrows), for the staging paths that write gene by gene (the GA trials).
+// The columns must hold finite values: they meet Q's zero columns, and the
+// rotated rows and the re-check scratch alias this region between
+// rotations.
+__device__ void zero_pads(const Smem& s, int D, int nrows) {
+  const int epr = s.bf16 ? 64 : 32;
+  const int kp = s.nkb * epr, npad = kp - D;
+  const size_t pl = (size_t)s.MA * 128;
   for (int it = threadIdx.x; it < nrows * npad; it += kThreads) {
     const int i = it / npad, j = D + (it - i * npad);
-    const uint32_t off = tc::sw128_offset(i, j & 31);
-    unsigned char* t = s.A + (size_t)((j >> 5) * 2) * s.MA * 128;
-    *reinterpret_cast<float*>(t + off) = 0.f;
-    *reinterpret_cast<float*>(t + (size_t)s.MA * 128 + off) = 0.f;
+    if (s.bf16) {
+      unsigned char* t = s.A + (size_t)((j >> 6) * 3) * pl + tc::sw128_offset_b16(i, j & 63);
+      *reinterpret_cast<uint16_t*>(t) = 0;
+      *reinterpret_cast<uint16_t*>(t + pl) = 0;
+      *reinterpret_cast<uint16_t*>(t + 2 * pl) = 0;
+    } else {
+      unsigned char* t = s.A + (size_t)((j >> 5) * 2) * pl + tc::sw128_offset(i, j & 31);
+      *reinterpret_cast<float*>(t) = 0.f;
+      *reinterpret_cast<float*>(t + pl) = 0.f;
+    }
   }
+}
+
+// Tensor-core rotation of rows [0, nrows) staged with their pad columns:
+// tcgen05 MMAs over the K steps that cover D (32 bytes of each 128-byte row
+// per step: 8 TF32 or 16 BF16 values), one issuing thread, completion on an
+// mbarrier that warp 0 waits for while the other warps wait at the CTA
+// barrier.  The product of the two leading parts accumulates alone in the
+// first accumulator; every other product of parts (TF32: hi.lo, lo.hi,
+// lo.lo; BF16: the other eight of the nine, so every product of the exact
+// splits is taken) in the second, so the large partial sums do not swallow
+// the small products (each MMA step rounds its accumulator to FP32).  Then
+// the warps drain both accumulators (TMEM lane = row; warp w reads lanes
+// 32 (w mod 4) on, its half of the columns), add them in FP32 and store Z.
+// phase: the mbarrier parity this CTA expects next.
+__device__ void rotate_tc(const Smem& s, int D, int DP, int nrows, uint32_t& phase) {
   tc::fence_async_smem();  // generic-proxy operand writes -> async proxy
   __syncthreads();
   const bool dead = *s.dead != 0;  // an earlier wait gave up: skip the MMAs
   if (threadIdx.x == 0 && !dead && !s.lose_completion) {
     tc::fence_after();
-    const int pa[4] = {0, 0, 1, 1}, pb[4] = {0, 1, 0, 1};
-    for (int p = 0; p < 4; ++p) {
+    // products of parts (a, b): the leading one first, alone in accumulator 0
+    const int pa[9] = {0, 0, 1, 1, 0, 2, 1, 2, 2}, pb[9] = {0, 1, 0, 1, 2, 0, 2, 1, 2};
+    const int nprod = s.bf16 ? 9 : 4;
+    // descriptors: the start address field (bits 0-13, address >> 4) of the
+    // tiles' base descriptors plus each step's offset >> 4 (no carry: shared
+    // addresses stay below 256 KB)
+    const uint64_t a0 = tc::sdesc_sw128(s.a_saddr), b0 = tc::sdesc_sw128(s.b_saddr);
+    const uint32_t atile = (uint32_t)s.MA * 8u, btile = (uint32_t)s.Np * 8u;  // (rows x 128 B) >> 4
+    for (int p = 0; p < nprod; ++p) {
       const uint32_t d = s.tmem + (p ? s.acc2 : 0u);
       for (int st = 0; st < s.ksteps; ++st) {
-        const int kb = st >> 2, ks = st & 3;
-        const uint64_t ad =
-            tc::sdesc_sw128(s.a_saddr + (uint32_t)((kb * 2 + pa[p]) * s.MA * 128 + ks * 32));
-        const uint64_t bd =
-            tc::sdesc_sw128(s.b_saddr + (uint32_t)((pb[p] * s.nkb + kb) * s.Np * 128 + ks * 32));
-        tc::mma_tf32(d, ad, bd, s.idesc, (st > 0 || p > 1) ? 1u : 0u);
+        const uint32_t kb = (uint32_t)st >> 2, ks = (uint32_t)st & 3u;
+        const uint64_t ad = a0 + ((kb * (uint32_t)s.planes + (uint32_t)pa[p]) * atile + 2u * ks);
+        const uint64_t bd = b0 + (((uint32_t)pb[p] * (uint32_t)s.nkb + kb) * btile + 2u * ks);
+        const uint32_t acc = (st > 0 || p > 1) ? 1u : 0u;
+        if (s.bf16)
+          tc::mma_bf16(d, ad, bd, s.idesc, acc);
+        else
+          tc::mma_tf32(d, ad, bd, s.idesc, acc);
       }
     }
     tc::mma_commit(s.mma_bar);
   }
-  if (!dead) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (!dead && warp == 0) {
     if (!tc::mbar_wait(s.mma_bar, phase, s.wait_ns)) atomicExch(s.dead, 1);
-    phase ^= 1u;
   }
+  if (!dead) phase ^= 1u;
   __syncthreads();
   tc::fence_after();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (*s.dead) {
     // no valid accumulator: finite zeros, and the epoch stops at the end of
     // this generation with CHECK_TIMEOUT reported
     for (int it = threadIdx.x; it < nrows * DP; it += kThreads) s.Z[it] = 0.f;
-  } else if (warp < 4 && 32 * warp < nrows) {  // warp-uniform: the loads are .sync.aligned
-    const int row = 32 * warp + lane;
-    for (int c0 = 0; c0 < s.N; c0 += 16) {
+  } else if (32 * (warp & 3) < nrows) {  // warp-uniform: the loads are .sync.aligned
+    const int q = warp & 3, row = 32 * q + lane;
+    const int nch = s.N >> 4, half = (nch + 1) >> 1;
+    const int c_lo = (warp >> 2) ? half : 0, c_hi = (warp >> 2) ? nch : half;
+    for (int c = c_lo; c < c_hi; ++c) {
+      const int c0 = 16 * c;
       float v[16], w[16];
-      tc::tmem_ld16(s.tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, v);
-      tc::tmem_ld16(s.tmem + ((uint32_t)(32 * warp) << 16) + s.acc2 + (uint32_t)c0, w);
+      tc::tmem_ld16(s.tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, v);
+      tc::tmem_ld16(s.tmem + ((uint32_t)(32 * q) << 16) + s.acc2 + (uint32_t)c0, w);
 #pragma unroll
       for (int g = 0; g < 16; ++g) v[g] = __fadd_rn(v[g], w[g]);
       if (row < nrows)
 #pragma unroll
-        for (int q = 0; q < 4; ++q)
-          if (c0 + 4 * q < DP)
-            reinterpret_cast<float4*>(s.Z + row * DP)[(c0 >> 2) + q] =
-                make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+        for (int g = 0; g < 4; ++g)
+          if (c0 + 4 * g < DP)
+            reinterpret_cast<float4*>(s.Z + row * DP)[(c0 >> 2) + g] =
+                make_float4(v[4 * g], v[4 * g + 1], v[4 * g + 2], v[4 * g + 3]);
     }
   }
   tc::fence_before();
@@ -364,9 +460,16 @@ __device__ void build_trials(const Smem& s, const EpochArgs& a, const TaskDev& t
       s.idx[4 * i + 3] = jr;
     }
     __syncthreads();
-    const int nb = (D + 3) >> 2;
-    for (int it = threadIdx.x; it < NP * nb; it += kThreads) {
-      const int b = it / NP, i = it - b * NP;
+    const int nbd = (D + 3) >> 2, nb = TC ? staged_blocks<TC>(s, DP) : nbd;
+    const bool pairs = TC && s.bf16;
+    const int nit = items_ib(NP, nb, pairs);
+    for (int it = threadIdx.x; it < nit; it += kThreads) {
+      int i, b;
+      if (!item_ib(it, NP, nb, pairs, i, b)) continue;
+      if (TC && b >= nbd) {  // pad columns of the operand only
+        stage4<TC>(s, i, b, make_float4(0.f, 0.f, 0.f, 0.f), NPP);
+        continue;
+      }
       const U4 w = draw(a.seed, (uint32_t)task, G, (uint32_t)i, P_DE_CR, (uint32_t)b);
       const int base = s.idx[4 * i], r2 = s.idx[4 * i + 1], r3 = s.idx[4 * i + 2],
                 jr = s.idx[4 * i + 3];
@@ -447,6 +550,7 @@ __device__ void build_trials(const Smem& s, const EpochArgs& a, const TaskDev& t
       stage<TC>(s, i, j, fsub(c, s.o[j]), NPP);
     }
   }
+  if constexpr (TC) zero_pads(s, D, NP);
 }
 
 // Selection of nrows candidates (rows of U, fitness ftr/ttr) against members
@@ -691,18 +795,16 @@ __device__ __forceinline__ void epoch_body(const EpochArgs& a, const void* tmap,
   Smem s;
   int DP, NPP;
   if constexpr (TC) {
-    if (NP > 128 || round16(D) > a.tc_np || round32(D) > a.tc_kp) {
+    if (NP > 128 || round8(D) > a.tc_np || (a.tc_bf16 ? round64(D) : round32(D)) > a.tc_kp) {
       if (threadIdx.x == 0) report(a.err, CHECK_TC_SHAPE);
       return;
     }
-    const TcLayout L = tc_layout(D, NP, a.tc_np, a.tc_kp);
+    const TcLayout L = tc_layout(D, NP, a.tc_np, a.tc_kp, a.tc_bf16 != 0);
     if (L.total > a.smem_bytes) {
       if (threadIdx.x == 0) report(a.err, CHECK_SMEM_TOO_SMALL);
       return;
     }
-    unsigned char* base =
-        (unsigned char*)(((uintptr_t)smem_raw + kTcHeader + 1023) & ~(uintptr_t)1023);
-    s = carve_tc(base, L);
+    s = carve_tc(smem_raw, L);
     s.mma_bar = cta.mma_bar;
     s.tma_bar = cta.tma_bar;
     s.tmem = cta.tmem;
@@ -714,8 +816,8 @@ __device__ __forceinline__ void epoch_body(const EpochArgs& a, const void* tmap,
     DP = L.DP;
     NPP = round4(NP);
     s.N = round16(D);
-    s.ksteps = (D + 7) >> 3;
-    s.idesc = tc::idesc_tf32(128, s.N);
+    s.ksteps = s.bf16 ? (D + 15) >> 4 : (D + 7) >> 3;
+    s.idesc = s.bf16 ? tc::idesc_bf16(128, s.N) : tc::idesc_tf32(128, s.N);
     // zero the operand tiles once: padded K columns meet zero Q columns, so
     // they only need to hold finite values
     for (size_t it = threadIdx.x; it < (L.B - L.A) / 16; it += kThreads)
@@ -724,11 +826,11 @@ __device__ __forceinline__ void epoch_body(const EpochArgs& a, const void* tmap,
     // into the B region, which no MMA reads any more (the previous island's
     // last MMAs completed before its selection)
     if (threadIdx.x == 0 && !*s.dead) {
-      tc::mbar_expect_tx(s.tma_bar, (uint32_t)(2 * s.nkb * s.Np * 128));
-      for (int h = 0; h < 2; ++h)
+      tc::mbar_expect_tx(s.tma_bar, (uint32_t)(s.planes * s.nkb * s.Np * 128));
+      for (int h = 0; h < s.planes; ++h)
         for (int kb = 0; kb < s.nkb; ++kb)
-          tc::tma_load_3d(s.b_saddr + (uint32_t)((h * s.nkb + kb) * s.Np * 128), tmap, 32 * kb, 0,
-                          2 * task + h, s.tma_bar);
+          tc::tma_load_3d(s.b_saddr + (uint32_t)((h * s.nkb + kb) * s.Np * 128), tmap,
+                          L.epr * kb, 0, s.planes * task + h, s.tma_bar);
     }
   } else {
     const Layout L = smem_layout(D, NP, td.qt_in_smem != 0);
@@ -795,7 +897,8 @@ __device__ __forceinline__ void epoch_body(const EpochArgs& a, const void* tmap,
   for (int it = threadIdx.x; it < NP * DP; it += kThreads) s.U[it] = 0.f;
   if constexpr (TC) {
     if (!*s.dead) {
-      if (!tc::mbar_wait(s.tma_bar, cta.tphase, s.wait_ns)) atomicExch(s.dead, 1);
+      if ((threadIdx.x >> 5) == 0 && !tc::mbar_wait(s.tma_bar, cta.tphase, s.wait_ns))
+        atomicExch(s.dead, 1);
       cta.tphase ^= 1u;
     }
   }
@@ -909,11 +1012,11 @@ __device__ __forceinline__ void epoch_body(const EpochArgs& a, const void* tmap,
 // accumulators of the rotation).
 __device__ __forceinline__ void tc_cta_begin(const EpochArgs& a, unsigned char* smem_raw,
                                              TcCta& cta) {
-  cta.hdr = reinterpret_cast<TcHeader*>(smem_raw);
+  cta.hdr = reinterpret_cast<TcHeader*>(smem_raw + a.smem_bytes - kTcHeader);
   cta.mma_bar = tc::smem_addr(&cta.hdr->mma_bar);
   cta.tma_bar = tc::smem_addr(&cta.hdr->tma_bar);
   uint32_t half = 32;
-  while (half < (uint32_t)a.tc_np) half <<= 1;
+  while (half < (uint32_t)round16(a.tc_np)) half <<= 1;
   cta.ncols = 2 * half;
   cta.mphase = cta.tphase = 0;
   if (threadIdx.x == 0) {
@@ -946,19 +1049,35 @@ template <bool TC, bool QUEUE>
 __device__ __forceinline__ void epoch_entry(const EpochArgs& a, const void* tmap,
                                             unsigned char* smem_raw) {
   TcCta cta{};
-  if constexpr (TC) tc_cta_begin(a, smem_raw, cta);
+  if constexpr (TC) {
+    // the swizzled operand tiles need 1024-byte alignment; the layout keeps
+    // no slack for it, so a launch that does not provide it stops here
+    if ((tc::smem_addr(smem_raw) & 1023u) != 0u || a.smem_bytes < kTcHeader) {
+      if (threadIdx.x == 0) report(a.err, CHECK_SMEM_ALIGN);
+      return;
+    }
+    tc_cta_begin(a, smem_raw, cta);
+  }
   if constexpr (!QUEUE) {
     epoch_body<TC>(a, tmap, smem_raw,
                    a.single_task >= 0 ? a.single_task
                                       : (a.order ? a.order[blockIdx.x] : (int)blockIdx.x),
                    cta);
   } else {
-    __shared__ int item;
+    // the island slot, in dynamic shared memory at a place no island's
+    // layout uses (the TC header; the FP32 layout's last bytes): static
+    // shared memory would push the dynamic allocation, whose alignment in
+    // this module is 1024 bytes (the TC kernels ask for it), back by 1 KB
+    int* item;
+    if constexpr (TC)
+      item = &cta.hdr->item;
+    else
+      item = reinterpret_cast<int*>(smem_raw + a.smem_bytes - kQueueSlot);
     for (;;) {
       __syncthreads();  // the previous island is written back; item is free
-      if (threadIdx.x == 0) item = atomicAdd(a.queue, 1);
+      if (threadIdx.x == 0) *item = atomicAdd(a.queue, 1);
       __syncthreads();
-      const int i = item;
+      const int i = *item;
       if (i >= a.n_tasks) break;
       if constexpr (TC) {
         if (cta.hdr->dead) break;  // written before the barrier above: CTA-uniform
@@ -979,16 +1098,17 @@ __global__ void __launch_bounds__(kThreads, 3) epoch_kernel_queue(const EpochArg
   epoch_entry<false, true>(a, nullptr, smem_raw);
 }
 
-// Tensor-core form: two islands per SM (~100 KB of operands and state each).
-__global__ void __launch_bounds__(kThreads, 2) epoch_kernel_tc(const EpochArgs a,
+// Tensor-core form: three islands per SM at D = 50, NP = 64 in the BF16
+// form (~74 KB of operands and state each).
+__global__ void __launch_bounds__(kThreads, 3) epoch_kernel_tc(const EpochArgs a,
                                                                 const __grid_constant__ CUtensorMap tmap) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  epoch_entry<true, false>(a, &tmap, smem_raw);
+  extern __shared__ __align__(1024) unsigned char smem_tc[];
+  epoch_entry<true, false>(a, &tmap, smem_tc);
 }
-__global__ void __launch_bounds__(kThreads, 2) epoch_kernel_tc_queue(
+__global__ void __launch_bounds__(kThreads, 3) epoch_kernel_tc_queue(
     const EpochArgs a, const __grid_constant__ CUtensorMap tmap) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  epoch_entry<true, true>(a, &tmap, smem_raw);
+  extern __shared__ __align__(1024) unsigned char smem_tc[];
+  epoch_entry<true, true>(a, &tmap, smem_tc);
 }
 
 // Evaluates n caller points of one task in chunks of up to 64 rows per CTA

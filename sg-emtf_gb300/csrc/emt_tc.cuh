@@ -24,6 +24,14 @@ __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
          ((uint32_t)(M >> 4) << 24);
 }
 
+// Instruction descriptor, kind::f16 with BF16 operands: D = F32 (bits 4-5 =
+// 1), A = B = BF16 (bits 7-9 = 1, bits 10-12 = 1), both K-major, N >> 3 in
+// bits 17-22, M >> 4 in bits 24-28.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
+}
+
 // Shared-memory matrix descriptor: start address >> 4 (bits 0-13), leading
 // byte offset (unused for swizzled K-major, 16 B), stride byte offset 1024 B
 // (bits 32-45), descriptor version 1 (bits 46-47), swizzle mode 128B = 2
@@ -44,6 +52,12 @@ __host__ __device__ __forceinline__ uint32_t sw128_offset(int row, int c) {
                     ((c & 3) << 2));
 }
 
+// Byte offset of 16-bit element (row, c) (c < 64) inside a 128B-swizzled tile.
+__host__ __device__ __forceinline__ uint32_t sw128_offset_b16(int row, int c) {
+  return (uint32_t)((row >> 3) * 1024 + (row & 7) * 128 + ((((c >> 3) ^ (row & 7)) & 7) << 4) +
+                    ((c & 7) << 1));
+}
+
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
@@ -60,6 +74,34 @@ __device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64
       "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
       "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
       "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+// D (+)= A B^T with BF16 operands (K = 16 per instruction), FP32 accumulator.
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                         uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+// Exact split of two FP32 values into three BF16 parts each, packed in pairs
+// (element a in the low half, b in the high half): a = a0 + a1 + a2 exactly
+// for normal FP32 a (each part is the round-to-nearest BF16 of what the
+// previous parts leave; 8 + 8 + 8 significand bits cover FP32's 24).
+__device__ __forceinline__ float bf16_lo_as_f32(uint32_t p) { return __uint_as_float(p << 16); }
+__device__ __forceinline__ float bf16_hi_as_f32(uint32_t p) { return __uint_as_float(p & 0xFFFF0000u); }
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
+  uint32_t r;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(b), "f"(a));
+  return r;
+}
+__device__ __forceinline__ void split3_bf16x2(float a, float b, uint32_t& p0, uint32_t& p1,
+                                              uint32_t& p2) {
+  p0 = pack_bf16x2(a, b);
+  const float ra = __fsub_rn(a, bf16_lo_as_f32(p0)), rb = __fsub_rn(b, bf16_hi_as_f32(p0));
+  p1 = pack_bf16x2(ra, rb);
+  p2 = pack_bf16x2(__fsub_rn(ra, bf16_lo_as_f32(p1)), __fsub_rn(rb, bf16_hi_as_f32(p1)));
 }
 
 __device__ __forceinline__ void mma_commit(uint32_t bar) {

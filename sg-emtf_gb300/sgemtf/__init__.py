@@ -23,7 +23,7 @@ PHASES_LIB_PATH = os.path.join(PKG_DIR, "_build", "libsgemtf_phases.so")
 OK, ERR_INVALID_ARG, ERR_OUT_OF_MEMORY, ERR_CUDA, ERR_DEVICE_TIMEOUT, ERR_STATE, \
     ERR_UNSUPPORTED, ERR_DEVICE_CHECK = range(8)
 DE_RAND1_BIN, DE_CURRENT1_BIN, GA_SBX_PM = range(3)
-ROT_FP32, ROT_TF32X3, ROT_AUTO = range(3)
+ROT_FP32, ROT_TF32X3, ROT_AUTO, ROT_BF16X3 = range(4)
 SPHERE, RASTRIGIN, ACKLEY, GRIEWANK, ROSENBROCK, SCHWEFEL, WEIERSTRASS = range(7)
 FUNCTION_NAMES = ["sphere", "rastrigin", "ackley", "griewank", "rosenbrock", "schwefel",
                   "weierstrass"]

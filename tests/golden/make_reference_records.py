@@ -16,17 +16,18 @@ task with task 0 forced to type 6 (SG-EMTF.cu:307-313).  Reference types are
 stored as recorded (0 Sphere, 1 Rosenbrock, 2 Ackley, 3 Rastrigin,
 4 Griewank, 5 Weierstrass, 6 Schwefel).
 
-Run here (the reference is mounted only on the build machine):
-    python tests/golden/make_reference_records.py
+Usage (wherever the reference tree is available):
+    python tests/golden/make_reference_records.py <reference root>
 """
 import ctypes
 import json
 import os
+import sys
 
 import numpy as np
 
-SRC = "/root/reference/data process/ANO_Tnum/data_record_T_ANO_100.txt"
-SRC_ANO = "/root/reference/data process/ANO_Tnum/data_record_T_ANO_100_1677482963.txt"
+REC = os.path.join("data process", "ANO_Tnum", "data_record_T_ANO_100.txt")
+REC_ANO = os.path.join("data process", "ANO_Tnum", "data_record_T_ANO_100_1677482963.txt")
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "reference_records_T100.json")
 
@@ -39,9 +40,10 @@ def reference_types(n):
     return t
 
 
-def main():
+def main(root):
+    src, src_ano = os.path.join(root, REC), os.path.join(root, REC_ANO)
     runs, cur = [], []
-    for line in open(SRC):
+    for line in open(src):
         line = line.strip()
         if not line:
             if cur:
@@ -61,7 +63,7 @@ def main():
     with open(OUT, "w") as f:
         json.dump(out, f, separators=(",", ":"))
     np.save(os.path.join(HERE, "reference_trajectories_T100.npy"), np.array(runs, np.float32))
-    ano = [v.strip() for v in open(SRC_ANO).read().split(",") if v.strip()]
+    ano = [v.strip() for v in open(src_ano).read().split(",") if v.strip()]
     with open(os.path.join(HERE, "reference_ano_T100.json"), "w") as f:
         json.dump({"source": "data process/ANO_Tnum/data_record_T_ANO_100_1677482963.txt",
                    "ano": ano}, f, indent=0)
@@ -69,4 +71,6 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: make_reference_records.py <reference root>")
+    main(sys.argv[1])

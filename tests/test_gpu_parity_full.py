@@ -4,9 +4,9 @@ selection decided in FP64 (proposed model/SG-EMTF_DE.cu:474-706 for DE,
 SG-EMTF.cu:548-831 for the GA, :1514-1591 for elite transfer).
 
 - 1000 rotated tasks of D = 50, NP = 64, DE/rand/1/bin F 0.5 CR 0.9, all 2000
-  generations, in both rotation forms: 14 of the tasks (two per function)
-  replayed from their initial populations, and the two forms' final
-  populations identical for all 1000 tasks.  Converged islands spend their
+  generations, in the three rotation forms (FP32, TF32X3, BF16X3): 14 of the
+  tasks (two per function) replayed from their initial populations, and the
+  forms' final populations identical for all 1000 tasks.  Converged islands spend their
   late generations on near ties, which is where a wrong re-check would show.
 - 8 tasks of D = 50, NP = 100, identity rotation, transfer of 10 % every 10
   generations, all 1000 generations, epoch by epoch from the device's state
@@ -42,7 +42,8 @@ def test_config2_full_length_both_forms(sgemtf, orc):
              for t in range(CONFIG2_TASKS)]
     digests, finals = {}, {}
     X0 = None
-    for prec in (sgemtf.ROT_FP32, sgemtf.ROT_TF32X3):
+    forms = (sgemtf.ROT_FP32, sgemtf.ROT_TF32X3, sgemtf.ROT_BF16X3)
+    for prec in forms:
         eng = sgemtf.Engine(sgemtf.Config(seed=1, precision=prec))
         eng.add_tasks(descs)
         eng.reset()
@@ -61,14 +62,14 @@ def test_config2_full_length_both_forms(sgemtf, orc):
         digests[prec] = _hash_populations(eng, CONFIG2_TASKS)
         finals[prec] = {t: eng.population(t)[0] for t in CONFIG2_CHECKED}
         eng.close()
-    assert digests[sgemtf.ROT_FP32] == digests[sgemtf.ROT_TF32X3]
+    assert len(set(digests.values())) == 1, digests
     # the oracle: FP64 decisions for every selection, one native thread per task
     X = [X0[t].copy() for t in CONFIG2_CHECKED]
     f64 = [np.array([tk.eval64(r)[0] for r in x]) for tk, x in zip(tasks, X)]
     f32 = [v.astype(np.float32) for v in f64]
     orc.run_threads(p, tasks, X, f32, f64, 0, CONFIG2_GENS, 0, len(tasks))
     for k, t in enumerate(CONFIG2_CHECKED):
-        for prec in (sgemtf.ROT_FP32, sgemtf.ROT_TF32X3):
+        for prec in forms:
             got = finals[prec][t]
             assert np.array_equal(got, X[k]), (prec, t, np.argwhere(got != X[k])[:5])
 

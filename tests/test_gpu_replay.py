@@ -92,7 +92,7 @@ def test_config1_shape_identity_rotation(sgemtf, orc):
         assert np.array_equal(eng.population(i)[0], want[i])
 
 
-@pytest.mark.parametrize("precision,flags", [(0, 0), (1, 0), (0, 0x40)])
+@pytest.mark.parametrize("precision,flags", [(0, 0), (1, 0), (3, 0), (0, 0x40)])
 def test_replay_converged_islands(sgemtf, orc, precision, flags):
     """Long runs of small islands converge until trial and parent differ by a
     few ulps and most selections are near-ties: every re-check path (the

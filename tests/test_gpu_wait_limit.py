@@ -17,8 +17,9 @@ def _descs(sgemtf):
     return [sgemtf.TaskDesc(f, 20, 32) for f in range(3)]
 
 
-def test_lost_completion_reports_and_context_survives(sgemtf):
-    cfg = dict(seed=4, precision=sgemtf.ROT_TF32X3)
+@pytest.mark.parametrize("precision", [3, 1])  # BF16X3, TF32X3
+def test_lost_completion_reports_and_context_survives(sgemtf, precision):
+    cfg = dict(seed=4, precision=precision)
     bad = sgemtf.Engine(sgemtf.Config(wait_limit_ms=20, flags=sgemtf.FLAG_TEST_LOST_COMPLETION,
                                       **cfg))
     bad.add_tasks(_descs(sgemtf))
@@ -37,7 +38,7 @@ def test_lost_completion_reports_and_context_survives(sgemtf):
     for eng in (good, ref):
         eng.add_tasks(_descs(sgemtf))
         eng.run(8)
-    assert good.stats()["precision_used"] == sgemtf.ROT_TF32X3
+    assert good.stats()["precision_used"] == precision
     for i in range(3):
         assert np.array_equal(good.population(i)[0], ref.population(i)[0])
 

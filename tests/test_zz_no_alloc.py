@@ -24,7 +24,7 @@ def _engine(sgemtf, seed, transfer_interval, tasks=7, D=20, NP=24):
     return eng
 
 
-@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1, 3])
 def test_noalloc_matches_run_two_calls(sgemtf, precision):
     ref = sgemtf.Engine(sgemtf.Config(seed=23, transfer_interval=5, transfer_rate=0.25,
                                       precision=precision))
