@@ -1086,6 +1086,9 @@ def main():
         "forms": {k: {"value": total_evals / (v["dev_ms"] * 1e-3), "ms_per_step": v["dev_ms"] / args.steps,
                       "epoch_kernel_ms": v["epoch_ms"],
                       "rechecks": v["stats"]["rechecks"], "recheck_flips": v["stats"]["recheck_flips"],
+                      "recheck_identical": v["stats"]["recheck_identical"],
+                      "recheck_differential": v["stats"]["recheck_differential"],
+                      "anchor_rotations": v["stats"]["anchor_rotations"],
                       "max_rel_err_vs_fp64": v["stats"]["max_rel_err"],
                       "final_populations_sha256": v["digest"],
                       "precision_used": v["precision_used"]} for k, v in results.items()},
