@@ -1089,6 +1089,7 @@ def main():
                       "recheck_identical": v["stats"]["recheck_identical"],
                       "recheck_differential": v["stats"]["recheck_differential"],
                       "anchor_rotations": v["stats"]["anchor_rotations"],
+                      "recheck_fp64_terms": v["stats"]["recheck_fp64_terms"],
                       "max_rel_err_vs_fp64": v["stats"]["max_rel_err"],
                       "final_populations_sha256": v["digest"],
                       "precision_used": v["precision_used"]} for k, v in results.items()},

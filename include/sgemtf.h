@@ -229,6 +229,9 @@ typedef struct emt_stats {
   double max_rel_err;         /* largest |f32 - f64| / scale over the tasks' best
                                  members (scale: the sum of |sub-terms| the FP32
                                  evaluation states); 0 before emt_reset        */
+  uint64_t recheck_fp64_terms; /* Weierstrass near ties whose FP32-term values
+                                  were closer than their error bound, decided
+                                  with every term in double precision         */
 } emt_stats;
 
 /* Fills *cfg with DE/rand/1/bin, F = 0.5, CR = 0.9, SBX eta 15 / p_c 0.9,

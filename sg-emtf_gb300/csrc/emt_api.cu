@@ -1542,6 +1542,7 @@ int emt_get_stats(emt_handle_t* h, emt_stats* out) {
     out->transfers_accepted = s[2];
     out->evaluations = s[3];
     out->migrations_accepted = s[7];
+    out->recheck_fp64_terms = s[emt::kStatWeierFp64];
     out->generations = h->initialized ? (uint64_t)h->gdone * h->tasks.size() : 0;
   }
   if (h->initialized && !h->tasks.empty()) {

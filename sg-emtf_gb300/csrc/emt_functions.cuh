@@ -426,6 +426,21 @@ __device__ __forceinline__ void dot2_pair(const float* __restrict__ x, const flo
   zm = (double)S1 + (double)C1;
 }
 
+// The calling team fills zbuf[0..D) with the FP64-class rotation of row x,
+// one output per member of the team at a time (the team synchronises before
+// returning).
+template <class Team>
+__device__ void precise_rotation_team(const float* __restrict__ x, const float* __restrict__ o,
+                                      const float* __restrict__ qt, int DP, int D, double* zbuf,
+                                      const Team& tm) {
+  for (int n = tm.rank(); n < D; n += tm.size()) {
+    double a, b;
+    dot2_pair(x, o, qt, DP, D, n, false, a, b);
+    zbuf[n] = a;
+  }
+  tm.sum(0.0);  // a barrier of the team
+}
+
 // The calling warp fills zbuf[0..D) with the FP64-class rotation of row x.
 __device__ __forceinline__ void precise_rotation(const float* __restrict__ x,
                                                  const float* __restrict__ o,
@@ -671,6 +686,64 @@ __device__ double eval_weier_precise_t(const FnConst& fc, const double* zbuf, co
 }
 __device__ double eval_weier_precise(const FnConst& fc, const double* zbuf) {
   return eval_weier_precise_t(fc, zbuf, WarpTeam{});
+}
+
+// Largest error of an eval_weier_precise value, per gene: each term's
+// argument y_k = 2 3^k |z| mod 2 reaches cospif as a 24-bit float after the
+// low bits are cut (< 2^-24) and the 25-bit rest rounded (<= 2^-24), so
+// |dy| < 2^-23 and the term moves by < pi 2^-23; cospif adds <= 1 ulp
+// (<= 2^-24 for |cos| <= 1); times 0.5^k summed over k (< 2) that is
+// < 8.7e-7, and the compensated sum of 21 terms adds < 2 u sum |terms|
+// (< 2.4e-7).  Over D genes: D x 1.2e-6.  Near ties closer than twice this
+// are decided by eval_weier_fp64 instead.
+__device__ __forceinline__ double weier_precise_bound(int D) { return 1.2e-6 * (double)D; }
+
+// One Weierstrass gene with every term in double precision: the same exact
+// reduction of y_k = 2 3^k |z| mod 2 as weier_gene_precise, then the reduced
+// argument (53 bits) through the double-precision cospi.  FP64 pipe: only
+// for the near ties the FP32 terms cannot separate.
+__device__ __forceinline__ double weier_gene_fp64(double z) {
+  const unsigned long long b =
+      (unsigned long long)__double_as_longlong(z) & 0x7FFFFFFFFFFFFFFFull;
+  const int E = (int)(b >> 52);
+  const unsigned long long M = (b & ((1ull << 52) - 1ull)) | (1ull << 52);
+  const int sh = 1074 - E;  // y_0 = M / 2^sh for normal |z|
+  double s = 0.0, ak = 1.0;
+  if (b == 0ull || E == 0 || sh > 127) {
+    for (int k = 0; k <= 20; ++k, ak *= 0.5) s -= ak;  // cos(pi (2 3^k |z| + 1)) = -1
+  } else if (sh <= 0) {
+    const double c = (sh == 0 && (M & 1ull)) ? -1.0 : 1.0;
+    for (int k = 0; k <= 20; ++k, ak *= 0.5) s -= ak * c;
+  } else if (sh < 64) {
+    const unsigned long long mask = (2ull << sh) - 1ull;
+    const double scale = ldexp(1.0, -sh);
+    unsigned long long r = M & mask;
+    for (int k = 0; k <= 20; ++k, ak *= 0.5) {
+      s -= ak * cospi(__ull2double_rn(r) * scale);
+      r = (r * 3ull) & mask;
+    }
+  } else {
+    unsigned long long r0 = M, r1 = 0ull;
+    const unsigned long long mask1 = sh >= 127 ? ~0ull : ((2ull << (sh - 64)) - 1ull);
+    for (int k = 0; k <= 20; ++k, ak *= 0.5) {
+      // r = r1 2^64 + r0 < 2^(sh+1); y = r 2^-sh
+      const double y = ldexp(__ull2double_rn(r1), 64 - sh) + ldexp(__ull2double_rn(r0), -sh);
+      s -= ak * cospi(y);
+      const unsigned long long lo = r0 * 3ull;
+      const unsigned long long carry = __umul64hi(r0, 3ull);
+      r1 = (r1 * 3ull + carry) & mask1;
+      r0 = lo;
+    }
+  }
+  return s;
+}
+
+template <class Team>
+__device__ double eval_weier_fp64_t(const FnConst& fc, const double* zbuf, const Team& tm) {
+  double acc = 0.0;
+  for (int n = tm.rank(); n < fc.D; n += tm.size()) acc += weier_gene_fp64(zbuf[n]);
+  acc = tm.sum(acc);
+  return acc + fc.woff64;
 }
 
 // FP64-class fitness of x (shared or global memory row) by the calling warp

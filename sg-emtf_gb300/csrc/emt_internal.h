@@ -42,7 +42,9 @@ enum Mode : int { MODE_EPOCH = 0, MODE_INIT = 1, MODE_EVAL = 2 };
 // device counters, indexed as in EpochArgs::stats; [8, 8 + kPhases) hold the
 // per-phase SM cycles of the phase-clock build (EMT_PHASE_CLOCKS)
 constexpr int kPhases = 6;
-constexpr int kStats = 8 + kPhases;
+// [8 + kPhases]: Weierstrass near ties decided with double-precision terms
+constexpr int kStatWeierFp64 = 8 + kPhases;
+constexpr int kStats = kStatWeierFp64 + 1;
 enum Phase : int {
   PH_OTHER = 0,    // loading and writing back islands, transfer bookkeeping, migration ranks
   PH_BUILD = 1,    // trial vectors and the rotation operand

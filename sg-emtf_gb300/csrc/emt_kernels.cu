@@ -652,10 +652,20 @@ __device__ int select_and_replace(const Smem& s, const EpochArgs& a, const FnCon
       }
       if (!decided) {
         // tier 3 (or the exact Weierstrass terms): FP64-class values, cached
-        ft = fc.fid == F_WEIERSTRASS ? eval_weier_precise(fc, zt) : eval_tier3(fc, zt);
+        const bool weier = fc.fid == F_WEIERSTRASS;
+        ft = weier ? eval_weier_precise(fc, zt) : eval_tier3(fc, zt);
+        bool zp_ready = false;
         if (isnan(fp)) {
           if (!tier2) precise_rotation(s.X + m * DP, s.o, s.QT, DP, fc.D, zp);
-          fp = fc.fid == F_WEIERSTRASS ? eval_weier_precise(fc, zp) : eval_tier3(fc, zp);
+          fp = weier ? eval_weier_precise(fc, zp) : eval_tier3(fc, zp);
+          zp_ready = true;
+        }
+        if (weier && fabs(ft - fp) <= 2.0 * weier_precise_bound(fc.D)) {
+          // closer than the FP32 terms' error: every term in double precision
+          if (!zp_ready) precise_rotation(s.X + m * DP, s.o, s.QT, DP, fc.D, zp);
+          ft = eval_weier_fp64_t(fc, zt, WarpTeam{});
+          fp = eval_weier_fp64_t(fc, zp, WarpTeam{});
+          if (lane == 0 && rechecks) atomicAdd(rechecks + kStatWeierFp64, 1ull);
         }
         d64 = strict ? (ft < fp) : (ft <= fp);
       }

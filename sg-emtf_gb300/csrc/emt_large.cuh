@@ -919,6 +919,7 @@ __device__ __forceinline__ void decide_write(const LargeArgs& a, const TaskDev& 
 // FP64 pipe, and a few such ties would set the launch length.
 __global__ void __launch_bounds__(256) decide_kernel(const LargeArgs a, int mode) {
   __shared__ double scratch[8];
+  __shared__ double zmem[kMaxDimLarge];  // a member's rotation, when a tie needs it here
   const CtaTeam tm{scratch};
   const bool strict = mode == SEL_IMPORT || mode == SEL_MIGRATE;  // candidates must be better
   const int items = a.nwork[0];
@@ -947,8 +948,23 @@ __global__ void __launch_bounds__(256) decide_kernel(const LargeArgs a, int mode
       }
     }
     if (!decided) {
-      ft = fc.fid == F_WEIERSTRASS ? eval_weier_precise_t(fc, zt, tm) : eval_tier3_t(fc, zt, tm);
-      if (zp) fpv = fc.fid == F_WEIERSTRASS ? eval_weier_precise_t(fc, zp, tm) : eval_tier3_t(fc, zp, tm);
+      const bool weier = fc.fid == F_WEIERSTRASS;
+      ft = weier ? eval_weier_precise_t(fc, zt, tm) : eval_tier3_t(fc, zt, tm);
+      if (zp) fpv = weier ? eval_weier_precise_t(fc, zp, tm) : eval_tier3_t(fc, zp, tm);
+      if (weier && fabs(ft - fpv) <= 2.0 * weier_precise_bound(fc.D)) {
+        // closer than the FP32 terms' error: every term in double precision,
+        // the member's rotation computed here when its value was cached
+        double* zm = zmem;
+        if (zp) {
+          zm = const_cast<double*>(zp);
+        } else {
+          precise_rotation_team(a.pop + td.pop_off + (size_t)m * td.DP, a.shift + td.o_off,
+                                a.qt + td.q_off, td.DP, td.D, zmem, tm);
+        }
+        ft = eval_weier_fp64_t(fc, zt, tm);
+        fpv = eval_weier_fp64_t(fc, zm, tm);
+        if (threadIdx.x == 0 && a.stats) atomicAdd(a.stats + kStatWeierFp64, 1ull);
+      }
       d64 = strict ? (ft < fpv) : (ft <= fpv);
     }
     if (threadIdx.x == 0) decide_write(a, td, strict, c, m, d64, ft, fpv);

@@ -95,7 +95,7 @@ class Stats(ctypes.Structure):
                 ("recheck_differential", ctypes.c_uint64), ("anchor_rotations", ctypes.c_uint64),
                 ("recheck_identical", ctypes.c_uint64), ("epoch_launches", ctypes.c_int32),
                 ("schedule_used", ctypes.c_int32), ("migrations_accepted", ctypes.c_uint64),
-                ("max_rel_err", ctypes.c_double)]
+                ("max_rel_err", ctypes.c_double), ("recheck_fp64_terms", ctypes.c_uint64)]
 
 
 class TaskDesc:
