@@ -695,55 +695,124 @@ __device__ double eval_weier_precise(const FnConst& fc, const double* zbuf) {
 // (<= 2^-24 for |cos| <= 1); times 0.5^k summed over k (< 2) that is
 // < 8.7e-7, and the compensated sum of 21 terms adds < 2 u sum |terms|
 // (< 2.4e-7).  Over D genes: D x 1.2e-6.  Near ties closer than twice this
-// are decided by eval_weier_fp64 instead.
+// are decided by eval_weier_ff_t instead.
 __device__ __forceinline__ double weier_precise_bound(int D) { return 1.2e-6 * (double)D; }
 
-// One Weierstrass gene with every term in double precision: the same exact
-// reduction of y_k = 2 3^k |z| mod 2 as weier_gene_precise, then the reduced
-// argument (53 bits) through the double-precision cospi.  FP64 pipe: only
-// for the near ties the FP32 terms cannot separate.
-__device__ __forceinline__ double weier_gene_fp64(double z) {
+// Float-float arithmetic (pairs h + l of FP32 values, ~2^-44 relative) on
+// the FP32 pipe, for the Weierstrass ties the FP32 terms cannot separate:
+// this GPU's FP64 pipe runs at ~1/64 of its FP32 rate, so a double-precision
+// cosine costs far more than the float-float one below.
+struct FF {
+  float h, l;
+};
+__device__ __forceinline__ FF ff_fast_two_sum(float a, float b) {  // |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return FF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  float s, e;
+  two_sum(a.h, b.h, s, e);
+  e = __fadd_rn(e, __fadd_rn(a.l, b.l));
+  return ff_fast_two_sum(s, e);
+}
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, __fmaf_rn(a.l, b.h, e));
+  return ff_fast_two_sum(p, e);
+}
+// a double constant as a float-float pair
+#define EMT_FF(v) FF{(float)(v), (float)((v) - (double)(float)(v))}
+
+// cos(pi y) for y = r 2^-sh in [0, 2) (r < 2^(sh+1), 1 <= sh <= 127) to
+// ~1e-13: y is split exactly as m/2 + t with m = round(2 y) and
+// |t| <= 1/4 in integers, t goes to float-float (48 significant bits), and
+// cos or sin of x = pi t comes from its Taylor series (|x| <= pi/4; the
+// first omitted terms are below 1e-15), the five leading coefficients in
+// float-float and the small tail in FP32.
+__device__ __forceinline__ FF cospi_ff(unsigned __int128 r, int sh) {
+  const unsigned __int128 half = (unsigned __int128)1 << (sh - 1);
+  const unsigned __int128 q = (r + (half >> 1)) >> (sh - 1);  // round(2 y)
+  __int128 d = (__int128)r - (__int128)(q * half);            // t = d 2^-sh, |d| <= 2^(sh-2)
+  int e = sh;
+  if (sh > 64) {  // keep 62 bits of d: the cut is below 2^-64 of t's scale
+    d >>= (sh - 64);
+    e = 64;
+  }
+  const long long dl = (long long)d;
+  const float th = __ll2float_rn(dl);
+  const float tl = __ll2float_rn(dl - (long long)th);
+  const FF t{ldexpf(th, -e), ldexpf(tl, -e)};
+  const FF x = ff_mul(t, EMT_FF(3.14159265358979323846));
+  const FF u = ff_mul(x, x);
+  const int quadrant = (int)(q & 3u);
+  FF v;
+  if (quadrant & 1) {  // sin x = x (1 - u/3! + u^2/5! - ...)
+    float tail = __fmaf_rn(u.h, -1.0f / 1307674368000.0f, 1.0f / 6227020800.0f);
+    tail = __fmaf_rn(u.h, tail, -1.0f / 39916800.0f);
+    FF w = FF{tail, 0.f};
+    w = ff_add(EMT_FF(1.0 / 362880.0), ff_mul(u, w));
+    w = ff_add(EMT_FF(-1.0 / 5040.0), ff_mul(u, w));
+    w = ff_add(EMT_FF(1.0 / 120.0), ff_mul(u, w));
+    w = ff_add(EMT_FF(-1.0 / 6.0), ff_mul(u, w));
+    w = ff_add(FF{1.f, 0.f}, ff_mul(u, w));
+    v = ff_mul(x, w);
+    if (quadrant == 1) v = FF{-v.h, -v.l};  // cos(pi t + pi/2) = -sin(pi t)
+  } else {  // cos x = 1 - u/2! + u^2/4! - ...
+    float tail = __fmaf_rn(u.h, -1.0f / 87178291200.0f, 1.0f / 479001600.0f);
+    tail = __fmaf_rn(u.h, tail, -1.0f / 3628800.0f);
+    FF w = FF{tail, 0.f};
+    w = ff_add(EMT_FF(1.0 / 40320.0), ff_mul(u, w));
+    w = ff_add(EMT_FF(-1.0 / 720.0), ff_mul(u, w));
+    w = ff_add(EMT_FF(1.0 / 24.0), ff_mul(u, w));
+    w = ff_add(FF{-0.5f, 0.f}, ff_mul(u, w));
+    v = ff_add(FF{1.f, 0.f}, ff_mul(u, w));
+    if (quadrant == 2) v = FF{-v.h, -v.l};  // cos(pi t + pi) = -cos(pi t)
+  }
+  return v;
+}
+
+// One Weierstrass gene with every term in float-float: the same exact
+// reduction of y_k = 2 3^k |z| mod 2 as weier_gene_precise (here in 128-bit
+// integers), then cospi_ff; the terms are summed in float-float.
+__device__ __forceinline__ double weier_gene_ff(double z) {
   const unsigned long long b =
       (unsigned long long)__double_as_longlong(z) & 0x7FFFFFFFFFFFFFFFull;
   const int E = (int)(b >> 52);
   const unsigned long long M = (b & ((1ull << 52) - 1ull)) | (1ull << 52);
   const int sh = 1074 - E;  // y_0 = M / 2^sh for normal |z|
-  double s = 0.0, ak = 1.0;
+  FF s{0.f, 0.f};
+  float ak = 1.f;
   if (b == 0ull || E == 0 || sh > 127) {
-    for (int k = 0; k <= 20; ++k, ak *= 0.5) s -= ak;  // cos(pi (2 3^k |z| + 1)) = -1
+    // |z| < 2^-75: every 2 3^k |z| < 2^-41, cos = 1 to far below the bound
+    for (int k = 0; k <= 20; ++k, ak *= 0.5f) s = ff_add(s, FF{-ak, 0.f});
   } else if (sh <= 0) {
-    const double c = (sh == 0 && (M & 1ull)) ? -1.0 : 1.0;
-    for (int k = 0; k <= 20; ++k, ak *= 0.5) s -= ak * c;
-  } else if (sh < 64) {
-    const unsigned long long mask = (2ull << sh) - 1ull;
-    const double scale = ldexp(1.0, -sh);
-    unsigned long long r = M & mask;
-    for (int k = 0; k <= 20; ++k, ak *= 0.5) {
-      s -= ak * cospi(__ull2double_rn(r) * scale);
-      r = (r * 3ull) & mask;
-    }
+    const float c = (sh == 0 && (M & 1ull)) ? -1.f : 1.f;
+    for (int k = 0; k <= 20; ++k, ak *= 0.5f) s = ff_add(s, FF{-ak * c, 0.f});
   } else {
-    unsigned long long r0 = M, r1 = 0ull;
-    const unsigned long long mask1 = sh >= 127 ? ~0ull : ((2ull << (sh - 64)) - 1ull);
-    for (int k = 0; k <= 20; ++k, ak *= 0.5) {
-      // r = r1 2^64 + r0 < 2^(sh+1); y = r 2^-sh
-      const double y = ldexp(__ull2double_rn(r1), 64 - sh) + ldexp(__ull2double_rn(r0), -sh);
-      s -= ak * cospi(y);
-      const unsigned long long lo = r0 * 3ull;
-      const unsigned long long carry = __umul64hi(r0, 3ull);
-      r1 = (r1 * 3ull + carry) & mask1;
-      r0 = lo;
+    const unsigned __int128 mask = sh >= 127 ? ~(unsigned __int128)0
+                                             : (((unsigned __int128)2 << sh) - 1);
+    unsigned __int128 r = (unsigned __int128)M & mask;
+    for (int k = 0; k <= 20; ++k, ak *= 0.5f) {
+      const FF c = cospi_ff(r, sh);
+      s = ff_add(s, FF{-ak * c.h, -ak * c.l});  // scaling by 0.5^k is exact
+      r = (r * 3u) & mask;
     }
   }
-  return s;
+  return (double)s.h + (double)s.l;
 }
 
 template <class Team>
-__device__ double eval_weier_fp64_t(const FnConst& fc, const double* zbuf, const Team& tm) {
+__device__ double eval_weier_ff_t(const FnConst& fc, const double* zbuf, const Team& tm) {
   double acc = 0.0;
-  for (int n = tm.rank(); n < fc.D; n += tm.size()) acc += weier_gene_fp64(zbuf[n]);
+  for (int n = tm.rank(); n < fc.D; n += tm.size()) acc += weier_gene_ff(zbuf[n]);
   acc = tm.sum(acc);
   return acc + fc.woff64;
+}
+// The warp form, out of line: a rare path that should not raise the
+// register needs of the fused kernel around it.
+__device__ __noinline__ double eval_weier_ff_warp(const FnConst& fc, const double* zbuf) {
+  return eval_weier_ff_t(fc, zbuf, WarpTeam{});
 }
 
 // FP64-class fitness of x (shared or global memory row) by the calling warp

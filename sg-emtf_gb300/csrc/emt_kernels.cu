@@ -661,10 +661,10 @@ __device__ int select_and_replace(const Smem& s, const EpochArgs& a, const FnCon
           zp_ready = true;
         }
         if (weier && fabs(ft - fp) <= 2.0 * weier_precise_bound(fc.D)) {
-          // closer than the FP32 terms' error: every term in double precision
+          // closer than the FP32 terms' error: every term in float-float
           if (!zp_ready) precise_rotation(s.X + m * DP, s.o, s.QT, DP, fc.D, zp);
-          ft = eval_weier_fp64_t(fc, zt, WarpTeam{});
-          fp = eval_weier_fp64_t(fc, zp, WarpTeam{});
+          ft = eval_weier_ff_warp(fc, zt);
+          fp = eval_weier_ff_warp(fc, zp);
           if (lane == 0 && rechecks) atomicAdd(rechecks + kStatWeierFp64, 1ull);
         }
         d64 = strict ? (ft < fp) : (ft <= fp);

@@ -952,7 +952,7 @@ __global__ void __launch_bounds__(256) decide_kernel(const LargeArgs a, int mode
       ft = weier ? eval_weier_precise_t(fc, zt, tm) : eval_tier3_t(fc, zt, tm);
       if (zp) fpv = weier ? eval_weier_precise_t(fc, zp, tm) : eval_tier3_t(fc, zp, tm);
       if (weier && fabs(ft - fpv) <= 2.0 * weier_precise_bound(fc.D)) {
-        // closer than the FP32 terms' error: every term in double precision,
+        // closer than the FP32 terms' error: every term in float-float,
         // the member's rotation computed here when its value was cached
         double* zm = zmem;
         if (zp) {
@@ -961,8 +961,8 @@ __global__ void __launch_bounds__(256) decide_kernel(const LargeArgs a, int mode
           precise_rotation_team(a.pop + td.pop_off + (size_t)m * td.DP, a.shift + td.o_off,
                                 a.qt + td.q_off, td.DP, td.D, zmem, tm);
         }
-        ft = eval_weier_fp64_t(fc, zt, tm);
-        fpv = eval_weier_fp64_t(fc, zm, tm);
+        ft = eval_weier_ff_t(fc, zt, tm);
+        fpv = eval_weier_ff_t(fc, zm, tm);
         if (threadIdx.x == 0 && a.stats) atomicAdd(a.stats + kStatWeierFp64, 1ull);
       }
       d64 = strict ? (ft < fpv) : (ft <= fpv);
