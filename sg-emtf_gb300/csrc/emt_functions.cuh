@@ -550,7 +550,7 @@ __device__ double eval_tier3_t(const FnConst& fc, const double* zbuf, const Team
   }
   return f;
 }
-__device__ double eval_tier3(const FnConst& fc, const double* zbuf) {
+__device__ __noinline__ double eval_tier3(const FnConst& fc, const double* zbuf) {
   return eval_tier3_t(fc, zbuf, WarpTeam{});
 }
 
@@ -663,7 +663,7 @@ __device__ double eval_tier2_t(const FnConst& fc, const double* zbuf, double* er
   *err = 2.0 * e;  // safety factor on the first-order bound
   return f;
 }
-__device__ double eval_tier2(const FnConst& fc, const double* zbuf, double* err) {
+__device__ __noinline__ double eval_tier2(const FnConst& fc, const double* zbuf, double* err) {
   return eval_tier2_t(fc, zbuf, err, WarpTeam{});
 }
 
@@ -684,7 +684,7 @@ __device__ double eval_weier_precise_t(const FnConst& fc, const double* zbuf, co
   acc = tm.sum(acc);
   return acc + fc.woff64;
 }
-__device__ double eval_weier_precise(const FnConst& fc, const double* zbuf) {
+__device__ __noinline__ double eval_weier_precise(const FnConst& fc, const double* zbuf) {
   return eval_weier_precise_t(fc, zbuf, WarpTeam{});
 }
 

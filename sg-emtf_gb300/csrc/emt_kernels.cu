@@ -604,6 +604,10 @@ __device__ int select_and_replace(const Smem& s, const EpochArgs& a, const FnCon
     // compensated rotation and dz = Q (u - x), FP32/INT pipes only; -1 when
     // its bound cannot separate the two
     int dd = -1;
+    // Weierstrass: whether fit64[m] is a float-float value afterwards (1),
+    // a tier-3 value (0), or unchanged (-1); kept in the member's first
+    // anchor-bound slot, which this function's islands do not use otherwise
+    int wprec = -1;
     if (!same && anchors) {
       float* zh = s.zc + (size_t)m * 2 * DP;
       float* zl = zh + DP;
@@ -654,20 +658,29 @@ __device__ int select_and_replace(const Smem& s, const EpochArgs& a, const FnCon
         // tier 3 (or the exact Weierstrass terms): FP64-class values, cached
         const bool weier = fc.fid == F_WEIERSTRASS;
         ft = weier ? eval_weier_precise(fc, zt) : eval_tier3(fc, zt);
+        // the member's cached value is already float-float
+        const bool pprec = weier && s.zcb && s.zcb[2 * m] == 0.f && !isnan(fp);
         bool zp_ready = false;
         if (isnan(fp)) {
           if (!tier2) precise_rotation(s.X + m * DP, s.o, s.QT, DP, fc.D, zp);
           fp = weier ? eval_weier_precise(fc, zp) : eval_tier3(fc, zp);
           zp_ready = true;
         }
-        if (weier && fabs(ft - fp) <= 2.0 * weier_precise_bound(fc.D)) {
-          // closer than the FP32 terms' error: every term in float-float
-          if (!zp_ready) precise_rotation(s.X + m * DP, s.o, s.QT, DP, fc.D, zp);
-          ft = eval_weier_ff_warp(fc, zt);
-          fp = eval_weier_ff_warp(fc, zp);
-          if (lane == 0 && rechecks) atomicAdd(rechecks + kStatWeierFp64, 1ull);
+        if (weier) {
+          const double bound = weier_precise_bound(fc.D);
+          if (fabs(ft - fp) <= (pprec ? bound : 2.0 * bound)) {
+            // closer than the FP32 terms' error: every term in float-float
+            if (!pprec) {
+              if (!zp_ready) precise_rotation(s.X + m * DP, s.o, s.QT, DP, fc.D, zp);
+              fp = eval_weier_ff_warp(fc, zp);
+            }
+            ft = eval_weier_ff_warp(fc, zt);
+            wprec = 1;
+            if (lane == 0 && rechecks) atomicAdd(rechecks + kStatWeierFp64, 1ull);
+          }
         }
         d64 = strict ? (ft < fp) : (ft <= fp);
+        if (weier && wprec < 0) wprec = (!d64 && pprec) ? 1 : 0;
       }
     }
     const bool d32 = strict ? (s.ftr[c] < s.fit[m]) : (s.ftr[c] <= s.fit[m]);
@@ -678,6 +691,7 @@ __device__ int select_and_replace(const Smem& s, const EpochArgs& a, const FnCon
       }
       // a trial accepted through the FP64-class tiers has no cached anchor
       if (!same && dd < 0 && d64 && s.zcb) s.zcb[2 * m] = __int_as_float(0x7FC00000);
+      if (wprec >= 0 && s.zcb) s.zcb[2 * m] = wprec ? 0.f : __int_as_float(0x7FC00000);
       s.flag[c] = d64 ? 3 : 0;
       // FP64 value of whichever vector member m holds after this selection,
       // cached for its next re-check.  Targets are distinct, so no race.

@@ -133,7 +133,7 @@ __device__ __forceinline__ float split_rows(const float* __restrict__ a,
 // max_n |z_n - z_exact,n|, the same on every lane: the Dot2 bound over 2D + 2
 // terms, gamma^2 sum_k |q_nk| |x_k - o_k| <= gamma^2 qnorm |x - o|_2, doubled.
 // *zmax receives max_n |z_n|; pr is D float2 of scratch.
-__device__ float anchor_rotation(const float* __restrict__ x, const float* __restrict__ o,
+__device__ __noinline__ float anchor_rotation(const float* __restrict__ x, const float* __restrict__ o,
                                  const float* __restrict__ qt, int DP, int D, float qnorm,
                                  float* zh, float* zl, float* zmax, float2* pr) {
   using namespace diffck;
@@ -216,7 +216,7 @@ __device__ __forceinline__ void row_offset(const float* __restrict__ from,
 // the function has no difference form here.  buf: 4 * DP floats of per-warp
 // scratch; its first 2 * DP receive dz = Q (to - from) and its bound, for the
 // caller's cache update.
-__device__ int diff_decide(const FnConst& fc, const float* __restrict__ bzh,
+__device__ __noinline__ int diff_decide(const FnConst& fc, const float* __restrict__ bzh,
                            const float* __restrict__ bzl, float ez, const float* __restrict__ from,
                            const float* __restrict__ to, const float* __restrict__ qt, int DP,
                            float* buf) {
