@@ -8,6 +8,7 @@
 // epoch boundaries between launches, so no host thread waits on another.
 #include <cuda.h>
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cmath>
@@ -23,6 +24,16 @@
 
 #include "../../include/sgemtf.h"
 #include "emt_internal.h"
+
+// NVTX range over a host call (header-only NVTX 3: without a profiler
+// attached a push/pop costs a branch), so timelines show the library's
+// calls and each epoch's launches.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 namespace {
 
@@ -856,12 +867,14 @@ int enqueue_plan(emt_handle* h, const std::vector<EpochStep>& plan, int sched, c
   const int interval = transfer_interval_of(h);
   if (h->large) {
     for (const EpochStep& s : plan) {
+      const NvtxRange range("emt epoch (large islands)");
       const int e = large_epoch(h, s.gens, s.imp, s.exp, s.parity, stream);
       if (e) return e;
     }
     return 0;
   }
   for (const EpochStep& s : plan) {
+    const NvtxRange range("emt epoch");
     emt::EpochArgs a = base_args(h, emt::MODE_EPOCH);
     a.gens = s.gens;
     if (interval) {
@@ -1015,6 +1028,7 @@ int emt_create(const emt_config* cfg, emt_handle_t** out) {
 
 int emt_add_tasks(emt_handle_t* h, int32_t n, const emt_task_desc* td) {
   if (!h) return EMT_ERR_INVALID_ARG;
+  const NvtxRange range("emt_add_tasks");
   if (n < 0 || (n > 0 && !td)) return h->fail(EMT_ERR_INVALID_ARG, "bad task array");
   const int smem_cap = max_smem_optin(h->device);
   std::vector<HostTask> add;
@@ -1141,6 +1155,7 @@ int emt_add_tasks(emt_handle_t* h, int32_t n, const emt_task_desc* td) {
 
 int emt_reset(emt_handle_t* h, void* stream) {
   if (!h) return EMT_ERR_INVALID_ARG;
+  const NvtxRange range("emt_reset");
   int rc = upload(h);
   if (rc) return rc;
   h->stream = (cudaStream_t)stream;
@@ -1161,6 +1176,7 @@ int emt_reset(emt_handle_t* h, void* stream) {
 
 int emt_run(emt_handle_t* h, int32_t generations, void* stream) {
   if (!h) return EMT_ERR_INVALID_ARG;
+  const NvtxRange range("emt_run");
   if (generations < 0) return h->fail(EMT_ERR_INVALID_ARG, "negative generation count");
   if (!h->initialized) {
     int rc = emt_reset(h, stream);

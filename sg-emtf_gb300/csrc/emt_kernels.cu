@@ -354,8 +354,8 @@ __device__ void zero_pads(const Smem& s, int D, int nrows) {
 // mbarrier that warp 0 waits for while the other warps wait at the CTA
 // barrier.  The product of the two leading parts accumulates alone in the
 // first accumulator; every other product of parts (TF32: hi.lo, lo.hi,
-// lo.lo; BF16: the other eight of the nine, so every product of the exact
-// splits is taken) in the second, so the large partial sums do not swallow
+// lo.lo; BF16: seven more, all but s2 q2, whose 2^-32 relative size is far
+// below the accumulation's rounding) in the second, so the large partial sums do not swallow
 // the small products (each MMA step rounds its accumulator to FP32).  Then
 // the warps drain both accumulators (TMEM lane = row; warp w reads lanes
 // 32 (w mod 4) on, its half of the columns), add them in FP32 and store Z.
@@ -366,9 +366,11 @@ __device__ void rotate_tc(const Smem& s, int D, int DP, int nrows, uint32_t& pha
   const bool dead = *s.dead != 0;  // an earlier wait gave up: skip the MMAs
   if (threadIdx.x == 0 && !dead && !s.lose_completion) {
     tc::fence_after();
-    // products of parts (a, b): the leading one first, alone in accumulator 0
-    const int pa[9] = {0, 0, 1, 1, 0, 2, 1, 2, 2}, pb[9] = {0, 1, 0, 1, 2, 0, 2, 1, 2};
-    const int nprod = s.bf16 ? 9 : 4;
+    // products of parts (a, b): the leading one first, alone in accumulator 0.
+    // BF16: eight of the nine; s2 q2 (<= 2^-32 of s0 q0) is below the FP32
+    // accumulation's own rounding
+    const int pa[8] = {0, 0, 1, 1, 0, 2, 1, 2}, pb[8] = {0, 1, 0, 1, 2, 0, 2, 1};
+    const int nprod = s.bf16 ? 8 : 4;
     // descriptors: the start address field (bits 0-13, address >> 4) of the
     // tiles' base descriptors plus each step's offset >> 4 (no carry: shared
     // addresses stay below 256 KB)

@@ -84,3 +84,21 @@ def test_failed_batch_is_released_and_skipped(sgemtf):
     st = svc.stats()
     assert st["batches_submitted"] == 2 and st["batches_done"] == 1 and st["tasks_done"] == 3
     svc.close()
+
+
+def test_unsupported_batch_is_released_and_skipped(sgemtf):
+    """Admission also rejects a batch the configured form cannot hold (a
+    tensor-core handle with islands of NP > 128): EMT_ERR_UNSUPPORTED, the
+    batch fails alone and the next one is served."""
+    svc = sgemtf.Service(sgemtf.Config(seed=6, precision=sgemtf.ROT_BF16X3), generations=20,
+                         epoch=10)
+    bad = svc.submit([sgemtf.TaskDesc(0, 50, 200)])
+    good = svc.submit(_batch(sgemtf, 0, 3))
+    with pytest.raises(sgemtf.EngineError) as e:
+        svc.drain()
+    assert e.value.status == sgemtf.ERR_UNSUPPORTED
+    assert svc.batch(bad)[0]["state"] == 3
+    svc.drain()
+    info, best = svc.batch(good)
+    assert info["state"] == 2 and best.shape == (3,)
+    svc.close()
