@@ -376,7 +376,20 @@ typedef struct emt_cvrp_config {
   float transfer_rate;       /* fraction of the island sent                  */
   uint64_t seed;
   int32_t device;
-  int32_t reserved[7];
+  /* Sub-islands (the reference's IslandMigration, SG-EMTF_cvrp.cu:965-1020):
+   * the island of pop members splits into subislands groups of pop /
+   * subislands (>= 4; pop must divide; 0 or 1 = one group).  Tournaments
+   * draw parents within the member's own group.  Before the children of
+   * generation g, when g > 1 and (g - 1) % migration_interval == 0, the r-th
+   * cheapest of group s replaces the r-th dearest of group s + 1 (mod
+   * subislands), r < migration_count, when strictly cheaper, all from the
+   * pre-migration state.  emt_cvrp_get_stats counts the replacements in
+   * migrations_accepted. */
+  int32_t subislands;
+  int32_t migration_interval; /* generations between migrations; 0 = none     */
+  int32_t migration_count;    /* members each group sends; 0 = group size / 8,
+                                 at least 1; 2 * count <= group size          */
+  int32_t reserved[4];
 } emt_cvrp_config;
 
 typedef struct emt_cvrp_instance {

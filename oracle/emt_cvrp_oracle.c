@@ -95,13 +95,18 @@ static int better(const int32_t* cost, int a, int b) {
   return (cost[a] < cost[b] || (cost[a] == cost[b] && a <= b)) ? a : b;
 }
 
+int orc_cvrp_migrate(const orc_cvrp_params* p, int n, int NP, uint8_t* pop, int32_t* cost,
+                     uint32_t g);
+
 /* Child of member i in generation g (bit-exact with the device). */
 void orc_cvrp_child(const orc_cvrp_params* p, uint32_t inst, int n, int NP, const uint8_t* pop,
                     const int32_t* cost, uint32_t g, int i, uint8_t* child) {
   uint32_t w[4], v[4], m[4], r[4];
   orc_draw(p->seed, inst, g, (uint32_t)i, ORC_P_CVRP_SELECT, 0, w);
-  const int p1 = better(cost, (int)(w[0] % (uint32_t)NP), (int)(w[1] % (uint32_t)NP));
-  const int p2 = better(cost, (int)(w[2] % (uint32_t)NP), (int)(w[3] % (uint32_t)NP));
+  /* tournaments within the member's sub-island of NPs members */
+  const int S = p->subislands > 1 ? p->subislands : 1, NPs = NP / S, base = (i / NPs) * NPs;
+  const int p1 = better(cost, base + (int)(w[0] % (uint32_t)NPs), base + (int)(w[1] % (uint32_t)NPs));
+  const int p2 = better(cost, base + (int)(w[2] % (uint32_t)NPs), base + (int)(w[3] % (uint32_t)NPs));
   const uint8_t* a = pop + (size_t)p1 * n;
   const uint8_t* b = pop + (size_t)p2 * n;
   orc_draw(p->seed, inst, g, (uint32_t)i, ORC_P_CVRP_OX, 0, v);
@@ -165,6 +170,7 @@ void orc_cvrp_init_population(uint64_t seed, uint32_t inst, int n, int NP, uint8
 int orc_cvrp_generation(const orc_cvrp_params* p, uint32_t inst, int n, int NP,
                         const int32_t* dist, const int32_t* demand, int32_t capacity,
                         uint8_t* pop, int32_t* cost, uint32_t g) {
+  orc_cvrp_migrate(p, n, NP, pop, cost, g); /* when due, before the children */
   uint8_t* kids = (uint8_t*)malloc((size_t)NP * n);
   int32_t* kc = (int32_t*)malloc(sizeof(int32_t) * NP);
   int acc = 0;
@@ -212,5 +218,48 @@ int orc_cvrp_transfer_in(int n, int NP, const int32_t* dist, const int32_t* dema
       ++acc;
     }
   }
+  return acc;
+}
+
+static int cvrp_mig_count(const orc_cvrp_params* p, int NPs) {
+  if (p->mig_count > 0) return p->mig_count;
+  const int m = NPs / 8;
+  return m < 1 ? 1 : m;
+}
+
+int orc_cvrp_migrate(const orc_cvrp_params* p, int n, int NP, uint8_t* pop, int32_t* cost,
+                     uint32_t g) {
+  const int S = p->subislands > 1 ? p->subislands : 1;
+  if (S < 2 || p->mig_interval <= 0 || g <= 1u || (g - 1u) % (uint32_t)p->mig_interval != 0u)
+    return 0;
+  const int NPs = NP / S, m = cvrp_mig_count(p, NPs), k = S * m;
+  int* byrank = (int*)malloc(sizeof(int) * NP);
+  for (int i = 0; i < NP; ++i) { /* rank within the member's sub-island */
+    const int base = (i / NPs) * NPs;
+    int r = 0;
+    for (int j = base; j < base + NPs; ++j)
+      if (cost[j] < cost[i] || (cost[j] == cost[i] && j < i)) ++r;
+    byrank[base + r] = i;
+  }
+  uint8_t* C = (uint8_t*)malloc((size_t)k * n);
+  int32_t* cc = (int32_t*)malloc(sizeof(int32_t) * k);
+  int* target = (int*)malloc(sizeof(int) * k);
+  for (int c = 0; c < k; ++c) {
+    const int s = c / m, r = c - s * m, d = (s + 1) % S, src = byrank[s * NPs + r];
+    memcpy(C + (size_t)c * n, pop + (size_t)src * n, (size_t)n);
+    cc[c] = cost[src];
+    target[c] = byrank[d * NPs + NPs - 1 - r];
+  }
+  int acc = 0;
+  for (int c = 0; c < k; ++c)
+    if (cc[c] < cost[target[c]]) {
+      memcpy(pop + (size_t)target[c] * n, C + (size_t)c * n, (size_t)n);
+      cost[target[c]] = cc[c];
+      ++acc;
+    }
+  free(C);
+  free(cc);
+  free(target);
+  free(byrank);
   return acc;
 }

@@ -163,6 +163,8 @@ double orc_run_threads(const orc_params* p, const orc_task* tasks, int n, float*
 typedef struct orc_cvrp_params {
   uint64_t seed;
   float p_cross, p_swap, p_2opt;
+  /* sub-islands: groups per island (<= 1: one), migration interval, count */
+  int subislands, mig_interval, mig_count;
 } orc_cvrp_params;
 
 uint32_t orc_cvrp_round_sqrt(uint64_t v);
@@ -178,6 +180,13 @@ int orc_cvrp_generation(const orc_cvrp_params* p, uint32_t inst, int n, int NP,
                         const int32_t* dist, const int32_t* demand, int32_t capacity,
                         uint8_t* pop, int32_t* cost, uint32_t g);
 void orc_cvrp_rank(const int32_t* cost, int NP, int* byrank);
+/* Ring migration between the CVRP island's sub-islands before generation g
+ * (when due): the r-th best of group s replaces the r-th worst of group
+ * s + 1 (mod S) when strictly cheaper, all from the pre-migration state
+ * (the reference's IslandMigration, SG-EMTF_cvrp.cu:965-1020).  Returns the
+ * replacements. */
+int orc_cvrp_migrate(const orc_cvrp_params* p, int n, int NP, uint8_t* pop, int32_t* cost,
+                     uint32_t g);
 int orc_cvrp_transfer_in(int n, int NP, const int32_t* dist, const int32_t* demand,
                          int32_t capacity, const uint8_t* elites, int k, uint8_t* pop,
                          int32_t* cost);

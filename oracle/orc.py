@@ -50,7 +50,8 @@ class Params(ctypes.Structure):
 
 class CvrpParams(ctypes.Structure):
     _fields_ = [("seed", ctypes.c_uint64), ("p_cross", ctypes.c_float), ("p_swap", ctypes.c_float),
-                ("p_2opt", ctypes.c_float)]
+                ("p_2opt", ctypes.c_float), ("subislands", ctypes.c_int),
+                ("mig_interval", ctypes.c_int), ("mig_count", ctypes.c_int)]
 
 
 def build(quiet=True):
@@ -132,6 +133,9 @@ def lib():
                                           ctypes.c_int, I32P, I32P, ctypes.c_int32, _U8P, I32P,
                                           ctypes.c_uint32]
         L.orc_cvrp_rank.argtypes = [I32P, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+        L.orc_cvrp_migrate.restype = ctypes.c_int
+        L.orc_cvrp_migrate.argtypes = [ctypes.POINTER(CvrpParams), ctypes.c_int, ctypes.c_int, _U8P,
+                                       I32P, ctypes.c_uint32]
         L.orc_cvrp_transfer_in.restype = ctypes.c_int
         L.orc_cvrp_transfer_in.argtypes = [ctypes.c_int, ctypes.c_int, I32P, I32P, ctypes.c_int32,
                                            _U8P, ctypes.c_int, _U8P, I32P]
@@ -314,8 +318,9 @@ class CvrpInstance:
         return (c, pred) if with_pred else c
 
 
-def cvrp_params(seed=1, p_cross=0.9, p_swap=0.2, p_2opt=0.2):
-    return CvrpParams(seed, p_cross, p_swap, p_2opt)
+def cvrp_params(seed=1, p_cross=0.9, p_swap=0.2, p_2opt=0.2, subislands=1, mig_interval=0,
+                mig_count=0):
+    return CvrpParams(seed, p_cross, p_swap, p_2opt, subislands, mig_interval, mig_count)
 
 
 def cvrp_init_population(seed, inst, n, NP):
@@ -361,8 +366,8 @@ class CvrpReplay:
     that closes an interval, imported at the start of the next epoch)."""
 
     def __init__(self, seed, instances, NP, p_cross=0.9, p_swap=0.2, p_2opt=0.2,
-                 interval=0, rate=0.1):
-        self.p = cvrp_params(seed, p_cross, p_swap, p_2opt)
+                 interval=0, rate=0.1, subislands=1, mig_interval=0, mig_count=0):
+        self.p = cvrp_params(seed, p_cross, p_swap, p_2opt, subislands, mig_interval, mig_count)
         self.seed, self.ins, self.NP = seed, instances, NP
         self.interval = interval if len(instances) > 1 else 0
         self.rate = rate

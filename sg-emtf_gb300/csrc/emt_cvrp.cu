@@ -66,9 +66,11 @@ struct Args {
   int32_t transfer_import, transfer_export;
   const uint8_t* elites_in;
   uint8_t* elites_out;
-  unsigned long long* stats;  // [0] evaluations [1] transfers accepted
+  unsigned long long* stats;  // [0] evaluations [1] transfers accepted [2] migrants accepted
   int32_t* err;
   size_t smem_bytes;
+  // sub-islands: groups per island (1 = none), migration interval and count
+  int32_t subislands, mig_interval, mig_count;
 };
 
 __host__ __device__ inline size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
@@ -328,12 +330,53 @@ __global__ void __launch_bounds__(256) cvrp_epoch_kernel(const Args a) {
       }
     }
     // ---- generations ----
+    const int S = a.subislands > 1 ? a.subislands : 1, NPs = NP / S;
     for (int g = 0; g < a.gens; ++g) {
       const uint32_t G = gen0 + (uint32_t)g + 1u;
+      // ring migration between the sub-islands (IslandMigration,
+      // SG-EMTF_cvrp.cu:965-1020): before generation G when due, the r-th
+      // best of group s replaces the r-th worst of group s + 1 (mod S) when
+      // strictly cheaper, all from the pre-migration state
+      if (S > 1 && a.mig_interval > 0 && G > 1u && (G - 1u) % (uint32_t)a.mig_interval == 0u) {
+        const int m = a.mig_count > 0 ? a.mig_count : max(1, NPs / 8), k = S * m;
+        if (i < NP) {  // rank within the member's group, ties by index
+          const int base = (i / NPs) * NPs;
+          int r = 0;
+          for (int j = base; j < base + NPs; ++j) r += (cost[j] < cost[i] || (cost[j] == cost[i] && j < i));
+          byrank[base + r] = i;
+        }
+        __syncthreads();
+        // copy each migrant into its target's spare row (sources are the
+        // best m of a group, targets the worst m: disjoint as 2m <= NPs)
+        for (int it = threadIdx.x; it < k * n; it += blockDim.x) {
+          const int c = it / n, q = it - c * n, sg = c / m, r = c - sg * m;
+          const int src = byrank[sg * NPs + r];
+          const int dst = byrank[(sg + 1 == S ? 0 : sg + 1) * NPs + NPs - 1 - r];
+          row(dst, cur[dst] ^ 1)[q] = row(src, cur[src])[q];
+        }
+        __syncthreads();
+        int acc = 0;
+        if (i < k) {
+          const int sg = i / m, r = i - sg * m;
+          const int src = byrank[sg * NPs + r];
+          const int dst = byrank[(sg + 1 == S ? 0 : sg + 1) * NPs + NPs - 1 - r];
+          const int32_t cs = cost[src];
+          if (cs < cost[dst]) {
+            cur[dst] ^= 1;
+            cost[dst] = cs;
+            acc = 1;
+          }
+        }
+        if (acc && a.stats) atomicAdd(a.stats + 2, 1ull);
+        __syncthreads();
+      }
       if (i < NP) {
         const U4 ws = draw(a.seed, (uint32_t)t, G, (uint32_t)i, P_SELECT, 0);
-        const int p1 = better(cost, (int)(ws.x % (uint32_t)NP), (int)(ws.y % (uint32_t)NP));
-        const int p2 = better(cost, (int)(ws.z % (uint32_t)NP), (int)(ws.w % (uint32_t)NP));
+        // binary tournaments within the member's sub-island
+        const uint32_t us = (uint32_t)NPs;
+        const int gb = (i / NPs) * NPs;
+        const int p1 = better(cost, gb + (int)(ws.x % us), gb + (int)(ws.y % us));
+        const int p2 = better(cost, gb + (int)(ws.z % us), gb + (int)(ws.w % us));
         const uint8_t* A = row(p1, cur[p1]);
         const uint8_t* B = row(p2, cur[p2]);
         uint8_t* c = row(i, cur[i] ^ 1);
@@ -603,7 +646,7 @@ int cvrp_upload(emt_cvrp_handle* h) {
   if ((e = cudaSetDevice(h->cfg.device)) != cudaSuccess) return h->cuda_fail(e, "cudaSetDevice");
   if ((e = h->d_inst.ensure(T)) || (e = h->d_node.ensure(hn.size())) ||
       (e = h->d_pop.ensure((size_t)pop)) || (e = h->d_cost.ensure((size_t)cost)) ||
-      (e = h->d_gen.ensure(T)) || (e = h->d_stats.ensure(2)) || (e = h->d_err.ensure(1)) ||
+      (e = h->d_gen.ensure(T)) || (e = h->d_stats.ensure(3)) || (e = h->d_err.ensure(1)) ||
       (e = h->d_best_idx.ensure(T)) || (e = h->d_best_cost.ensure(T)))
     return h->cuda_fail(e, "cudaMalloc");
   if (h->cfg.transfer_interval > 0 && T > 1)
@@ -612,7 +655,7 @@ int cvrp_upload(emt_cvrp_handle* h) {
   if ((e = cudaMemcpy(h->d_inst.p, h->table.data(), sizeof(emt::cvrp::InstDev) * T, cudaMemcpyHostToDevice)) ||
       (e = cudaMemcpy(h->d_node.p, hn.data(), sizeof(int4) * hn.size(), cudaMemcpyHostToDevice)) ||
       (e = cudaMemset(h->d_gen.p, 0, sizeof(uint32_t) * T)) ||
-      (e = cudaMemset(h->d_stats.p, 0, sizeof(unsigned long long) * 2)) ||
+      (e = cudaMemset(h->d_stats.p, 0, sizeof(unsigned long long) * 3)) ||
       (e = cudaMemset(h->d_err.p, 0, sizeof(int32_t))))
     return h->cuda_fail(e, "upload");
   h->uploaded = true;
@@ -640,6 +683,9 @@ emt::cvrp::Args cvrp_args(emt_cvrp_handle* h, int mode) {
   a.stats = h->d_stats.p;
   a.err = h->d_err.p;
   a.smem_bytes = h->smem;
+  a.subislands = h->cfg.subislands > 1 ? h->cfg.subislands : 1;
+  a.mig_interval = h->cfg.migration_interval;
+  a.mig_count = h->cfg.migration_count;
   return a;
 }
 
@@ -677,6 +723,14 @@ int emt_cvrp_create(const emt_cvrp_config* cfg, emt_cvrp_handle_t** out) {
   if (cfg->pop < 2 || cfg->pop > 256 || !(cfg->p_cross >= 0.f && cfg->p_cross <= 1.f) ||
       !(cfg->p_swap >= 0.f && cfg->p_swap <= 1.f) || !(cfg->p_2opt >= 0.f && cfg->p_2opt <= 1.f) ||
       cfg->transfer_interval < 0 || !(cfg->transfer_rate > 0.f && cfg->transfer_rate <= 1.f))
+    return EMT_ERR_INVALID_ARG;
+  // sub-islands: NP splits evenly into groups of at least 4, each sending at
+  // most half of its members
+  const int S = cfg->subislands > 1 ? cfg->subislands : 1;
+  if (cfg->subislands < 0 || cfg->migration_interval < 0 || cfg->migration_count < 0 ||
+      cfg->pop % S != 0 || (S > 1 && cfg->pop / S < 4) ||
+      2 * (cfg->migration_count > 0 ? cfg->migration_count : std::max(1, cfg->pop / S / 8)) >
+          cfg->pop / S)
     return EMT_ERR_INVALID_ARG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return EMT_ERR_CUDA;
@@ -915,11 +969,12 @@ int emt_cvrp_get_stats(emt_cvrp_handle_t* h, emt_stats* out) {
   if (h->d_stats.p) {
     int rc = emt_cvrp_sync(h);
     if (rc) return rc;
-    unsigned long long s[2];
+    unsigned long long s[3];
     cudaError_t e = cudaMemcpy(s, h->d_stats.p, sizeof(s), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return h->cuda_fail(e, "copy stats");
     out->evaluations = s[0];
     out->transfers_accepted = s[1];
+    out->migrations_accepted = s[2];
     out->generations = h->initialized ? (uint64_t)h->gdone * h->inst.size() : 0;
   }
   return EMT_OK;

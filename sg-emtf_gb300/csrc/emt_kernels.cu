@@ -1124,14 +1124,16 @@ __global__ void __launch_bounds__(kThreads, 3) epoch_kernel_queue(const EpochArg
   epoch_entry<false, true>(a, nullptr, smem_raw);
 }
 
-// Tensor-core form: three islands per SM at D = 50, NP = 64 in the BF16
-// form (~74 KB of operands and state each).
-__global__ void __launch_bounds__(kThreads, 3) epoch_kernel_tc(const EpochArgs a,
+// Tensor-core forms: two islands per SM with up to 128 registers a thread
+// (no spills).  Three per SM at 80 registers, which the BF16 form's ~76 KB
+// of shared memory would allow, spilled and ran slower (D = 50, NP = 64:
+// 165 against 155 ms per config-2 step).
+__global__ void __launch_bounds__(kThreads, 2) epoch_kernel_tc(const EpochArgs a,
                                                                 const __grid_constant__ CUtensorMap tmap) {
   extern __shared__ __align__(1024) unsigned char smem_tc[];
   epoch_entry<true, false>(a, &tmap, smem_tc);
 }
-__global__ void __launch_bounds__(kThreads, 3) epoch_kernel_tc_queue(
+__global__ void __launch_bounds__(kThreads, 2) epoch_kernel_tc_queue(
     const EpochArgs a, const __grid_constant__ CUtensorMap tmap) {
   extern __shared__ __align__(1024) unsigned char smem_tc[];
   epoch_entry<true, true>(a, &tmap, smem_tc);

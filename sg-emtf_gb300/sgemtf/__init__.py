@@ -140,7 +140,9 @@ class CvrpConfig(ctypes.Structure):
     _fields_ = [("pop", ctypes.c_int32), ("p_cross", ctypes.c_float), ("p_swap", ctypes.c_float),
                 ("p_2opt", ctypes.c_float), ("transfer_interval", ctypes.c_int32),
                 ("transfer_rate", ctypes.c_float), ("seed", ctypes.c_uint64),
-                ("device", ctypes.c_int32), ("reserved", ctypes.c_int32 * 7)]
+                ("device", ctypes.c_int32), ("subislands", ctypes.c_int32),
+                ("migration_interval", ctypes.c_int32), ("migration_count", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 4)]
 
     def __init__(self, **kw):
         super().__init__()

@@ -113,3 +113,35 @@ def test_deque_split_matches_label_correcting(orc, dem_hi):
         ins = orc.CvrpInstance(0, 0, n, cap, x, y, d)
         perm = (rng.permutation(n) + 1).astype(np.uint8)
         assert split_deque(ins, perm) == ins.split(perm)
+
+
+def test_cvrp_migration_oracle(orc):
+    """The oracle's CVRP ring migration: S = 1 changes nothing; with groups,
+    the r-th cheapest of each group replaces the r-th dearest of the next one
+    when strictly cheaper, from the pre-migration state."""
+    import numpy as np
+    ins = orc.CvrpInstance(4, 0, 12, 20)
+    pop = orc.cvrp_init_population(4, 0, 12, 16)
+    cost = np.array([ins.split(r) for r in pop], np.int32)
+    p1 = orc.cvrp_params(4, subislands=1, mig_interval=1)
+    a, ca = pop.copy(), cost.copy()
+    assert orc.lib().orc_cvrp_migrate(orc.ctypes.byref(p1), 12, 16, orc._u8(a), orc._i32(ca), 2) == 0
+    p = orc.cvrp_params(4, subislands=2, mig_interval=1, mig_count=2)
+    b, cb = pop.copy(), cost.copy()
+    n = orc.lib().orc_cvrp_migrate(orc.ctypes.byref(p), 12, 16, orc._u8(b), orc._i32(cb), 2)
+    want, cw = pop.copy(), cost.copy()
+    groups = [list(range(0, 8)), list(range(8, 16))]
+    ranked = [sorted(g, key=lambda i: (cost[i], i)) for g in groups]
+    moved = 0
+    for s in range(2):
+        for r in range(2):
+            src, dst = ranked[s][r], ranked[(s + 1) % 2][7 - r]
+            if cost[src] < cost[dst]:
+                want[dst] = pop[src]
+                cw[dst] = cost[src]
+                moved += 1
+    assert n == moved and np.array_equal(b, want) and np.array_equal(cb, cw)
+    # not due: generation 1, or off the interval
+    p3 = orc.cvrp_params(4, subislands=2, mig_interval=3)
+    assert orc.lib().orc_cvrp_migrate(orc.ctypes.byref(p3), 12, 16, orc._u8(pop.copy()),
+                                      orc._i32(cost.copy()), 3) == 0

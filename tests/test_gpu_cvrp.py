@@ -206,3 +206,28 @@ def test_demand_prefix_widths(sgemtf, orc, cap, dem_hi):
     tours = np.stack([rng.permutation(n) + 1 for _ in range(200)]).astype(np.uint8)
     np.testing.assert_array_equal(e.evaluate(0, tours), [ins[0].split(t) for t in tours])
     e.close()
+
+
+@pytest.mark.parametrize("S,interval,count", [(2, 3, 0), (4, 2, 3)])
+def test_subislands_and_migration_bit_exact(sgemtf, orc, S, interval, count):
+    """Sub-islands (the reference's IslandMigration, SG-EMTF_cvrp.cu:965-1020):
+    tournaments within each group and ring migration between the groups,
+    with elite transfer between instances, against the host replay."""
+    specs = [(40, 30), (40, 30), (25, 20)]
+    ins = [orc.CvrpInstance(12, t, n, c) for t, (n, c) in enumerate(specs)]
+    e = engine(sgemtf, specs, seed=12, pop=64, transfer_interval=5, transfer_rate=0.1,
+               subislands=S, migration_interval=interval, migration_count=count)
+    rep = orc.CvrpReplay(12, ins, 64, interval=5, rate=0.1, subislands=S, mig_interval=interval,
+                         mig_count=count)
+    e.run(12)
+    rep.run(12)
+    check_islands(e, rep)
+    assert e.stats()["migrations_accepted"] > 0
+    e.close()
+
+
+def test_subisland_arguments(sgemtf):
+    for bad in (dict(pop=30, subislands=4), dict(pop=32, subislands=16),
+                dict(pop=32, subislands=2, migration_count=9), dict(pop=32, subislands=-1)):
+        with pytest.raises(sgemtf.EngineError):
+            sgemtf.CvrpEngine(**bad)
