@@ -18,6 +18,10 @@ Workload (one "step" = one full optimisation run of every task):
   --impl reference: the same metric on the host cores with the CPU
   restatement of the algorithm (the reference has no CPU path of its own).
 
+  other_workloads: at N = 1 the default line also carries the headline
+  fields of the workloads below, each run afterwards as its own bench.py
+  process on the same GPU (--no-extra skips them).
+
 --workload uneven: 4096 tasks with D in {10,30,50,100} and NP in {32,64,128}
   (seeded), 200 generations with transfer every 20: the launch schedules
   (one launch, occupancy buckets, one launch per task; with and without CUDA
@@ -65,7 +69,7 @@ TASKS, DIM, POP, GENS = 1000, 50, 64, 2000
 FLOPS_PER_EVAL = 2 * DIM * DIM  # rotation, unpadded D, one product counted
 # DRAM bytes (read + write) of one epoch launch of 304 tasks, 200 generations,
 # from the committed ncu captures; per launch the state moves once
-EPOCH_DRAM_BYTES_304 = {"fp32": 8.12e6, "tf32x3": 16.9e6}
+EPOCH_DRAM_BYTES_304 = {"fp32": 8.09e6, "tf32x3": 16.9e6, "bf16x3": 13.37e6}
 TC_FORMS = ("tf32x3", "bf16x3")
 
 
@@ -85,7 +89,51 @@ def parse():
                    choices=["continuous", "cvrp", "uneven", "large", "quality", "service",
                             "phases"])
     p.add_argument("--seeds", type=int, default=30)
+    p.add_argument("--no-extra", action="store_true",
+                   help="skip the other workloads' summaries in the default line")
     return p.parse_args()
+
+
+# The other workloads, each run as its own bench.py process after the
+# headline measurement (one GPU, N = 1), and the fields of its line that the
+# headline line carries under "other_workloads".
+EXTRA_WORKLOADS = {
+    "uneven": (["--workload", "uneven", "--no-cpu"],
+               ["metric", "value", "unit", "ms_per_step", "config", "schedules", "clocks"]),
+    "large": (["--workload", "large", "--steps", "2", "--warmup", "3"],
+              ["metric", "value", "unit", "ms_per_step", "forms", "roofline", "clocks",
+               "cpu_baseline"]),
+    "cvrp": (["--workload", "cvrp"],
+             ["metric", "value", "unit", "ms_per_step", "e2e", "cpu_baseline", "clocks"]),
+    "quality": (["--workload", "quality"],
+                ["metric", "setting", "per_type", "ano_final", "ano_reference_final",
+                 "ano_max_abs_diff", "shipped_setting", "island", "wall_s"]),
+    "service": (["--workload", "service"],
+                ["metric", "value", "unit", "mean_response_ms", "mean_solve_ms",
+                 "max_device_mem_mb", "wall_s", "last_arrival_ms"]),
+}
+
+
+def other_workloads(local):
+    """Runs each workload of EXTRA_WORKLOADS in a child process on this GPU
+    and keeps the named fields of its JSON line (or the error's last line)."""
+    env = dict(os.environ, CUDA_VISIBLE_DEVICES=os.environ.get("CUDA_VISIBLE_DEVICES", str(local)))
+    for k in ("RANK", "LOCAL_RANK", "WORLD_SIZE", "MASTER_ADDR", "MASTER_PORT"):
+        env.pop(k, None)
+    out = {}
+    for name, (argv, keep) in EXTRA_WORKLOADS.items():
+        t0 = time.perf_counter()
+        r = subprocess.run([sys.executable, os.path.abspath(__file__), *argv], cwd=ROOT, env=env,
+                           stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+        lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+        if r.returncode != 0 or not lines:
+            tail = (r.stderr.strip().splitlines() or ["no output"])[-1]
+            out[name] = {"error": "exit %d: %s" % (r.returncode, tail[:300])}
+            continue
+        d = json.loads(lines[-1])
+        out[name] = {k: d[k] for k in keep if k in d}
+        out[name]["process_s"] = time.perf_counter() - t0
+    return out
 
 
 def dist_env():
@@ -807,16 +855,14 @@ def main_large(args, rank, world, local):
 
 def main_quality(args, rank, world, local):
     """--workload quality: the statistical harness (sgemtf/quality.py) beside
-    the reference's own recorded runs of the same setting."""
+    the reference's own recorded runs of the same setting: the setting the
+    recorded runs match (mutation probability 1/D) and, beside it, the GA
+    file's own mutation probability 1."""
     if rank != 0:
         return
-    import sgemtf
+    import sgemtf  # noqa: F401
     from sgemtf import quality
 
-    t0 = time.perf_counter()
-    types, rec = quality.run(seeds=args.seeds, device=local)
-    wall = time.perf_counter() - t0
-    ours = quality.summarise(types, rec)
     golden = os.path.join(ROOT, "tests", "golden")
     with open(os.path.join(golden, "reference_records_T100.json")) as f:
         ref = json.load(f)
@@ -826,20 +872,41 @@ def main_quality(args, rank, world, local):
     rtypes = np.array(ref["types"])
     names = {0: "sphere", 1: "rosenbrock", 2: "ackley", 3: "rastrigin", 4: "griewank",
              5: "weierstrass", 6: "schwefel"}
-    per_type = {}
-    for rt, v in ours["per_type"].items():
-        r = runs[:, rtypes == rt, 1]
-        per_type[names[rt]] = {
-            "tasks": v["tasks"], "mean": v["mean"], "median": v["median"],
-            "reference_mean": float(r.mean()), "reference_median": float(np.median(r)),
-            "median_ratio": v["median"] / float(np.median(r))}
+
+    def measure(operators):
+        t0 = time.perf_counter()
+        types, rec = quality.run(seeds=args.seeds, device=local, operators=operators)
+        wall = time.perf_counter() - t0
+        ours = quality.summarise(types, rec)
+        per_type = {}
+        for rt, v in ours["per_type"].items():
+            r = runs[:, rtypes == rt, 1]
+            per_type[names[rt]] = {
+                "tasks": v["tasks"], "mean": v["mean"], "median": v["median"],
+                "reference_mean": float(r.mean()), "reference_median": float(np.median(r)),
+                "median_ratio": v["median"] / float(np.median(r))}
+        return {"per_type": per_type, "ano": ours["ano"], "ano_final": ours["ano"][-1],
+                "ano_max_abs_diff": float(np.abs(np.array(ours["ano"]) - ref_ano).max()),
+                "wall_s": wall}
+
+    recorded = measure(quality.RECORDED_GA)
+    shipped = measure(quality.SHIPPED_GA)
     print(json.dumps({
         "metric": "best fitness after 1000 generations over %d seeds vs the reference's 18 "
                   "recorded runs (100 tasks, D=50, GA, reference instances)" % args.seeds,
         "workload": "quality", "seeds": args.seeds, "reference_runs": int(runs.shape[0]),
-        "per_type": per_type, "ano": ours["ano"], "ano_reference": ref_ano,
-        "ano_final": ours["ano"][-1], "ano_reference_final": ref_ano[-1],
-        "island": "256 members (the reference: 512)", "wall_s": wall,
+        "setting": "GA as recorded: SBX eta 2 on every gene, PM eta 5 with probability 1/D "
+                   "(SG-EMTF_DE.cu:481)",
+        "per_type": recorded["per_type"], "ano": recorded["ano"], "ano_reference": ref_ano,
+        "ano_final": recorded["ano_final"], "ano_reference_final": ref_ano[-1],
+        "ano_max_abs_diff": recorded["ano_max_abs_diff"],
+        "shipped_setting": {"setting": "PM on every gene (SG-EMTF.cu:555)",
+                            "median_ratio": {k: v["median_ratio"]
+                                             for k, v in shipped["per_type"].items()},
+                            "ano_max_abs_diff": shipped["ano_max_abs_diff"]},
+        "island": "512 members as 4 islands of 128, 32 migrants every 25 generations "
+                  "(HBM-resident pipeline)",
+        "wall_s": recorded["wall_s"] + shipped["wall_s"],
         "data": "synthetic (reference-distributed diagonal instances, seeded)"}))
 
 
@@ -913,7 +980,7 @@ def main_phases(args, rank, world, local):
         st = eng.stats()
         eng.close()
         tot = float(sum(cyc.values()))
-        rot = cyc["rotate"] / tot
+        rot = sum(cyc[k] for k in sgemtf.Engine.ROTATION_PHASES) / tot
         out[name] = {"cycles": cyc, "share": {k: v / tot for k, v in cyc.items()},
                      "device_ms": st["device_ms"],
                      # Amdahl: the step's speed-up if the rotation cost nothing
@@ -924,7 +991,8 @@ def main_phases(args, rank, world, local):
         "%d tasks, D=%d, NP=%d, %d generations" % (n, DIM, POP, gens),
         "forms": out,
         # a tensor-core form can at most remove the FP32 form's rotation cycles
-        "tc_over_fp32_ceiling": sum(f.values()) / (sum(f.values()) - f["rotate"]),
+        "tc_over_fp32_ceiling": sum(f.values()) / (
+            sum(f.values()) - sum(f[k] for k in sgemtf.Engine.ROTATION_PHASES)),
         "fp32_over_tc_cycles": {k: sum(f.values()) / sum(out[k]["cycles"].values())
                                 for k in TC_FORMS},
         "note": "measurement build: a barrier at every phase boundary"}), flush=True)
@@ -1104,6 +1172,8 @@ def main():
         line["e2e"] = e2e
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(n, gens)
+    if world == 1 and not args.no_extra and n == TASKS and gens == GENS:
+        line["other_workloads"] = other_workloads(local)
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

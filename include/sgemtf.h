@@ -200,15 +200,18 @@ typedef struct emt_task_desc {
   const float* shift;            /* D floats; NULL draws o ~ U(0.8 * box)   */
 } emt_task_desc;
 
-/* Islands with D <= EMT_MAX_FUSED_DIM run in the fused kernel (one CTA per
- * island, state in shared memory).  A handle holding any task with a larger
- * D (up to EMT_MAX_DIM, e.g. 256 tasks of D = 1000) runs every island as an
- * HBM-resident pipeline instead: trial kernel, rotation GEMM (tcgen05
- * tensor cores or FP32 CUDA cores), evaluation, selection; emt_evaluate and
- * emt_run_noalloc return EMT_ERR_UNSUPPORTED for such a handle. */
+/* Islands with D <= EMT_MAX_FUSED_DIM and NP <= EMT_MAX_FUSED_POP run in the
+ * fused kernel (one CTA per island, state in shared memory).  A handle
+ * holding any task with a larger D (up to EMT_MAX_DIM, e.g. 256 tasks of
+ * D = 1000) or a larger NP (up to EMT_MAX_POP, the reference's 512-member
+ * islands, SG-EMTF.cu:29) runs every island as an HBM-resident pipeline
+ * instead: trial kernel, rotation GEMM (tcgen05 tensor cores or FP32 CUDA
+ * cores), evaluation, selection; emt_evaluate and emt_run_noalloc return
+ * EMT_ERR_UNSUPPORTED for such a handle. */
 #define EMT_MAX_DIM 1024
 #define EMT_MAX_FUSED_DIM 128
-#define EMT_MAX_POP 256
+#define EMT_MAX_POP 512
+#define EMT_MAX_FUSED_POP 256
 
 typedef struct emt_stats {
   uint64_t evaluations;       /* fitness evaluations on the device         */
@@ -249,7 +252,16 @@ EMT_API int emt_function_box(int32_t function, int32_t reference_boxes, float* l
 EMT_API int emt_create(const emt_config* cfg, emt_handle_t** out);
 
 /* Adds n tasks (para_init + pop_init, SG-EMTF.cu:146-195): copies the
- * rotation and shift, generates what the descriptors leave to the seed. */
+ * rotation and shift, generates what the descriptors leave to the seed.
+ * Before emt_reset the tasks simply join the handle.  On a handle that has
+ * been reset or run, the tasks join the running handle (the reference's
+ * batch arrivals, SG-EMTF.cu:1842-1912): the running islands keep their
+ * state and generation counter, the new islands get the initial populations
+ * a handle created with every task would draw and evolve from the handle's
+ * next generation on (transfer partners are then drawn over all tasks).  The
+ * call synchronises the handle's stream.  If the grown handle is refused
+ * (e.g. an explicit tensor-core form the new islands do not fit), the call
+ * returns that error and the handle keeps its running islands unchanged. */
 EMT_API int emt_add_tasks(emt_handle_t* h, int32_t n, const emt_task_desc* tasks);
 
 /* Draws every task's initial population from the seed and evaluates it
@@ -309,8 +321,11 @@ EMT_API int emt_time_rotation(emt_handle_t* h, int32_t reps, void* stream, float
 
 /* Measurement hook: SM cycles the fused epoch kernel's CTAs spent per phase
  * since emt_reset, summed over CTAs: [0] loading and writing back islands
- * and transfer bookkeeping, [1] trial vectors, [2] rotation, [3] function
- * epilogue, [4] FP32 selection, [5] near-tie re-checks.  Only the library's
+ * and transfer bookkeeping, [1] trial vectors, [2] rotation (tensor-core
+ * forms: the operand hand-off), [3] function epilogue, [4] FP32 selection,
+ * [5] near-tie re-checks, and for the tensor-core forms [6] the issuing
+ * thread's MMAs and commit, [7] the wait for their completion, [8] the
+ * accumulator drain.  Only the library's
  * measurement build counts them (compiled with EMT_PHASE_CLOCKS, which adds
  * a barrier at each phase boundary); the regular build returns
  * EMT_ERR_UNSUPPORTED.  No counterpart in the reference. */

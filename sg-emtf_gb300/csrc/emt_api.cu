@@ -80,7 +80,8 @@ struct emt_handle {
   std::vector<TaskDev> table;
   std::vector<int32_t> order;
   bool uploaded = false, initialized = false;
-  uint32_t gdone = 0;  // generations completed by every task
+  uint32_t gdone = 0;  // generation counter of the handle (every task's next draw is gdone + 1)
+  uint64_t gen_joined = 0;  // sum over joined tasks of gdone at their join (stats)
   int elite_parity = 0;
   size_t smem_bytes = 0;
   std::string err;
@@ -438,11 +439,11 @@ int upload(emt_handle* h) {
   h->use_tc = false;
   h->tc_bf16 = false;
   h->large = false;
-  for (const auto& t : h->tasks) h->large |= t.D > emt::kMaxDim;
+  for (const auto& t : h->tasks) h->large |= t.D > emt::kMaxDim || t.NP > emt::kMaxPop;
   if (h->large) {
     // the pipeline's work items carry the task index in 15 bits
     if (h->tasks.size() > 32767)
-      return h->fail(EMT_ERR_UNSUPPORTED, "a handle with islands of D > 128 holds at most 32767 tasks");
+      return h->fail(EMT_ERR_UNSUPPORTED, "a handle with islands of D > 128 or NP > 256 holds at most 32767 tasks");
     // (large islands run the TF32 hi/lo GEMM for either tensor-core form)
     h->large_tc = h->cfg.precision != EMT_ROT_FP32 && device_has_tcgen05(h->device);
     if (!h->large_tc && (h->cfg.precision == EMT_ROT_TF32X3 || h->cfg.precision == EMT_ROT_BF16X3))
@@ -721,6 +722,8 @@ emt::LargeArgs large_args(emt_handle* h) {
   emt::LargeArgs a{};
   a.tasks = h->d_tasks.p;
   a.n_tasks = (int32_t)h->tasks.size();
+  a.max_np = 4;
+  for (const auto& t : h->tasks) a.max_np = std::max(a.max_np, t.NP);
   a.Kp = h->lKp;
   a.Nq = h->lNq;
   a.tc = h->large_tc ? 1 : 0;
@@ -779,7 +782,7 @@ int large_eval_members(emt_handle* h, cudaStream_t stream) {
   const emt::LargeArgs a = large_args(h);
   int e = emt_large_build(a, emt::large::BUILD_X, stream);
   if (!e) e = emt_large_gemm(a, &h->smap, &h->qmap, stream);
-  if (!e) e = emt_large_eval(a, 0, emt::kMaxPop, stream);
+  if (!e) e = emt_large_eval(a, 0, emt::kMaxPopLarge, stream);
   return e;
 }
 
@@ -788,7 +791,7 @@ int large_eval_members(emt_handle* h, cudaStream_t stream) {
 int large_generation(emt_handle* h, const emt::LargeArgs& a, cudaStream_t stream) {
   int e = emt_large_build(a, emt::large::BUILD_TRIALS, stream);
   if (!e) e = emt_large_gemm(a, &h->smap, &h->qmap, stream);
-  if (!e) e = emt_large_eval(a, 1, emt::kMaxPop, stream);
+  if (!e) e = emt_large_eval(a, 1, emt::kMaxPopLarge, stream);
   if (!e) e = emt_large_selection(a, emt::large::SEL_GENERATION, stream);
   return e;
 }
@@ -804,7 +807,7 @@ int large_epoch(emt_handle* h, int gens, int imp, int exp, int parity, cudaStrea
     e = emt_large_select(a, emt::large::SEL_RANK, stream);
     if (!e) e = emt_large_build(a, emt::large::BUILD_CANDIDATES, stream);
     if (!e) e = emt_large_gemm(a, &h->smap, &h->qmap, stream);
-    if (!e) e = emt_large_eval(a, 1, emt::kMaxPop, stream);
+    if (!e) e = emt_large_eval(a, 1, emt::kMaxPopLarge, stream);
     if (!e) e = emt_large_selection(a, emt::large::SEL_IMPORT, stream);
   }
   const bool migrate = a.subislands > 1 && a.mig_interval > 0;
@@ -1026,6 +1029,74 @@ int emt_create(const emt_config* cfg, emt_handle_t** out) {
   return EMT_OK;
 }
 
+// Tasks joining an initialized handle (the reference admits batches of
+// tasks into a running service, SG-EMTF.cu:1842-1912).  The islands already
+// running keep their members, fitness values and generation counter; the new
+// ones start from the initial populations a handle created with every task
+// would draw (the draws depend on the seed and the task index only) and take
+// part from generation gdone + 1 on, transfer partners included.  The layout
+// of the device arrays changes, so the running islands travel through a
+// snapshot: state out, new layout and initial islands in, state back.
+int join_tasks(emt_handle* h, std::vector<HostTask>& add) {
+  const size_t n_old = h->tasks.size();
+  size_t bytes = 0;
+  emt_snapshot_size(h, &bytes);
+  std::vector<unsigned char> before(bytes);
+  int rc = emt_snapshot(h, before.data(), bytes);  // synchronises the handle
+  if (rc) return rc;
+  unsigned long long st[emt::kStats];
+  cudaError_t e = cudaMemcpy(st, h->d_stats.p, sizeof(st), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return h->cuda_fail(e, "copy stats");
+  const uint32_t gdone = h->gdone;
+  const uint64_t joined = h->gen_joined;
+  uint64_t np_new = 0;
+  for (auto& t : add) {
+    np_new += (uint64_t)t.NP;
+    h->tasks.push_back(std::move(t));
+  }
+  h->uploaded = false;
+  h->initialized = false;
+  if ((rc = emt_reset(h, h->stream))) {  // new layout; every island initial
+    // refused (e.g. a form the new islands do not fit): the handle goes back
+    // to its running islands, and the error stays the refusal's
+    const std::string why = h->err;
+    h->tasks.resize(n_old);
+    h->uploaded = false;
+    h->initialized = false;
+    if (!emt_reset(h, h->stream) && !emt_restore(h, before.data(), before.size()) &&
+        cudaMemcpy(h->d_stats.p, st, sizeof(st), cudaMemcpyHostToDevice) == cudaSuccess)
+      h->gen_joined = joined;
+    h->err = why;
+    return rc;
+  }
+  emt_snapshot_size(h, &bytes);
+  std::vector<unsigned char> after(bytes);
+  if ((rc = emt_snapshot(h, after.data(), bytes))) return rc;
+  // the running islands' records, then the new islands' initial ones with
+  // the handle's generation counter
+  std::vector<unsigned char> merged(after.size());
+  const size_t hdr = 3 * sizeof(uint64_t);
+  const size_t old_body = before.size() - hdr;
+  std::memcpy(merged.data(), after.data(), hdr);
+  const uint64_t g64 = gdone;
+  std::memcpy(merged.data() + 2 * sizeof(uint64_t), &g64, sizeof(g64));
+  std::memcpy(merged.data() + hdr, before.data() + hdr, old_body);
+  size_t at = hdr + old_body;
+  std::memcpy(merged.data() + at, after.data() + at, after.size() - at);
+  for (size_t t = n_old; t < h->tasks.size(); ++t) {
+    const HostTask& ht = h->tasks[t];
+    at += (size_t)ht.NP * ht.D * 4 + (size_t)ht.NP * (4 + 4 + 8);
+    std::memcpy(merged.data() + at, &gdone, sizeof(gdone));
+    at += 4;
+  }
+  if ((rc = emt_restore(h, merged.data(), merged.size()))) return rc;
+  st[3] += np_new;  // the new islands' initial evaluation
+  if ((e = cudaMemcpy(h->d_stats.p, st, sizeof(st), cudaMemcpyHostToDevice)) != cudaSuccess)
+    return h->cuda_fail(e, "restore stats");
+  h->gen_joined = joined + (uint64_t)gdone * (h->tasks.size() - n_old);
+  return EMT_OK;
+}
+
 int emt_add_tasks(emt_handle_t* h, int32_t n, const emt_task_desc* td) {
   if (!h) return EMT_ERR_INVALID_ARG;
   const NvtxRange range("emt_add_tasks");
@@ -1050,7 +1121,8 @@ int emt_add_tasks(emt_handle_t* h, int32_t n, const emt_task_desc* td) {
                                                 ": pop must split into sub-islands of >= 4 "
                                                 "members, each sending at most half");
     }
-    if (d.dim <= emt::kMaxDim && (size_t)smem_cap < emt::smem_layout(d.dim, d.pop, false).total)
+    if (d.dim <= emt::kMaxDim && d.pop <= emt::kMaxPop &&
+        (size_t)smem_cap < emt::smem_layout(d.dim, d.pop, false).total)
       return h->fail(EMT_ERR_UNSUPPORTED, "task " + std::to_string(i) +
                                               ": island does not fit in shared memory");
     HostTask ht;
@@ -1147,6 +1219,7 @@ int emt_add_tasks(emt_handle_t* h, int32_t n, const emt_task_desc* td) {
   }
   for (size_t i = 0; i < add.size(); ++i)
     if (bad[i]) return h->fail(EMT_ERR_INVALID_ARG, "task " + std::to_string(i) + ": non-finite rotation");
+  if (h->initialized && !add.empty()) return join_tasks(h, add);
   for (auto& t : add) h->tasks.push_back(std::move(t));
   h->uploaded = false;
   h->initialized = false;
@@ -1170,6 +1243,7 @@ int emt_reset(emt_handle_t* h, void* stream) {
   if (e) return h->cuda_fail((cudaError_t)e, "init launch");
   h->initialized = true;
   h->gdone = 0;
+  h->gen_joined = 0;
   h->elite_parity = 0;
   return EMT_OK;
 }
@@ -1559,7 +1633,7 @@ int emt_get_stats(emt_handle_t* h, emt_stats* out) {
     out->evaluations = s[3];
     out->migrations_accepted = s[7];
     out->recheck_fp64_terms = s[emt::kStatWeierFp64];
-    out->generations = h->initialized ? (uint64_t)h->gdone * h->tasks.size() : 0;
+    out->generations = h->initialized ? (uint64_t)h->gdone * h->tasks.size() - h->gen_joined : 0;
   }
   if (h->initialized && !h->tasks.empty()) {
     // the largest relative error of a task's best FP32 fitness against its

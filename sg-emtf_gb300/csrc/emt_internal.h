@@ -13,7 +13,8 @@ namespace emt {
 constexpr int kThreads = 256;  // one CTA per task, 8 warps
 constexpr int kWarps = kThreads / 32;
 constexpr int kMaxDim = 128;
-constexpr int kMaxPop = 256;
+constexpr int kMaxPop = 256;       // members of a fused (shared-memory) island
+constexpr int kMaxPopLarge = 512;  // members of an HBM-resident island (the reference's 512)
 
 // Per-task descriptor resident in HBM.  Row strides are padded to DP (a
 // multiple of 4 floats) so every population row starts 16-byte aligned and
@@ -41,7 +42,7 @@ enum Mode : int { MODE_EPOCH = 0, MODE_INIT = 1, MODE_EVAL = 2 };
 
 // device counters, indexed as in EpochArgs::stats; [8, 8 + kPhases) hold the
 // per-phase SM cycles of the phase-clock build (EMT_PHASE_CLOCKS)
-constexpr int kPhases = 6;
+constexpr int kPhases = 9;
 // [8 + kPhases]: Weierstrass near ties decided with double-precision terms
 constexpr int kStatWeierFp64 = 8 + kPhases;
 constexpr int kStats = kStatWeierFp64 + 1;
@@ -51,8 +52,16 @@ enum Phase : int {
   PH_ROTATE = 2,   // the rotation (FP32 tiles, or the MMAs and the TMEM drain)
   PH_EVAL = 3,     // the function epilogue: f and its near-tie window
   PH_SELECT = 4,   // FP32 decisions, anchors carried forward, copies of accepted trials
-  PH_RECHECK = 5   // near ties re-decided: differential form, FP64-class tiers
+  PH_RECHECK = 5,  // near ties re-decided: differential form, FP64-class tiers
+  // the tensor-core rotation after its operands are published (PH_ROTATE):
+  PH_MMA_ISSUE = 6,  // the issuing thread's MMA instructions and commit
+  PH_MMA_WAIT = 7,   // from the commit to the completion seen by every warp
+  PH_DRAIN = 8       // accumulators out of tensor memory into the rotated rows
 };
+// MMA descriptors of one island: at most 8 products of parts x 8 K-steps
+// (BF16, K <= 128) or 4 x 16 (TF32); each entry {A and B descriptor low
+// words, accumulator column, accumulate flag}
+constexpr int kMaxMmas = 64;
 
 struct EpochArgs {
   const TaskDev* tasks;
@@ -109,6 +118,7 @@ constexpr int kLargeBN = 256;  // GEMM tile columns (rotated genes), tensor-core
 struct LargeArgs {
   const TaskDev* tasks;
   int32_t n_tasks;
+  int32_t max_np;         // largest island of the handle (sizes the per-row grids)
   int32_t Kp, Nq;        // padded GEMM K (multiple of 32) and N (multiple of 256)
   int32_t tc;            // 1: S holds the TF32 hi part, S + split the lo part
   const int64_t* srow;   // per task: first row of its block in S and Z
@@ -166,7 +176,7 @@ enum SelectMode : int {
 // Dynamic shared memory of the large-island selection kernel: per-warp
 // re-check scratch (2 DP doubles) and the flag/list/target/misc arrays.
 EMT_HD size_t large_select_smem(int DP) {
-  return sizeof(double) * kWarps * 2 * (size_t)DP + sizeof(int) * (4 * kMaxPop + 16);
+  return sizeof(double) * kWarps * 2 * (size_t)DP + sizeof(int) * (4 * kMaxPopLarge + 16);
 }
 
 // Arguments of the standalone evaluation kernel (emt_evaluate).
@@ -228,9 +238,8 @@ EMT_HD Layout smem_layout(int D, int NP, bool qt_in_smem = true) {
 // `planes` split parts of each operand (TF32: hi, lo; BF16: three parts),
 // each part nkb tiles of 128-byte rows (32 TF32 or 64 BF16 values per row):
 // A = planes x nkb tiles of MA rows, B = planes x nkb tiles of Np rows.  With
-// NP <= 64 the A tiles hold 64 rows and an M = 128 MMA reads the next 64
-// rows past each tile (data whose output rows are ignored), so B (or slack)
-// must follow A.  B holds Np = round8(D) rows of Q: an MMA of N = round16(D)
+// NP <= 64 the A tiles hold 64 rows and the MMAs are M = 64; above, 128 rows
+// and M = 128.  B holds Np = round8(D) rows of Q: an MMA of N = round16(D)
 // columns reads up to 8 rows past a part, whose output columns (>= D) are
 // never used.  The FP32 rotated rows Z alias the A region once the MMAs have
 // completed.  The last kTcHeader bytes of the launch's allocation hold the
@@ -248,7 +257,7 @@ static_assert(sizeof(TcHeader) <= kTcHeader, "tensor-core header");
 
 struct TcLayout {
   int DP, Np, Kp, nkb, MA, planes, epr;
-  size_t A, B, fit64, z64, X, U, o, fit, tol, ftr, ttr, idx, flag, list, misc, total;
+  size_t A, B, fit64, z64, X, U, o, fit, tol, ftr, ttr, idx, flag, list, misc, mdesc, total;
 };
 
 EMT_HD TcLayout tc_layout(int D, int NP, int Np, int Kp, bool bf16) {
@@ -264,8 +273,7 @@ EMT_HD TcLayout tc_layout(int D, int NP, int Np, int Kp, bool bf16) {
   L.A = off;
   off += (size_t)L.planes * L.nkb * L.MA * 128;
   L.B = off;
-  const size_t bsz = (size_t)L.planes * L.nkb * Np * 128, slack = (size_t)(128 - L.MA) * 128;
-  off += bsz > slack ? bsz : slack;
+  off += (size_t)L.planes * L.nkb * Np * 128;
   L.fit64 = off; off = align16(off + sizeof(double) * NP);
   // FP64 re-check scratch: idle A-region space past Z (the re-checks run
   // after the epilogue has consumed Z and before the next operands are staged)
@@ -288,6 +296,7 @@ EMT_HD TcLayout tc_layout(int D, int NP, int Np, int Kp, bool bf16) {
   L.flag = off;  off = align16(off + sizeof(int) * NP);
   L.list = off;  off = align16(off + sizeof(int) * NP);
   L.misc = off;  off = align16(off + sizeof(int) * 8);
+  L.mdesc = off; off = align16(off + sizeof(uint32_t) * 4 * kMaxMmas);
   L.total = off + kTcHeader;  // the header closes the allocation
   return L;
 }

@@ -1,5 +1,5 @@
-// emt_kernels.cu -- the fused generation kernel (FP32 CUDA-core rotation form)
-// and the standalone evaluation kernel.
+// emt_kernels.cu -- the fused generation kernel (FP32 CUDA-core and tcgen05
+// tensor-core rotation forms) and the standalone evaluation kernel.
 //
 // One CTA owns one task for a whole epoch (all generations between two elite
 // transfers).  Its island lives in shared memory across generations, as the
@@ -12,13 +12,16 @@
 //   1. trial vectors: DE/rand/1/bin, DE/current/1/bin or SBX + polynomial
 //      mutation, from the counter-based Philox stream (bit-exact with the
 //      host replay);
-//   2. rotation Z = (U - o) Q^T, in one of two forms:
-//      FP32: 4x4 register tiles on CUDA cores, float4 operand loads;
-//      TC:   tcgen05 MMA, kind::tf32, with hi/lo split operands (3 products,
-//            FP32 accumulation in tensor memory); the trial builder writes the
-//            split A operand into 128B-swizzled shared memory tiles, the Q
-//            tiles arrive by TMA once per epoch;
-//   3. function epilogue: one warp per trial, FP32 value + error scale;
+//   2. rotation Z = (U - o) Q^T, in one of three forms:
+//      FP32:   4x4 register tiles on CUDA cores, float4 operand loads;
+//      BF16X3: tcgen05 MMA, kind::f16, both operands split exactly into
+//              three BF16 parts, eight products of parts;
+//      TF32X3: tcgen05 MMA, kind::tf32, hi/lo TF32 parts, four products;
+//      (FP32 accumulation in tensor memory, the leading product in its own
+//      accumulator; the trial builder writes the split A operand into
+//      128B-swizzled shared-memory tiles, Q's parts arrive by TMA once per
+//      island);
+//   3. function epilogue: f and its rounding-error scale per trial;
 //   4. selection (ties go to the trial, SG-EMTF_DE.cu:679-706): a trial whose
 //      FP32 fitness lies within the rounding window of its parent's is
 //      re-decided in FP64 so that selections do not depend on FP32 rounding.
@@ -56,6 +59,15 @@ struct PhaseClock {
       cur = next;
     }
   }
+  // thread 0 alone (no barrier): the rest of the current phase is `next`
+  __device__ __forceinline__ void lap(int next) {
+    if (threadIdx.x == 0) {
+      const long long t = clock64();
+      acc[cur] += t - t0;
+      t0 = t;
+      cur = next;
+    }
+  }
   __device__ __forceinline__ void flush(unsigned long long* stats) {
     mark(PH_OTHER);
     if (threadIdx.x == 0 && stats)
@@ -66,9 +78,14 @@ struct PhaseClock {
   do {                      \
     if ((s).ph) (s).ph->mark(k); \
   } while (0)
+#define EMT_PHASE_LAP(s, k) \
+  do {                          \
+    if ((s).ph) (s).ph->lap(k); \
+  } while (0)
 #else
 struct PhaseClock {};
 #define EMT_PHASE(s, k) ((void)0)
+#define EMT_PHASE_LAP(s, k) ((void)0)
 #endif
 
 struct Smem {
@@ -79,11 +96,17 @@ struct Smem {
   // tensor-core form
   unsigned char *A, *B;
   uint32_t a_saddr, b_saddr, mma_bar, tma_bar, tmem;
-  uint32_t acc2;  // TMEM column offset of the second accumulator
+  uint32_t acc_cols;  // TMEM columns per accumulator (accumulator k starts at k * acc_cols)
+  int nacc;           // accumulators: the leading product's, then 1 or 3 for the others
   int MA, nkb, Np, N, ksteps;
   int planes;     // split parts per operand: 2 (TF32 hi/lo) or 3 (BF16)
   bool bf16;      // exact 3 x BF16 split, kind::f16 MMAs
   uint32_t idesc;
+  // the island's MMAs in issue order (mma_descriptors): descriptor low
+  // words, accumulator column and accumulate flag in shared memory; the
+  // descriptors' high words are the same for every MMA
+  const uint4* mdesc;
+  uint32_t ad_hi, bd_hi;
   int* dead;         // CTA-wide: a bounded wait gave up (the MMAs are skipped)
   uint64_t wait_ns;  // limit of each bounded wait
   bool lose_completion;  // test switch: issue no MMA and no commit
@@ -98,6 +121,7 @@ struct Smem {
 struct TcCta {
   TcHeader* hdr;
   uint32_t tmem, ncols, mma_bar, tma_bar;
+  uint32_t acc_cols, nacc;  // accumulators of acc_cols TMEM columns each
   uint32_t mphase, tphase;  // parity each barrier completes next
 };
 
@@ -123,6 +147,7 @@ __device__ __forceinline__ Smem carve_tc(unsigned char* base, const TcLayout& L)
   s.flag = (int*)(base + L.flag);
   s.list = (int*)(base + L.list);
   s.misc = (int*)(base + L.misc);
+  s.mdesc = (const uint4*)(base + L.mdesc);
   s.a_saddr = tc::smem_addr(s.A);
   s.b_saddr = tc::smem_addr(s.B);
   s.MA = L.MA;
@@ -348,6 +373,39 @@ __device__ void zero_pads(const Smem& s, int D, int nrows) {
   }
 }
 
+// The island's MMAs in issue order, written once per island by all threads
+// (read after the next barrier).  Products of parts (a of s, b of Q), the
+// leading one first; BF16 takes eight of the nine (s2 q2, at most 2^-32 of
+// s0 q0, is below the FP32 accumulation's own rounding).  The leading
+// product accumulates alone in accumulator 0.  With four accumulators the
+// others go round-robin to accumulators 1-3, with two all to accumulator 1.
+// The issue order is K-step outer, product inner, so consecutive MMAs
+// mostly update different accumulators.  Each descriptor is the tile's base
+// descriptor plus the K-step's offset >> 4 in the start-address field (bits
+// 0-13: shared addresses stay below 256 KB, so there is no carry and the
+// high words are the base descriptors').
+__device__ __noinline__ void mma_descriptors(uint4* tab, uint32_t a_saddr, uint32_t b_saddr,
+                                             int MA, int Np, int planes, int nkb, int ksteps,
+                                             uint32_t acc_cols, int nacc) {
+  const uint64_t a0 = tc::sdesc_sw128(a_saddr), b0 = tc::sdesc_sw128(b_saddr);
+  const uint32_t pa = 0x21201100u, pb = 0x12021010u;  // parts per product, 4 bits each
+  const uint32_t atile = (uint32_t)MA * 8u, btile = (uint32_t)Np * 8u;  // (rows x 128 B) >> 4
+  const int nprod = planes == 3 ? 8 : 4;
+  const int n = nprod * ksteps;
+  for (int i = threadIdx.x; i < n && i < kMaxMmas; i += kThreads) {
+    const int st = i / nprod, p = i - st * nprod;
+    const uint32_t kb = (uint32_t)st >> 2, ks = (uint32_t)st & 3u;
+    const uint32_t ap = (pa >> (4 * p)) & 15u, bp = (pb >> (4 * p)) & 15u;
+    const uint64_t ad = a0 + ((kb * (uint32_t)planes + ap) * atile + 2u * ks);
+    const uint64_t bd = b0 + ((bp * (uint32_t)nkb + kb) * btile + 2u * ks);
+    const uint32_t k = p == 0 ? 0u : nacc == 4 ? 1u + (uint32_t)(p - 1) % 3u : 1u;
+    // the first MMA into each accumulator overwrites it: products 0 .. nacc-1
+    // of K-step 0 are the first of their accumulators
+    const uint32_t accumulate = (st > 0 || p >= nacc) ? 1u : 0u;
+    tab[i] = make_uint4((uint32_t)ad, (uint32_t)bd, k * acc_cols, accumulate);
+  }
+}
+
 // Tensor-core rotation of rows [0, nrows) staged with their pad columns:
 // tcgen05 MMAs over the K steps that cover D (32 bytes of each 128-byte row
 // per step: 8 TF32 or 16 BF16 values), one issuing thread, completion on an
@@ -364,55 +422,66 @@ __device__ void rotate_tc(const Smem& s, int D, int DP, int nrows, uint32_t& pha
   tc::fence_async_smem();  // generic-proxy operand writes -> async proxy
   __syncthreads();
   const bool dead = *s.dead != 0;  // an earlier wait gave up: skip the MMAs
+  EMT_PHASE(s, PH_MMA_ISSUE);
   if (threadIdx.x == 0 && !dead && !s.lose_completion) {
     tc::fence_after();
-    // products of parts (a, b): the leading one first, alone in accumulator 0.
-    // BF16: eight of the nine; s2 q2 (<= 2^-32 of s0 q0) is below the FP32
-    // accumulation's own rounding
-    const int pa[8] = {0, 0, 1, 1, 0, 2, 1, 2}, pb[8] = {0, 1, 0, 1, 2, 0, 2, 1};
-    const int nprod = s.bf16 ? 8 : 4;
-    // descriptors: the start address field (bits 0-13, address >> 4) of the
-    // tiles' base descriptors plus each step's offset >> 4 (no carry: shared
-    // addresses stay below 256 KB)
-    const uint64_t a0 = tc::sdesc_sw128(s.a_saddr), b0 = tc::sdesc_sw128(s.b_saddr);
-    const uint32_t atile = (uint32_t)s.MA * 8u, btile = (uint32_t)s.Np * 8u;  // (rows x 128 B) >> 4
-    for (int p = 0; p < nprod; ++p) {
-      const uint32_t d = s.tmem + (p ? s.acc2 : 0u);
-      for (int st = 0; st < s.ksteps; ++st) {
-        const uint32_t kb = (uint32_t)st >> 2, ks = (uint32_t)st & 3u;
-        const uint64_t ad = a0 + ((kb * (uint32_t)s.planes + (uint32_t)pa[p]) * atile + 2u * ks);
-        const uint64_t bd = b0 + (((uint32_t)pb[p] * (uint32_t)s.nkb + kb) * btile + 2u * ks);
-        const uint32_t acc = (st > 0 || p > 1) ? 1u : 0u;
-        if (s.bf16)
-          tc::mma_bf16(d, ad, bd, s.idesc, acc);
-        else
-          tc::mma_tf32(d, ad, bd, s.idesc, acc);
-      }
+    // the descriptor table (mma_descriptors) in issue order: the leading
+    // product alone into accumulator 0, then the others into accumulator 1
+    const int n = (s.bf16 ? 8 : 4) * s.ksteps;
+    for (int i = 0; i < n; ++i) {
+      const uint4 w = s.mdesc[i];
+      const uint64_t ad = ((uint64_t)s.ad_hi << 32) | w.x, bd = ((uint64_t)s.bd_hi << 32) | w.y;
+      if (s.bf16)
+        tc::mma_bf16(s.tmem + w.z, ad, bd, s.idesc, w.w);
+      else
+        tc::mma_tf32(s.tmem + w.z, ad, bd, s.idesc, w.w);
     }
     tc::mma_commit(s.mma_bar);
   }
+  EMT_PHASE_LAP(s, PH_MMA_WAIT);
+  // Each warp that drains rows waits for the completion itself, so no CTA
+  // barrier stands between the completion and the drain; the others go on
+  // to the closing barrier.  A wait that gives up marks the CTA dead; its
+  // warp writes finite zeros instead, and the epoch stops at the end of this
+  // generation with CHECK_TIMEOUT reported.
+  // TMEM holds row r of an M = 128 result in lane r; an M = 64 result puts
+  // rows 16q .. 16q + 15 in lanes 32q .. 32q + 15 of sub-partition q
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (!dead && warp == 0) {
-    if (!tc::mbar_wait(s.mma_bar, phase, s.wait_ns)) atomicExch(s.dead, 1);
-  }
-  if (!dead) phase ^= 1u;
-  __syncthreads();
-  tc::fence_after();
-  if (*s.dead) {
-    // no valid accumulator: finite zeros, and the epoch stops at the end of
-    // this generation with CHECK_TIMEOUT reported
-    for (int it = threadIdx.x; it < nrows * DP; it += kThreads) s.Z[it] = 0.f;
-  } else if (32 * (warp & 3) < nrows) {  // warp-uniform: the loads are .sync.aligned
-    const int q = warp & 3, row = 32 * q + lane;
+  const int rpq = s.MA >> 2;  // rows per sub-partition: 16 or 32
+  if (rpq * (warp & 3) < nrows) {  // warp-uniform: the loads are .sync.aligned
+    bool ok = !dead;
+    if (ok) {
+      ok = tc::mbar_wait(s.mma_bar, phase, s.wait_ns);
+      ok = __all_sync(0xFFFFFFFFu, ok);
+      if (!ok && lane == 0) atomicExch(s.dead, 1);
+      if (ok) tc::fence_after();
+    }
+    EMT_PHASE_LAP(s, PH_DRAIN);
+    const int q = warp & 3, row = lane < rpq ? rpq * q + lane : nrows;  // nrows: no row
     const int nch = s.N >> 4, half = (nch + 1) >> 1;
     const int c_lo = (warp >> 2) ? half : 0, c_hi = (warp >> 2) ? nch : half;
     for (int c = c_lo; c < c_hi; ++c) {
       const int c0 = 16 * c;
       float v[16], w[16];
-      tc::tmem_ld16(s.tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, v);
-      tc::tmem_ld16(s.tmem + ((uint32_t)(32 * q) << 16) + s.acc2 + (uint32_t)c0, w);
+      if (ok) {
+        // the small products' accumulators first, then the leading one
+        const uint32_t t0 = s.tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c0;
+        tc::tmem_ld16(t0 + s.acc_cols, w);
+        if (s.nacc == 4) {
+          tc::tmem_ld16(t0 + 2u * s.acc_cols, v);
 #pragma unroll
-      for (int g = 0; g < 16; ++g) v[g] = __fadd_rn(v[g], w[g]);
+          for (int g = 0; g < 16; ++g) w[g] = __fadd_rn(w[g], v[g]);
+          tc::tmem_ld16(t0 + 3u * s.acc_cols, v);
+#pragma unroll
+          for (int g = 0; g < 16; ++g) w[g] = __fadd_rn(w[g], v[g]);
+        }
+        tc::tmem_ld16(t0, v);
+#pragma unroll
+        for (int g = 0; g < 16; ++g) v[g] = __fadd_rn(v[g], w[g]);
+      } else {
+#pragma unroll
+        for (int g = 0; g < 16; ++g) v[g] = 0.f;
+      }
       if (row < nrows)
 #pragma unroll
         for (int g = 0; g < 4; ++g)
@@ -421,6 +490,7 @@ __device__ void rotate_tc(const Smem& s, int D, int DP, int nrows, uint32_t& pha
                 make_float4(v[4 * g], v[4 * g + 1], v[4 * g + 2], v[4 * g + 3]);
     }
   }
+  if (!dead) phase ^= 1u;
   tc::fence_before();
   __syncthreads();
 }
@@ -834,7 +904,8 @@ __device__ __forceinline__ void epoch_body(const EpochArgs& a, const void* tmap,
     s.mma_bar = cta.mma_bar;
     s.tma_bar = cta.tma_bar;
     s.tmem = cta.tmem;
-    s.acc2 = cta.ncols / 2;
+    s.acc_cols = cta.acc_cols;
+    s.nacc = (int)cta.nacc;
     s.dead = &cta.hdr->dead;
     s.wait_ns = a.wait_ns ? a.wait_ns : tc::kWaitLimitNs;
     s.lose_completion = (a.flags & FLAG_TEST_LOST_COMPLETION) != 0;
@@ -843,7 +914,12 @@ __device__ __forceinline__ void epoch_body(const EpochArgs& a, const void* tmap,
     NPP = round4(NP);
     s.N = round16(D);
     s.ksteps = s.bf16 ? (D + 15) >> 4 : (D + 7) >> 3;
-    s.idesc = s.bf16 ? tc::idesc_bf16(128, s.N) : tc::idesc_tf32(128, s.N);
+    // M = 64 for islands of <= 64 members (the A tiles' own rows), else 128
+    s.idesc = s.bf16 ? tc::idesc_bf16(s.MA, s.N) : tc::idesc_tf32(s.MA, s.N);
+    mma_descriptors(const_cast<uint4*>(s.mdesc), s.a_saddr, s.b_saddr, s.MA, s.Np, s.planes,
+                    s.nkb, s.ksteps, s.acc_cols, s.nacc);
+    s.ad_hi = (uint32_t)(tc::sdesc_sw128(s.a_saddr) >> 32);
+    s.bd_hi = (uint32_t)(tc::sdesc_sw128(s.b_saddr) >> 32);
     // zero the operand tiles once: padded K columns meet zero Q columns, so
     // they only need to hold finite values
     for (size_t it = threadIdx.x; it < (L.B - L.A) / 16; it += kThreads)
@@ -1041,9 +1117,13 @@ __device__ __forceinline__ void tc_cta_begin(const EpochArgs& a, unsigned char* 
   cta.hdr = reinterpret_cast<TcHeader*>(smem_raw + a.smem_bytes - kTcHeader);
   cta.mma_bar = tc::smem_addr(&cta.hdr->mma_bar);
   cta.tma_bar = tc::smem_addr(&cta.hdr->tma_bar);
+  // accumulators of N <= 64 columns come four to a CTA (256 columns), wider
+  // ones two: two CTAs per SM stay within the SM's 512 columns
   uint32_t half = 32;
   while (half < (uint32_t)round16(a.tc_np)) half <<= 1;
-  cta.ncols = 2 * half;
+  cta.acc_cols = half;
+  cta.nacc = half <= 64 ? 4u : 2u;
+  cta.ncols = cta.nacc * half;
   cta.mphase = cta.tphase = 0;
   if (threadIdx.x == 0) {
     tc::mbar_init(cta.mma_bar, 1);

@@ -1,5 +1,6 @@
 // emt_large.cuh -- islands too large for one CTA's shared memory (D up to
-// 1024; config 4: D = 1000, NP = 256, GA).  Included at the end of
+// 1024 or NP up to 512; D = 1000, NP = 256 GA islands, or the reference's
+// D = 50, NP = 512 GA islands).  Included at the end of
 // emt_kernels.cu, whose selection and ranking code it reuses.
 //
 // A generation is a pipeline of kernels over HBM-resident islands:
@@ -20,7 +21,7 @@ namespace emt {
 namespace large {
 
 __device__ __forceinline__ bool large_ok(const TaskDev& t) {
-  return t.D >= 1 && t.D <= kMaxDimLarge && t.NP >= 4 && t.NP <= kMaxPop && t.DP == round4(t.D);
+  return t.D >= 1 && t.D <= kMaxDimLarge && t.NP >= 4 && t.NP <= kMaxPopLarge && t.DP == round4(t.D);
 }
 
 __device__ __forceinline__ FnConst fn_const(const TaskDev& td, float rel) {
@@ -607,9 +608,9 @@ __global__ void __launch_bounds__(256) select_kernel(const LargeArgs a, int mode
   s.z64 = reinterpret_cast<double*>(smraw);
   int* ip = reinterpret_cast<int*>(s.z64 + (size_t)kWarps * 2 * DP);
   s.flag = ip;
-  s.list = ip + kMaxPop;
-  s.idx = ip + 2 * kMaxPop;  // targets (transfer)
-  s.misc = ip + 4 * kMaxPop;
+  s.list = ip + kMaxPopLarge;
+  s.idx = ip + 2 * kMaxPopLarge;  // targets (transfer)
+  s.misc = ip + 4 * kMaxPopLarge;
   s.X = a.pop + td.pop_off;
   s.U = a.U + td.pop_off;
   s.fit = a.fit32 + td.fit_off;
@@ -731,8 +732,8 @@ constexpr int kRotCols = 128;  // outputs per item: one per thread of a 128-thre
 // task: blocks x chunks <= (1024 / 128) x ceil(2 NP / 8) <= 2 NP + 8, within
 // the host's 2 fit + 8 T allocation.
 static_assert((kMaxDimLarge + kRotCols - 1) / kRotCols <= 16, "column block in 4 bits");
-static_assert((2 * kMaxPop + kRotJobs - 1) / kRotJobs < 4096, "job chunk in 12 bits");
-static_assert(2 * kMaxPop + 1 < 0xFFFF, "job and tie indices in 16 bits");
+static_assert((2 * kMaxPopLarge + kRotJobs - 1) / kRotJobs < 4096, "job chunk in 12 bits");
+static_assert(2 * kMaxPopLarge + 1 < 0xFFFF, "job and tie indices in 16 bits");
 static_assert(kRotCols >= kRotJobs && kRotCols % 32 == 0, "row pointers set by the first threads");
 
 __global__ void __launch_bounds__(256) classify_kernel(const LargeArgs a, int mode) {
@@ -1062,13 +1063,13 @@ int emt_large_init(const emt::LargeArgs& a, void* stream) {
 }
 
 int emt_large_build(const emt::LargeArgs& a, int mode, void* stream) {
-  const int gx = (emt::kMaxPop + emt::large::kBuildRows - 1) / emt::large::kBuildRows;
+  const int gx = (a.max_np + emt::large::kBuildRows - 1) / emt::large::kBuildRows;
   emt::large::build_kernel<<<dim3(gx, a.n_tasks), 256, 0, (cudaStream_t)stream>>>(a, mode);
   return (int)cudaGetLastError();
 }
 
 int emt_large_gemm(const emt::LargeArgs& a, const void* smap, const void* qmap, void* stream) {
-  const int gy = emt::kMaxPop / emt::kLargeBM;
+  const int gy = (a.max_np + emt::kLargeBM - 1) / emt::kLargeBM;
   if (a.tc) {
     static_assert(emt::large::kGemmTcSmem <= 227 * 1024, "tile pipeline");
     cudaError_t e = cudaFuncSetAttribute(emt::large::gemm_tc_kernel,
@@ -1086,7 +1087,7 @@ int emt_large_gemm(const emt::LargeArgs& a, const void* smap, const void* qmap, 
 }
 
 int emt_large_eval(const emt::LargeArgs& a, int which, int rows, void* stream) {
-  const int gx = (emt::kMaxPop + 7) / 8;
+  const int gx = (a.max_np + 7) / 8;
   emt::large::eval_kernel<<<dim3(gx, a.n_tasks), 256, 0, (cudaStream_t)stream>>>(a, which, rows);
   return (int)cudaGetLastError();
 }

@@ -37,7 +37,8 @@ FLAG_RIGOROUS_WINDOW = 0x20
 FLAG_NO_DIFF_RECHECK = 0x40
 FLAG_TEST_LOST_COMPLETION = 0x80
 SCHEDULE_AUTO, SCHEDULE_SINGLE, SCHEDULE_BUCKETS, SCHEDULE_PER_TASK, SCHEDULE_QUEUE = 0, 1, 2, 3, 4
-MAX_DIM, MAX_POP = 128, 256
+MAX_DIM, MAX_POP = 128, 256  # fused islands; larger ones run the HBM-resident pipeline
+MAX_DIM_LARGE, MAX_POP_LARGE = 1024, 512
 NOALLOC_EXCHANGE_FLOATS = 1 << 19
 
 EXPORTED = [
@@ -340,7 +341,11 @@ class Engine:
     def sync(self):
         self._check(lib().emt_sync(self._h), "emt_sync")
 
-    PHASES = ["other", "build", "rotate", "eval", "select", "recheck"]
+    # "rotate" is the FP32 rotation, or the tensor-core forms' operand hand-off;
+    # their MMAs, the wait for them and the accumulator drain follow
+    PHASES = ["other", "build", "rotate", "eval", "select", "recheck", "mma_issue", "mma_wait",
+              "drain"]
+    ROTATION_PHASES = ("rotate", "mma_issue", "mma_wait", "drain")
 
     def phase_cycles(self):
         """emt_get_phase_cycles (measurement build only): SM cycles per phase."""

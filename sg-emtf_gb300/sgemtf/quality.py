@@ -8,11 +8,19 @@ types come from glibc srand(0); rand() % 7 with task 0 forced to type 6
 (proposed model/SG-EMTF.cu:307-313); D = 50; diagonal instances
 z = M (x + b), M ~ U(0, 1], b ~ U(0, box width] (:181-195); the reference's
 box table and function variants (:197-214, :1029, :354-361, E = 2.718282);
-its GA (SBX eta 2 with every gene crossed, polynomial mutation eta 5 on every
-gene, :44-49,555,718); best fitness recorded every 50 of 1000 generations.
-Elite transfer is off, as in the shipped reference (:1714).  Islands hold
-256 members, the largest this engine serves; the reference evolved 512 per
-task in 32-member blocks."""
+its GA: SBX eta 2 with every gene crossed (:44-49, 718) and polynomial
+mutation eta 5 (:49); best fitness recorded every 50 of 1000 generations.
+Elite transfer is off, as in the shipped reference (:1714).  Each task has
+the reference's 512 members (:29, INDIVNUM) in 4 islands of 128 (:30, :39)
+that exchange 32 members every 25 generations (:36, :56); islands of more
+than 256 members run the engine's HBM-resident pipeline.
+
+Two mutation probabilities.  The GA file mutates every gene (P = 1.f,
+SG-EMTF.cu:555); its DE variant mutates each gene with P = 1/DIMENSION
+(SG-EMTF_DE.cu:481).  The recorded GA runs match the second: with P = 1/D
+the median best of every function type lies near the recorded one, with
+P = 1 Schwefel and Weierstrass end several times worse.  RECORDED_GA is the
+default; SHIPPED_GA keeps the GA file's own value."""
 import ctypes
 
 import numpy as np
@@ -49,18 +57,35 @@ def reference_instances(types, D, seed=0):
     return out
 
 
-def run(seeds=30, tasks=100, D=50, pop=256, generations=1000, interval=50, device=0,
-        first_seed=1, subislands=1, migration_interval=0, migration_count=0, instance_seed=0):
+# the GA operators as the GA file ships them (SG-EMTF.cu:44-49, 555, 718)
+SHIPPED_GA = dict(algorithm=GA, eta_c=2.0, p_c=1.0, eta_m=5.0, p_m=1.0)
+# the same with the DE variant's mutation probability 1/D (SG-EMTF_DE.cu:481;
+# p_m < 0 means 1/D): the setting the recorded runs match
+RECORDED_GA = dict(SHIPPED_GA, p_m=-1.0)
+# 512 members as 4 islands of 128, 32 migrants every 25 generations
+# (SG-EMTF.cu:29-30, 36, 39, 56)
+REFERENCE_LAYOUT = dict(pop=512, subislands=4, migration_interval=25, migration_count=32)
+
+
+def run(seeds=30, tasks=100, D=50, generations=1000, interval=50, device=0, first_seed=1,
+        instance_seed=0, operators=None, **layout):
     """Records of `seeds` runs: array [seeds, tasks, generations/interval + 2]
-    (best fitness at each recording point, then the initial near-worst)."""
+    (best fitness at each recording point, then the initial near-worst).
+    `operators`: Config fields (algorithm, F, CR, eta_c, p_c, eta_m, p_m)
+    over RECORDED_GA; `layout` (pop, subislands, migration_interval,
+    migration_count) over REFERENCE_LAYOUT."""
     types = reference_types(tasks)
     inst = reference_instances(types, D, instance_seed)
     rec = np.zeros((seeds, tasks, generations // interval + 2), np.float32)
+    ops = dict(RECORDED_GA, **(operators or {}))
+    lay = dict(REFERENCE_LAYOUT, **layout)
+    pop = lay.pop("pop")
+    subislands, migration_interval, migration_count = (
+        lay["subislands"], lay["migration_interval"], lay["migration_count"])
     for s in range(seeds):
-        eng = Engine(Config(seed=first_seed + s, algorithm=GA, eta_c=2.0, p_c=1.0, eta_m=5.0,
-                            p_m=1.0, flags=REF_FLAGS, device=device, subislands=subislands,
-                            migration_interval=migration_interval,
-                            migration_count=migration_count))
+        eng = Engine(Config(seed=first_seed + s, flags=REF_FLAGS, device=device,
+                            subislands=subislands, migration_interval=migration_interval,
+                            migration_count=migration_count, **ops))
         eng.add_tasks([TaskDesc(fid, D, pop, rotation=ROTATION_DIAG, diag=M, shift=-b)
                        for fid, M, b in inst])
         eng.reset()

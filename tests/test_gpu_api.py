@@ -89,7 +89,7 @@ def test_invalid_arguments(sgemtf):
     assert e.value.status == sgemtf.ERR_STATE
     for bad in [dict(function=9, dim=4, pop=8), dict(function=0, dim=0, pop=8),
                 dict(function=0, dim=1025, pop=8), dict(function=0, dim=4, pop=3),
-                dict(function=0, dim=4, pop=257)]:
+                dict(function=0, dim=4, pop=513)]:
         with pytest.raises(sgemtf.EngineError) as e:
             eng.add_tasks([sgemtf.TaskDesc(**bad)])
         assert e.value.status == sgemtf.ERR_INVALID_ARG

@@ -44,6 +44,36 @@ def test_large_replay_bit_exact(sgemtf, orc, precision, alg):
     eng.close()
 
 
+# islands of the reference's 512 members (SG-EMTF.cu:29, INDIVNUM): any
+# NP > 256 sends the handle through the same pipeline at D <= 128
+SPECS512 = [(0, 50, 512, 1), (5, 50, 512, 1), (6, 20, 300, 1), (2, 50, 260, 1), (1, 8, 16, 1)]
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("alg", [0, 2])
+def test_np512_replay_bit_exact(sgemtf, orc, precision, alg):
+    kw = dict(algorithm=alg)
+    if alg == 2:  # the reference's GA: SBX eta 2 on every gene, PM eta 5 on every gene
+        kw.update(eta_c=2.0, p_c=1.0, eta_m=5.0, p_m=1.0)
+    try:
+        eng, tasks = make_engine(sgemtf, orc, SPECS512, seed=23, precision=precision, **kw)
+    except sgemtf.EngineError as e:
+        pytest.skip(str(e))
+    eng.reset()
+    X0 = [eng.population(i)[0] for i in range(len(tasks))]
+    gens = 5
+    eng.run(gens)
+    want = replay(orc, oracle_params(orc, eng), tasks, X0, gens)
+    for i in range(len(tasks)):
+        got = eng.population(i)[0]
+        assert got.shape == (tasks[i].NP, tasks[i].D)
+        assert np.array_equal(got, want[i]), (precision, alg, i, np.argwhere(got != want[i])[:5])
+    st = eng.stats()
+    assert st["evaluations"] == sum(t.NP for t in tasks) * (gens + 1)
+    assert st["precision_used"] == (sgemtf.ROT_TF32X3 if precision else sgemtf.ROT_FP32)
+    eng.close()
+
+
 @pytest.mark.parametrize("precision", [0, 1])
 def test_large_fitness_within_window(sgemtf, orc, precision):
     eng, tasks = engine(sgemtf, orc, precision)

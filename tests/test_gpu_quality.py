@@ -1,21 +1,28 @@
 """Statistical quality against the reference's own recorded runs: 30 seeded
-runs of the reference's GA setting (sgemtf/quality.py) beside its 18 recorded
-runs of 100 tasks (data process/ANO_Tnum/data_record_T_ANO_100.txt) and the
-ANO curve its tool computed from them.
+runs of the reference's GA setting (sgemtf/quality.py: 100 tasks, D = 50,
+512 members in 4 islands of 128) beside its 18 recorded runs of 100 tasks
+(data process/ANO_Tnum/data_record_T_ANO_100.txt) and the ANO curve its tool
+computed from them.
 
-Stated tolerances (measured; 30 seeds, five instance draws):
-  - ANO, the reference's own figure of merit: within 0.1 absolute at every
-    recording point (measured <= 0.08) and within 25 % at generation 1000
-    (measured 0.039-0.046 against 0.0367);
-  - median best fitness at generation 1000 per function type, ours over the
-    reference's: within [0.5, 2] for sphere, rosenbrock, ackley, rastrigin
-    and griewank (measured 0.95-1.73); Weierstrass within 3 (measured
-    2.4-2.5) and Schwefel within 8 (measured 5.6-6.4).  The last two stay
-    outside a tight bound whatever the island layout: panmictic islands of
-    64, 256 and 512, and 8-member groups regrouped every generation as the
-    reference's blocks are (SG-EMTF.cu:856-896,1220-1260), all end Schwefel
-    near the same value on the oracle, so the recorded runs' configuration
-    differs from the shipped one there."""
+Which setting the recorded runs came from.  The GA file mutates every gene
+(P = 1.f, proposed model/SG-EMTF.cu:555); its DE variant mutates each gene
+with probability 1/DIMENSION (SG-EMTF_DE.cu:481).  With 1/D (RECORDED_GA)
+the median best of every function type lands near the recorded one and the
+ANO curve follows the recorded curve within 0.01; with every gene mutated
+(SHIPPED_GA) Schwefel ends ~5x and Weierstrass ~2.3x above the record.
+So the recorded runs used the 1/D mutation probability.
+
+Stated tolerances (measured; 30 seeds):
+  - RECORDED_GA, median best at generation 1000 per reference type, ours
+    over the reference's: at most 2 for every type (measured 0.88-1.17 for
+    six types).  Schwefel ends better than the record: 0.48 on this instance
+    draw, 0.44-1.04 over three draws (8 of the 100 tasks are Schwefel, so
+    their instances move its median), hence a lower bound of 0.35.  The
+    other types stay within [0.5, 2];
+  - RECORDED_GA, ANO: within 0.03 absolute at every recording point
+    (measured 0.009);
+  - SHIPPED_GA: Schwefel above 3 and Weierstrass above 2 (measured about
+    5.3 and 2.3): the shipped probability does not give the recorded runs."""
 import json
 import os
 
@@ -24,40 +31,59 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 HERE = os.path.dirname(os.path.abspath(__file__))
-BOUNDS = {0: 2.0, 1: 2.0, 2: 2.0, 3: 2.0, 4: 2.0, 5: 3.0, 6: 8.0}  # by reference type
+WEIERSTRASS, SCHWEFEL = 5, 6  # reference types
+LOWER = {t: (0.35 if t == SCHWEFEL else 0.5) for t in range(7)}
+UPPER = {t: 2.0 for t in range(7)}
+
+
+def _reference():
+    with open(os.path.join(HERE, "golden", "reference_records_T100.json")) as f:
+        d = json.load(f)
+    with open(os.path.join(HERE, "golden", "reference_ano_T100.json")) as f:
+        ano = np.array([float(v) for v in json.load(f)["ano"]])
+    return np.array(d["runs"]), np.array(d["types"]), ano
+
+
+def _ratios(types, summary, runs, rtypes):
+    assert list(types) == list(rtypes)
+    return {rt: v["median"] / float(np.median(runs[:, rtypes == rt, 1]))
+            for rt, v in summary["per_type"].items()}
 
 
 @pytest.fixture(scope="module")
-def harness(sgemtf):
+def recorded(sgemtf):
     from sgemtf import quality
-    types, rec = quality.run(seeds=30)
+    types, rec = quality.run(seeds=30, operators=quality.RECORDED_GA)
     return types, rec, quality.summarise(types, rec)
 
 
-def test_ano_tracks_the_reference(harness):
-    with open(os.path.join(HERE, "golden", "reference_ano_T100.json")) as f:
-        ref = np.array([float(v) for v in json.load(f)["ano"]])
-    ano = np.array(harness[2]["ano"])
+def test_ano_tracks_the_reference(recorded):
+    _, _, ref = _reference()
+    ano = np.array(recorded[2]["ano"])
     assert ano.shape == ref.shape == (21,)
-    assert np.abs(ano - ref).max() <= 0.1
-    assert abs(ano[-1] / ref[-1] - 1.0) <= 0.25
+    assert np.abs(ano - ref).max() <= 0.03
     assert (np.diff(ano) <= 1e-6).all()  # normalised progress never reverses
 
 
-def test_final_medians_by_type(harness):
-    with open(os.path.join(HERE, "golden", "reference_records_T100.json")) as f:
-        d = json.load(f)
-    runs, rtypes = np.array(d["runs"]), np.array(d["types"])
-    types, _, s = harness
-    assert list(types) == list(rtypes)
-    for rt, v in s["per_type"].items():
-        ratio = v["median"] / float(np.median(runs[:, rtypes == rt, 1]))
-        assert 0.5 <= ratio <= BOUNDS[rt], (rt, ratio)
+def test_final_medians_by_type(recorded):
+    runs, rtypes, _ = _reference()
+    types, _, s = recorded
+    for rt, ratio in _ratios(types, s, runs, rtypes).items():
+        assert LOWER[rt] <= ratio <= UPPER[rt], (rt, ratio)
 
 
-def test_records_are_best_so_far(harness):
-    _, rec, _ = harness
+def test_records_are_best_so_far(recorded):
+    _, rec, _ = recorded
     best = rec[:, :, :-1]
     # no transfer: a task's recorded best never rises beyond the FP32 error
+    # (migration moves members between a task's own islands only)
     assert (np.diff(best, axis=2) <= 1e-5 * np.abs(best[:, :, 1:]) + 2e-2).all()
     assert (rec[:, :, -1] >= rec[:, :, 0]).all()  # near-worst >= best at generation 0
+
+
+def test_shipped_mutation_probability_misses_the_record(sgemtf):
+    from sgemtf import quality
+    runs, rtypes, _ = _reference()
+    types, rec = quality.run(seeds=30, operators=quality.SHIPPED_GA)
+    r = _ratios(types, quality.summarise(types, rec), runs, rtypes)
+    assert r[SCHWEFEL] > 3.0 and r[WEIERSTRASS] > 2.0, r

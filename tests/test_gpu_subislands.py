@@ -85,6 +85,16 @@ def test_migration_large_islands(sgemtf, orc, precision, alg):
     assert migrated > 0
 
 
+def test_migration_np512_sixteen_subislands(sgemtf, orc):
+    """The reference's layout: 512 members per task in sub-islands of 32
+    (SG-EMTF.cu:29-31, 856-896), migration every few generations, on the
+    HBM-resident pipeline that islands of more than 256 members take."""
+    specs = [(6, 50, 512, 1), (0, 30, 512, 1), (3, 20, 64, 1)]
+    migrated = _replay(sgemtf, orc, specs, 16, 3, 3, algorithm=2, eta_c=2.0, p_c=1.0,
+                       eta_m=5.0, p_m=1.0, migration_count=2)
+    assert migrated > 0
+
+
 def test_migration_inside_long_epochs(sgemtf, orc):
     """One run of many generations migrates at every interval inside the
     kernel; the same run cut into interval-long epochs gives the same state."""
