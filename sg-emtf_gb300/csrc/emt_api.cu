@@ -275,7 +275,8 @@ bool device_has_tcgen05(int device) {
 bool tc_fits(const std::vector<HostTask>& tasks, bool bf16, int& np, int& kp) {
   int dmax = 1;
   for (const auto& t : tasks) dmax = std::max(dmax, t.D);
-  np = emt::round8(dmax);
+  // islands of D <= 64 take Q in 64-row tiles (the paired form, N = 128)
+  np = std::max(64, emt::round8(dmax));
   kp = bf16 ? emt::round64(dmax) : emt::round32(dmax);
   for (const auto& t : tasks)
     if (t.NP > 128 || emt::tc_layout(t.D, t.NP, np, kp, bf16).total > emt::kSmemLimit) return false;

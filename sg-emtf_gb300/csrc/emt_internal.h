@@ -237,11 +237,17 @@ EMT_HD Layout smem_layout(int D, int NP, bool qt_in_smem = true) {
 // starts 1024-byte aligned (the kernel checks it) with the operand tiles,
 // `planes` split parts of each operand (TF32: hi, lo; BF16: three parts),
 // each part nkb tiles of 128-byte rows (32 TF32 or 64 BF16 values per row):
-// A = planes x nkb tiles of MA rows, B = planes x nkb tiles of Np rows.  With
-// NP <= 64 the A tiles hold 64 rows and the MMAs are M = 64; above, 128 rows
-// and M = 128.  B holds Np = round8(D) rows of Q: an MMA of N = round16(D)
-// columns reads up to 8 rows past a part, whose output columns (>= D) are
-// never used.  The FP32 rotated rows Z alias the A region once the MMAs have
+// A = planes x nkb tiles of MA rows.  With NP <= 64 the A tiles hold 64 rows
+// and the MMAs are M = 64; above, 128 rows and M = 128, so no MMA reads past
+// A.  B holds Q's parts in tiles of Np rows:
+//  - paired form, Np = 64 (every island of the handle has D <= 64): per K
+//    block the parts' tiles side by side, kb-major, plus (BF16) a zero tile,
+//    so an MMA of N = 128 over two adjacent tiles takes two parts of Q;
+//  - otherwise Np = round8(D) of the widest island, part-major: an MMA of
+//    N = round16(D) columns reads up to 8 rows (1 KB) past a part, whose
+//    output columns (>= D) are never used; past the last part that stays
+//    inside the allocation, which ends with at least the 1 KB MMA table and
+//    the header.  The FP32 rotated rows Z alias the A region once the MMAs have
 // completed.  The last kTcHeader bytes of the launch's allocation hold the
 // CTA's own tensor-core state, at the same place whatever island it works on
 // (the persistent queue kernel runs many): two mbarriers (MMA completion, TMA
@@ -257,6 +263,7 @@ static_assert(sizeof(TcHeader) <= kTcHeader, "tensor-core header");
 
 struct TcLayout {
   int DP, Np, Kp, nkb, MA, planes, epr;
+  int bplanes;  // B tiles per K block: planes, and a zero tile in the paired BF16 form
   size_t A, B, fit64, z64, X, U, o, fit, tol, ftr, ttr, idx, flag, list, misc, mdesc, total;
 };
 
@@ -273,7 +280,8 @@ EMT_HD TcLayout tc_layout(int D, int NP, int Np, int Kp, bool bf16) {
   L.A = off;
   off += (size_t)L.planes * L.nkb * L.MA * 128;
   L.B = off;
-  off += (size_t)L.planes * L.nkb * Np * 128;
+  L.bplanes = (Np == 64 && bf16) ? 4 : L.planes;
+  off += (size_t)L.bplanes * L.nkb * Np * 128;
   L.fit64 = off; off = align16(off + sizeof(double) * NP);
   // FP64 re-check scratch: idle A-region space past Z (the re-checks run
   // after the epilogue has consumed Z and before the next operands are staged)

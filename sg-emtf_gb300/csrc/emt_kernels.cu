@@ -97,7 +97,9 @@ struct Smem {
   unsigned char *A, *B;
   uint32_t a_saddr, b_saddr, mma_bar, tma_bar, tmem;
   uint32_t acc_cols;  // TMEM columns per accumulator (accumulator k starts at k * acc_cols)
-  int nacc;           // accumulators: the leading product's, then 1 or 3 for the others
+  int nmma;           // MMAs per rotation
+  int bplanes;        // B tiles per K block
+  bool paired;        // Q in 64-row tiles, N = 128 MMAs over two of them
   int MA, nkb, Np, N, ksteps;
   int planes;     // split parts per operand: 2 (TF32 hi/lo) or 3 (BF16)
   bool bf16;      // exact 3 x BF16 split, kind::f16 MMAs
@@ -121,7 +123,6 @@ struct Smem {
 struct TcCta {
   TcHeader* hdr;
   uint32_t tmem, ncols, mma_bar, tma_bar;
-  uint32_t acc_cols, nacc;  // accumulators of acc_cols TMEM columns each
   uint32_t mphase, tphase;  // parity each barrier completes next
 };
 
@@ -155,6 +156,8 @@ __device__ __forceinline__ Smem carve_tc(unsigned char* base, const TcLayout& L)
   s.bf16 = L.planes == 3;
   s.nkb = L.nkb;
   s.Np = L.Np;
+  s.bplanes = L.bplanes;
+  s.paired = L.Np == 64;
   return s;
 }
 
@@ -374,36 +377,57 @@ __device__ void zero_pads(const Smem& s, int D, int nrows) {
 }
 
 // The island's MMAs in issue order, written once per island by all threads
-// (read after the next barrier).  Products of parts (a of s, b of Q), the
-// leading one first; BF16 takes eight of the nine (s2 q2, at most 2^-32 of
-// s0 q0, is below the FP32 accumulation's own rounding).  The leading
-// product accumulates alone in accumulator 0.  With four accumulators the
-// others go round-robin to accumulators 1-3, with two all to accumulator 1.
-// The issue order is K-step outer, product inner, so consecutive MMAs
-// mostly update different accumulators.  Each descriptor is the tile's base
-// descriptor plus the K-step's offset >> 4 in the start-address field (bits
+// (read after the next barrier); returns their number.  Products of parts
+// (a of s, b of Q), the leading one first; BF16 takes eight of the nine
+// (s2 q2, at most 2^-32 of s0 q0, is below the FP32 accumulation's own
+// rounding).  Two accumulators of 128 TMEM columns; the leading product
+// alone in the first.  Each entry: descriptor low words (the tile's base
+// descriptor plus the K-step's offset >> 4 in the start-address field, bits
 // 0-13: shared addresses stay below 256 KB, so there is no carry and the
-// high words are the base descriptors').
-__device__ __noinline__ void mma_descriptors(uint4* tab, uint32_t a_saddr, uint32_t b_saddr,
-                                             int MA, int Np, int planes, int nkb, int ksteps,
-                                             uint32_t acc_cols, int nacc) {
+// high words are the base descriptors'), accumulator column, accumulate flag.
+//
+// Paired form (Q in 64-row tiles, N = 128): an MMA on B tile b reads tiles
+// b and b + 1 of the K block, so its columns 0-63 take part b of Q and
+// columns 64-127 part b + 1.  Per K-step, TF32: hi [q_hi q_lo] -> acc 0
+// (columns 0-63 the leading hi q_hi alone), lo [q_hi q_lo] -> acc 1.  BF16:
+// s0 [q0 q1] -> acc 0; s1 [q0 q1], s2 [q0 q1], s0 [q2 0], s1 [q2 0] -> acc 1
+// (the zero tile keeps columns 64-127 of the last two clean).  z is acc 0's
+// columns 0-63 plus the sum of acc 0's columns 64-127 and both halves of
+// acc 1: all eight products, five MMAs instead of eight (TF32: two of four).
+//
+// Otherwise one MMA per product and K-step (N = round16(D), part-major B),
+// K-step outer, the other products all into accumulator 1.
+__device__ __noinline__ int mma_descriptors(uint4* tab, uint32_t a_saddr, uint32_t b_saddr,
+                                            int MA, int Np, int planes, int nkb, int bplanes,
+                                            int ksteps, bool paired) {
   const uint64_t a0 = tc::sdesc_sw128(a_saddr), b0 = tc::sdesc_sw128(b_saddr);
-  const uint32_t pa = 0x21201100u, pb = 0x12021010u;  // parts per product, 4 bits each
   const uint32_t atile = (uint32_t)MA * 8u, btile = (uint32_t)Np * 8u;  // (rows x 128 B) >> 4
-  const int nprod = planes == 3 ? 8 : 4;
-  const int n = nprod * ksteps;
-  for (int i = threadIdx.x; i < n && i < kMaxMmas; i += kThreads) {
-    const int st = i / nprod, p = i - st * nprod;
-    const uint32_t kb = (uint32_t)st >> 2, ks = (uint32_t)st & 3u;
-    const uint32_t ap = (pa >> (4 * p)) & 15u, bp = (pb >> (4 * p)) & 15u;
-    const uint64_t ad = a0 + ((kb * (uint32_t)planes + ap) * atile + 2u * ks);
-    const uint64_t bd = b0 + ((bp * (uint32_t)nkb + kb) * btile + 2u * ks);
-    const uint32_t k = p == 0 ? 0u : nacc == 4 ? 1u + (uint32_t)(p - 1) % 3u : 1u;
-    // the first MMA into each accumulator overwrites it: products 0 .. nacc-1
-    // of K-step 0 are the first of their accumulators
-    const uint32_t accumulate = (st > 0 || p >= nacc) ? 1u : 0u;
-    tab[i] = make_uint4((uint32_t)ad, (uint32_t)bd, k * acc_cols, accumulate);
+  // per K-step: part of s, part (paired: first B tile) of Q, accumulator; 4 bits each
+  uint32_t pa, pb, pk;
+  int per;
+  if (paired && planes == 3) {
+    pa = 0x10210u; pb = 0x22000u; pk = 0x11110u; per = 5;
+  } else if (paired) {
+    pa = 0x10u; pb = 0x00u; pk = 0x10u; per = 2;
+  } else if (planes == 3) {
+    pa = 0x21201100u; pb = 0x12021010u; pk = 0x11111110u; per = 8;
+  } else {
+    pa = 0x1100u; pb = 0x1010u; pk = 0x1110u; per = 4;
   }
+  const int n = per * ksteps;
+  for (int i = threadIdx.x; i < n && i < kMaxMmas; i += kThreads) {
+    const int st = i / per, p = i - st * per;
+    const uint32_t kb = (uint32_t)st >> 2, ks = (uint32_t)st & 3u;
+    const uint32_t ap = (pa >> (4 * p)) & 15u, bp = (pb >> (4 * p)) & 15u, k = (pk >> (4 * p)) & 15u;
+    const uint64_t ad = a0 + ((kb * (uint32_t)planes + ap) * atile + 2u * ks);
+    const uint32_t btl = paired ? kb * (uint32_t)bplanes + bp : bp * (uint32_t)nkb + kb;
+    const uint64_t bd = b0 + (btl * btile + 2u * ks);
+    // the first MMA into each accumulator (K-step 0, the first product with
+    // that accumulator) overwrites it
+    const uint32_t accumulate = (st > 0 || p > (int)k) ? 1u : 0u;
+    tab[i] = make_uint4((uint32_t)ad, (uint32_t)bd, k * 128u, accumulate);
+  }
+  return n < kMaxMmas ? n : kMaxMmas;
 }
 
 // Tensor-core rotation of rows [0, nrows) staged with their pad columns:
@@ -425,10 +449,8 @@ __device__ void rotate_tc(const Smem& s, int D, int DP, int nrows, uint32_t& pha
   EMT_PHASE(s, PH_MMA_ISSUE);
   if (threadIdx.x == 0 && !dead && !s.lose_completion) {
     tc::fence_after();
-    // the descriptor table (mma_descriptors) in issue order: the leading
-    // product alone into accumulator 0, then the others into accumulator 1
-    const int n = (s.bf16 ? 8 : 4) * s.ksteps;
-    for (int i = 0; i < n; ++i) {
+    // the table of mma_descriptors, in issue order
+    for (int i = 0; i < s.nmma; ++i) {
       const uint4 w = s.mdesc[i];
       const uint64_t ad = ((uint64_t)s.ad_hi << 32) | w.x, bd = ((uint64_t)s.bd_hi << 32) | w.y;
       if (s.bf16)
@@ -458,20 +480,22 @@ __device__ void rotate_tc(const Smem& s, int D, int DP, int nrows, uint32_t& pha
     }
     EMT_PHASE_LAP(s, PH_DRAIN);
     const int q = warp & 3, row = lane < rpq ? rpq * q + lane : nrows;  // nrows: no row
-    const int nch = s.N >> 4, half = (nch + 1) >> 1;
+    // output columns: the paired form's first 64 (its columns 64-127 hold the
+    // second part of Q), else N
+    const int nch = (s.paired ? 64 : s.N) >> 4, half = (nch + 1) >> 1;
     const int c_lo = (warp >> 2) ? half : 0, c_hi = (warp >> 2) ? nch : half;
     for (int c = c_lo; c < c_hi; ++c) {
       const int c0 = 16 * c;
       float v[16], w[16];
       if (ok) {
-        // the small products' accumulators first, then the leading one
+        // the small products first, then the leading one
         const uint32_t t0 = s.tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c0;
-        tc::tmem_ld16(t0 + s.acc_cols, w);
-        if (s.nacc == 4) {
-          tc::tmem_ld16(t0 + 2u * s.acc_cols, v);
+        tc::tmem_ld16(t0 + 128u, w);
+        if (s.paired) {
+          tc::tmem_ld16(t0 + 64u, v);
 #pragma unroll
           for (int g = 0; g < 16; ++g) w[g] = __fadd_rn(w[g], v[g]);
-          tc::tmem_ld16(t0 + 3u * s.acc_cols, v);
+          tc::tmem_ld16(t0 + 192u, v);
 #pragma unroll
           for (int g = 0; g < 16; ++g) w[g] = __fadd_rn(w[g], v[g]);
         }
@@ -904,35 +928,43 @@ __device__ __forceinline__ void epoch_body(const EpochArgs& a, const void* tmap,
     s.mma_bar = cta.mma_bar;
     s.tma_bar = cta.tma_bar;
     s.tmem = cta.tmem;
-    s.acc_cols = cta.acc_cols;
-    s.nacc = (int)cta.nacc;
+    s.acc_cols = 128;
     s.dead = &cta.hdr->dead;
     s.wait_ns = a.wait_ns ? a.wait_ns : tc::kWaitLimitNs;
     s.lose_completion = (a.flags & FLAG_TEST_LOST_COMPLETION) != 0;
     s.QT = const_cast<float*>(a.qt + td.q_off);  // FP32 Q^T for the re-checks
     DP = L.DP;
     NPP = round4(NP);
-    s.N = round16(D);
+    s.N = s.paired ? 128 : round16(D);
     s.ksteps = s.bf16 ? (D + 15) >> 4 : (D + 7) >> 3;
     // M = 64 for islands of <= 64 members (the A tiles' own rows), else 128
     s.idesc = s.bf16 ? tc::idesc_bf16(s.MA, s.N) : tc::idesc_tf32(s.MA, s.N);
-    mma_descriptors(const_cast<uint4*>(s.mdesc), s.a_saddr, s.b_saddr, s.MA, s.Np, s.planes,
-                    s.nkb, s.ksteps, s.acc_cols, s.nacc);
+    s.nmma = mma_descriptors(const_cast<uint4*>(s.mdesc), s.a_saddr, s.b_saddr, s.MA, s.Np,
+                             s.planes, s.nkb, s.bplanes, s.ksteps, s.paired);
     s.ad_hi = (uint32_t)(tc::sdesc_sw128(s.a_saddr) >> 32);
     s.bd_hi = (uint32_t)(tc::sdesc_sw128(s.b_saddr) >> 32);
     // zero the operand tiles once: padded K columns meet zero Q columns, so
-    // they only need to hold finite values
+    // they only need to hold finite values; and the paired BF16 form's zero
+    // tiles of B (the fourth of each K block), which no TMA copy writes
     for (size_t it = threadIdx.x; it < (L.B - L.A) / 16; it += kThreads)
       reinterpret_cast<float4*>(s.A)[it] = make_float4(0.f, 0.f, 0.f, 0.f);
-    // B operand: Q hi/lo tiles of this task by TMA (box 32 x Np x 1 per tile)
-    // into the B region, which no MMA reads any more (the previous island's
-    // last MMAs completed before its selection)
+    if (s.bplanes > s.planes)
+      for (int it = threadIdx.x; it < s.nkb * s.Np * 8; it += kThreads) {
+        const int kb = it / (s.Np * 8), r = it - kb * s.Np * 8;
+        reinterpret_cast<float4*>(s.B + (size_t)(kb * s.bplanes + s.planes) * s.Np * 128)[r] =
+            make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    // B operand: Q's part tiles of this task by TMA (box one 128-byte row x
+    // Np x 1 per tile) into the B region, which no MMA reads any more (the
+    // previous island's last MMAs completed before its selection)
     if (threadIdx.x == 0 && !*s.dead) {
       tc::mbar_expect_tx(s.tma_bar, (uint32_t)(s.planes * s.nkb * s.Np * 128));
       for (int h = 0; h < s.planes; ++h)
-        for (int kb = 0; kb < s.nkb; ++kb)
-          tc::tma_load_3d(s.b_saddr + (uint32_t)((h * s.nkb + kb) * s.Np * 128), tmap,
-                          L.epr * kb, 0, s.planes * task + h, s.tma_bar);
+        for (int kb = 0; kb < s.nkb; ++kb) {
+          const int tile = s.paired ? kb * s.bplanes + h : h * s.nkb + kb;
+          tc::tma_load_3d(s.b_saddr + (uint32_t)(tile * s.Np * 128), tmap, L.epr * kb, 0,
+                          s.planes * task + h, s.tma_bar);
+        }
     }
   } else {
     const Layout L = smem_layout(D, NP, td.qt_in_smem != 0);
@@ -1117,13 +1149,9 @@ __device__ __forceinline__ void tc_cta_begin(const EpochArgs& a, unsigned char* 
   cta.hdr = reinterpret_cast<TcHeader*>(smem_raw + a.smem_bytes - kTcHeader);
   cta.mma_bar = tc::smem_addr(&cta.hdr->mma_bar);
   cta.tma_bar = tc::smem_addr(&cta.hdr->tma_bar);
-  // accumulators of N <= 64 columns come four to a CTA (256 columns), wider
-  // ones two: two CTAs per SM stay within the SM's 512 columns
-  uint32_t half = 32;
-  while (half < (uint32_t)round16(a.tc_np)) half <<= 1;
-  cta.acc_cols = half;
-  cta.nacc = half <= 64 ? 4u : 2u;
-  cta.ncols = cta.nacc * half;
+  // two accumulators of 128 columns (N <= 128): two CTAs per SM stay within
+  // the SM's 512 columns
+  cta.ncols = 256;
   cta.mphase = cta.tphase = 0;
   if (threadIdx.x == 0) {
     tc::mbar_init(cta.mma_bar, 1);
