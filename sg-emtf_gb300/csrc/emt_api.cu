@@ -355,6 +355,8 @@ int large_upload(emt_handle* h, int64_t pop, int32_t fit) {
     qrow[t] = (int64_t)t * h->lNq;
   }
   h->lrows = rows;
+  int64_t ritems = 0;  // rotation work items of one selection step, at most
+  for (const auto& t : h->tasks) ritems += emt::large::rot_items_max(t.D, t.NP);
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
   emt_large_recheck_grids(sms, &h->lrot_grid, &h->ldecide_grid);  // persistent re-check grids
@@ -366,7 +368,7 @@ int large_upload(emt_handle* h, int64_t pop, int32_t fit) {
       (e = h->d_flag.ensure((size_t)fit)) || (e = h->d_ties.ensure((size_t)fit)) ||
       (e = h->d_ntie.ensure(n)) || (e = h->d_work.ensure((size_t)fit)) || (e = h->d_nwork.ensure(2)) ||
       (e = h->d_tjob.ensure((size_t)fit)) || (e = h->d_jobs.ensure(2 * (size_t)fit)) ||
-      (e = h->d_njob.ensure(n)) || (e = h->d_rwork.ensure(2 * (size_t)fit + 8 * (size_t)n)) ||
+      (e = h->d_njob.ensure(n)) || (e = h->d_rwork.ensure((size_t)ritems)) ||
       (e = h->d_zr.ensure(2 * (size_t)pop)) ||
       (e = h->d_srow.ensure(n)) || (e = h->d_qrow.ensure(n)) ||
       (e = h->d_S.ensure((size_t)planes * rows * h->lKp)) ||

@@ -721,16 +721,13 @@ __device__ __forceinline__ int sel_target(const LargeArgs& a, const TaskDev& td,
                                : c;
 }
 
-// near-tie rows rotated per work item (registers: 2 per job and thread) and
-// the k-tile of their exact splits staged in shared memory
-constexpr int kRotJobs = 8;
+// the k-tile of the rows' exact splits staged in shared memory (the item
+// shape kRotCols x kRotJobs is in emt_internal.h)
 constexpr int kRotTile = 128;
-constexpr int kRotCols = 128;  // outputs per item: one per thread of a 128-thread CTA
 // work-item encodings: rotation items task << 16 | block << 12 | chunk, jobs
 // row | member << 16, tie jobs trial | (member + 1) << 16, decisions
 // task << 16 | tie (tasks < 2^15, checked on the host).  Rotation items per
-// task: blocks x chunks <= (1024 / 128) x ceil(2 NP / 8) <= 2 NP + 8, within
-// the host's 2 fit + 8 T allocation.
+// task: at most rot_items_max(D, NP), which the host allocates per task.
 static_assert((kMaxDimLarge + kRotCols - 1) / kRotCols <= 16, "column block in 4 bits");
 static_assert((2 * kMaxPopLarge + kRotJobs - 1) / kRotJobs < 4096, "job chunk in 12 bits");
 static_assert(2 * kMaxPopLarge + 1 < 0xFFFF, "job and tie indices in 16 bits");
@@ -806,7 +803,7 @@ __global__ void __launch_bounds__(256) classify_kernel(const LargeArgs a, int mo
   }
 }
 
-// Rotation work item: outputs [128 b, 128 b + 128) of up to kRotJobs rows of
+// Rotation work item: outputs [kRotCols b, kRotCols (b + 1)) of up to kRotJobs rows of
 // one task (small items keep the grid busy when few islands have near ties).  A persistent grid takes items from the queue; each thread owns
 // one output and streams its column of Q once for all the item's rows, the
 // exact splits x - o of the rows staged in shared memory a k-tile at a time.
