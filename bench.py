@@ -69,7 +69,7 @@ TASKS, DIM, POP, GENS = 1000, 50, 64, 2000
 FLOPS_PER_EVAL = 2 * DIM * DIM  # rotation, unpadded D, one product counted
 # DRAM bytes (read + write) of one epoch launch of 304 tasks, 200 generations,
 # from the committed ncu captures; per launch the state moves once
-EPOCH_DRAM_BYTES_304 = {"fp32": 8.04e6, "tf32x3": 16.80e6}
+EPOCH_DRAM_BYTES_304 = {"fp32": 8.04e6, "tf32x3": 16.80e6, "bf16x3": 14.36e6}
 TC_FORMS = ("tf32x3", "bf16x3")
 
 

@@ -32,11 +32,6 @@
 #include "emt_recheck.cuh"
 #include "emt_tc.cuh"
 
-// threads that issue a rotation's MMAs (a build may set 2: one per accumulator)
-#ifndef EMT_MMA_ISSUERS
-#define EMT_MMA_ISSUERS 1
-#endif
-
 namespace emt {
 
 // Phase clocks (build with -DEMT_PHASE_CLOCKS, the measurement build): thread
@@ -452,21 +447,11 @@ __device__ void rotate_tc(const Smem& s, int D, int DP, int nrows, uint32_t& pha
   __syncthreads();
   const bool dead = *s.dead != 0;  // an earlier wait gave up: skip the MMAs
   EMT_PHASE(s, PH_MMA_ISSUE);
-#if EMT_MMA_ISSUERS == 2
-  // two issuing threads in different warps, one per accumulator; each
-  // commits its own MMAs to the barrier, which counts two arrivals
-  const int issuer = threadIdx.x == 0 ? 0 : threadIdx.x == 32 ? 1 : -1;
-#else
-  const int issuer = threadIdx.x == 0 ? 0 : -1;
-#endif
-  if (issuer >= 0 && !dead && !s.lose_completion) {
+  if (threadIdx.x == 0 && !dead && !s.lose_completion) {
     tc::fence_after();
     // the table of mma_descriptors, in issue order
     for (int i = 0; i < s.nmma; ++i) {
       const uint4 w = s.mdesc[i];
-#if EMT_MMA_ISSUERS == 2
-      if ((w.z != 0u) != (issuer == 1)) continue;
-#endif
       const uint64_t ad = ((uint64_t)s.ad_hi << 32) | w.x, bd = ((uint64_t)s.bd_hi << 32) | w.y;
       if (s.bf16)
         tc::mma_bf16(s.tmem + w.z, ad, bd, s.idesc, w.w);
@@ -1169,7 +1154,7 @@ __device__ __forceinline__ void tc_cta_begin(const EpochArgs& a, unsigned char* 
   cta.ncols = 256;
   cta.mphase = cta.tphase = 0;
   if (threadIdx.x == 0) {
-    tc::mbar_init(cta.mma_bar, EMT_MMA_ISSUERS);
+    tc::mbar_init(cta.mma_bar, 1);
     tc::mbar_init(cta.tma_bar, 1);
     cta.hdr->dead = 0;
   }
