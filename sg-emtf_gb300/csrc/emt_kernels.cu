@@ -431,16 +431,14 @@ __device__ __noinline__ int mma_descriptors(uint4* tab, uint32_t a_saddr, uint32
 }
 
 // Tensor-core rotation of rows [0, nrows) staged with their pad columns:
-// tcgen05 MMAs over the K steps that cover D (32 bytes of each 128-byte row
-// per step: 8 TF32 or 16 BF16 values), one issuing thread, completion on an
-// mbarrier that warp 0 waits for while the other warps wait at the CTA
-// barrier.  The product of the two leading parts accumulates alone in the
-// first accumulator; every other product of parts (TF32: hi.lo, lo.hi,
-// lo.lo; BF16: seven more, all but s2 q2, whose 2^-32 relative size is far
-// below the accumulation's rounding) in the second, so the large partial sums do not swallow
-// the small products (each MMA step rounds its accumulator to FP32).  Then
-// the warps drain both accumulators (TMEM lane = row; warp w reads lanes
-// 32 (w mod 4) on, its half of the columns), add them in FP32 and store Z.
+// the island's MMAs (mma_descriptors) over the K steps that cover D (32
+// bytes of each 128-byte row per step: 8 TF32 or 16 BF16 values) from one
+// issuing thread, completion on an mbarrier.  The product of the two leading
+// parts accumulates alone, so the large partial sums do not swallow the small
+// products (each MMA step rounds its accumulator to FP32).  Each warp that
+// drains rows waits on the mbarrier itself, reads its TMEM lanes (warp w
+// reads the lanes of sub-partition w mod 4, its half of the columns), adds
+// the small products, then the leading one, in FP32 and stores Z.
 // phase: the mbarrier parity this CTA expects next.
 __device__ void rotate_tc(const Smem& s, int D, int DP, int nrows, uint32_t& phase) {
   tc::fence_async_smem();  // generic-proxy operand writes -> async proxy
