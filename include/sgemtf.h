@@ -80,17 +80,19 @@ typedef enum emt_precision {
   EMT_ROT_FP32 = 0,   /* FP32 FMA on CUDA cores                          */
   EMT_ROT_TF32X3 = 1, /* tcgen05 tensor cores, kind::tf32: hi/lo TF32 split
                          of both operands (both parts rounded to nearest),
-                         FP32 accumulation in tensor memory: hi.hi in one
-                         accumulator, hi.lo + lo.hi + lo.lo in a second,
-                         added in FP32                                     */
+                         FP32 accumulation in tensor memory, hi.hi apart
+                         from hi.lo + lo.hi + lo.lo, added in FP32         */
   EMT_ROT_AUTO = 2,   /* the tensor-core form when the device and the
                          islands allow it (BF16X3), else FP32              */
   EMT_ROT_BF16X3 = 3  /* tcgen05 tensor cores, kind::f16: each operand split
-                         exactly into three BF16 parts (x = x0 + x1 + x2), all
-                         nine products of parts, so every product is exact;
-                         x0.y0 in one FP32 tensor-memory accumulator, the
-                         other eight in a second.  Islands of D <= 128; a
-                         large-island handle runs TF32X3 instead            */
+                         exactly into three BF16 parts (x = x0 + x1 + x2),
+                         eight of the nine products of parts (x2.y2, at most
+                         2^-32 of x0.y0, is dropped), every product exact;
+                         x0.y0 accumulated apart from the other seven in
+                         FP32 tensor memory.  Islands of D <= 128; a
+                         large-island handle runs TF32X3 instead.  (A plain
+                         one-part TF32 form is not offered: its 2^-11
+                         operand rounding is ~100x the 1e-5 tolerance.)     */
 } emt_precision;
 
 typedef enum emt_function {
