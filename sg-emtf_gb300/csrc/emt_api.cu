@@ -272,6 +272,15 @@ bool device_has_tcgen05(int device) {
 // Whether every island fits the tensor-core form (NP <= 128, one 128-row MMA
 // tile; operands and state within the shared-memory limit).  np: rows of the
 // B tiles, kp: their K extent in elements.
+// emt::tc_island_reads_inside for every island at the launch's allocation
+bool tc_reads_inside(const std::vector<HostTask>& tasks, int np, int kp, bool bf16) {
+  size_t smem = 0;
+  for (const auto& t : tasks) smem = std::max(smem, emt::tc_layout(t.D, t.NP, np, kp, bf16).total);
+  for (const auto& t : tasks)
+    if (!emt::tc_island_reads_inside(t.D, t.NP, np, kp, bf16, smem)) return false;
+  return true;
+}
+
 bool tc_fits(const std::vector<HostTask>& tasks, bool bf16, int& np, int& kp) {
   int dmax = 1;
   for (const auto& t : tasks) dmax = std::max(dmax, t.D);
@@ -280,7 +289,7 @@ bool tc_fits(const std::vector<HostTask>& tasks, bool bf16, int& np, int& kp) {
   kp = bf16 ? emt::round64(dmax) : emt::round32(dmax);
   for (const auto& t : tasks)
     if (t.NP > 128 || emt::tc_layout(t.D, t.NP, np, kp, bf16).total > emt::kSmemLimit) return false;
-  return true;
+  return tc_reads_inside(tasks, np, kp, bf16);
 }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,

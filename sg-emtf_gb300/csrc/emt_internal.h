@@ -330,6 +330,84 @@ EMT_HD int round16(int v) { return (v + 15) & ~15; }
 EMT_HD int round32(int v) { return (v + 31) & ~31; }
 EMT_HD int round64(int v) { return (v + 63) & ~63; }
 
+// MMAs of one island's tensor-core rotation, in issue order: K-step outer,
+// product of parts inner.  Products (a of s, b of Q), the leading one first;
+// BF16 takes eight of the nine (s2 q2, at most 2^-32 of s0 q0, is below the
+// FP32 accumulation's rounding).  Two accumulators of 128 TMEM columns, the
+// leading product alone in the first.
+//  - paired form (Q in 64-row tiles, N = 128): an MMA on B tile b reads tiles
+//    b and b + 1 of the K block, so its columns 0-63 take part b of Q and
+//    columns 64-127 part b + 1.  Per K-step, TF32: hi [q_hi q_lo] -> acc 0,
+//    lo [q_hi q_lo] -> acc 1.  BF16: s0 [q0 q1] -> acc 0; s1 [q0 q1],
+//    s2 [q0 q1], s0 [q2 0], s1 [q2 0] -> acc 1 (the zero tile keeps columns
+//    64-127 of the last two clean);
+//  - otherwise one MMA per product (N = round16(D), part-major B tiles).
+struct MmaEntry {
+  uint32_t a_off, b_off;  // bytes from the A and B regions to the MMA's tiles
+  uint32_t k_off;         // bytes of the K-step inside the 128-byte rows
+  uint32_t acc;           // accumulator 0 or 1
+  uint32_t accumulate;    // 0 for the first MMA into its accumulator
+};
+EMT_HD int mma_per_kstep(int planes, bool paired) {
+  return paired ? (planes == 3 ? 5 : 2) : (planes == 3 ? 8 : 4);
+}
+EMT_HD MmaEntry mma_entry(int i, int MA, int Np, int planes, int nkb, int bplanes, bool paired) {
+  // per K-step: part of s, part (paired: first B tile) of Q, accumulator; 4 bits each
+  uint32_t pa, pb, pk;
+  if (paired && planes == 3) {
+    pa = 0x10210u; pb = 0x22000u; pk = 0x11110u;
+  } else if (paired) {
+    pa = 0x10u; pb = 0x00u; pk = 0x10u;
+  } else if (planes == 3) {
+    pa = 0x21201100u; pb = 0x12021010u; pk = 0x11111110u;
+  } else {
+    pa = 0x1100u; pb = 0x1010u; pk = 0x1110u;
+  }
+  const int per = mma_per_kstep(planes, paired);
+  const int st = i / per, p = i - st * per;
+  const uint32_t kb = (uint32_t)st >> 2, ks = (uint32_t)st & 3u;
+  const uint32_t ap = (pa >> (4 * p)) & 15u, bp = (pb >> (4 * p)) & 15u, k = (pk >> (4 * p)) & 15u;
+  const uint32_t btile = paired ? kb * (uint32_t)bplanes + bp : bp * (uint32_t)nkb + kb;
+  MmaEntry e;
+  e.a_off = (kb * (uint32_t)planes + ap) * (uint32_t)MA * 128u;
+  e.b_off = btile * (uint32_t)Np * 128u;
+  e.k_off = 32u * ks;
+  e.acc = k;
+  // the first MMA into each accumulator (K-step 0, the first product with
+  // that accumulator) overwrites it
+  e.accumulate = (st > 0 || p > (int)k) ? 1u : 0u;
+  return e;
+}
+
+// One island of a tensor-core handle (Q tiles of np rows, K padded to kp,
+// launch allocation smem bytes): every MMA reads its tiles inside the
+// allocation (A reads inside A, paired B reads inside B), every TMA copy of
+// Q's parts lands inside B, and the MMA table fits.  The host checks it
+// before configuring a tensor-core launch.
+inline bool tc_island_reads_inside(int D, int NP, int np, int kp, bool bf16, size_t smem) {
+  const TcLayout L = tc_layout(D, NP, np, kp, bf16);
+  if (L.total > smem) return false;
+  const bool paired = L.Np == 64;
+  const size_t N = paired ? 128 : (size_t)round16(D);
+  if (N > 128) return false;  // two accumulators of 128 TMEM columns
+  const size_t bend = L.B + (size_t)L.bplanes * L.nkb * L.Np * 128;
+  const int ksteps = bf16 ? (D + 15) >> 4 : (D + 7) >> 3;
+  const int n = mma_per_kstep(L.planes, paired) * ksteps;
+  if (n > kMaxMmas) return false;
+  for (int i = 0; i < n; ++i) {
+    const MmaEntry e = mma_entry(i, L.MA, L.Np, L.planes, L.nkb, L.bplanes, paired);
+    if (L.A + e.a_off + (size_t)L.MA * 128 > L.B) return false;
+    const size_t b_end = L.B + e.b_off + N * 128;
+    if (b_end > smem || (paired && b_end > bend)) return false;
+  }
+  for (int h = 0; h < L.planes; ++h)
+    for (int kb = 0; kb < L.nkb; ++kb) {
+      const int tile = paired ? kb * L.bplanes + h : h * L.nkb + kb;
+      if (L.B + (size_t)(tile + 1) * L.Np * 128 > bend) return false;
+    }
+  return true;
+}
+
 // Error codes written to EpochArgs::err by the kernels' own checks.
 enum DeviceCheck : int32_t {
   CHECK_OK = 0,

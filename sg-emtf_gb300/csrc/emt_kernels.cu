@@ -376,56 +376,22 @@ __device__ void zero_pads(const Smem& s, int D, int nrows) {
   }
 }
 
-// The island's MMAs in issue order, written once per island by all threads
-// (read after the next barrier); returns their number.  Products of parts
-// (a of s, b of Q), the leading one first; BF16 takes eight of the nine
-// (s2 q2, at most 2^-32 of s0 q0, is below the FP32 accumulation's own
-// rounding).  Two accumulators of 128 TMEM columns; the leading product
-// alone in the first.  Each entry: descriptor low words (the tile's base
-// descriptor plus the K-step's offset >> 4 in the start-address field, bits
-// 0-13: shared addresses stay below 256 KB, so there is no carry and the
-// high words are the base descriptors'), accumulator column, accumulate flag.
-//
-// Paired form (Q in 64-row tiles, N = 128): an MMA on B tile b reads tiles
-// b and b + 1 of the K block, so its columns 0-63 take part b of Q and
-// columns 64-127 part b + 1.  Per K-step, TF32: hi [q_hi q_lo] -> acc 0
-// (columns 0-63 the leading hi q_hi alone), lo [q_hi q_lo] -> acc 1.  BF16:
-// s0 [q0 q1] -> acc 0; s1 [q0 q1], s2 [q0 q1], s0 [q2 0], s1 [q2 0] -> acc 1
-// (the zero tile keeps columns 64-127 of the last two clean).  z is acc 0's
-// columns 0-63 plus the sum of acc 0's columns 64-127 and both halves of
-// acc 1: all eight products, five MMAs instead of eight (TF32: two of four).
-//
-// Otherwise one MMA per product and K-step (N = round16(D), part-major B),
-// K-step outer, the other products all into accumulator 1.
+// The island's MMAs (mma_entry, issue order), written once per island by all
+// threads (read after the next barrier); returns their number.  Each entry:
+// descriptor low words (the tile's base descriptor plus its offset >> 4 in
+// the start-address field, bits 0-13: shared addresses stay below 256 KB, so
+// there is no carry and the high words are the base descriptors'),
+// accumulator column, accumulate flag.
 __device__ __noinline__ int mma_descriptors(uint4* tab, uint32_t a_saddr, uint32_t b_saddr,
                                             int MA, int Np, int planes, int nkb, int bplanes,
                                             int ksteps, bool paired) {
   const uint64_t a0 = tc::sdesc_sw128(a_saddr), b0 = tc::sdesc_sw128(b_saddr);
-  const uint32_t atile = (uint32_t)MA * 8u, btile = (uint32_t)Np * 8u;  // (rows x 128 B) >> 4
-  // per K-step: part of s, part (paired: first B tile) of Q, accumulator; 4 bits each
-  uint32_t pa, pb, pk;
-  int per;
-  if (paired && planes == 3) {
-    pa = 0x10210u; pb = 0x22000u; pk = 0x11110u; per = 5;
-  } else if (paired) {
-    pa = 0x10u; pb = 0x00u; pk = 0x10u; per = 2;
-  } else if (planes == 3) {
-    pa = 0x21201100u; pb = 0x12021010u; pk = 0x11111110u; per = 8;
-  } else {
-    pa = 0x1100u; pb = 0x1010u; pk = 0x1110u; per = 4;
-  }
-  const int n = per * ksteps;
+  const int n = mma_per_kstep(planes, paired) * ksteps;
   for (int i = threadIdx.x; i < n && i < kMaxMmas; i += kThreads) {
-    const int st = i / per, p = i - st * per;
-    const uint32_t kb = (uint32_t)st >> 2, ks = (uint32_t)st & 3u;
-    const uint32_t ap = (pa >> (4 * p)) & 15u, bp = (pb >> (4 * p)) & 15u, k = (pk >> (4 * p)) & 15u;
-    const uint64_t ad = a0 + ((kb * (uint32_t)planes + ap) * atile + 2u * ks);
-    const uint32_t btl = paired ? kb * (uint32_t)bplanes + bp : bp * (uint32_t)nkb + kb;
-    const uint64_t bd = b0 + (btl * btile + 2u * ks);
-    // the first MMA into each accumulator (K-step 0, the first product with
-    // that accumulator) overwrites it
-    const uint32_t accumulate = (st > 0 || p > (int)k) ? 1u : 0u;
-    tab[i] = make_uint4((uint32_t)ad, (uint32_t)bd, k * 128u, accumulate);
+    const MmaEntry e = mma_entry(i, MA, Np, planes, nkb, bplanes, paired);
+    const uint64_t ad = a0 + ((e.a_off + e.k_off) >> 4);
+    const uint64_t bd = b0 + ((e.b_off + e.k_off) >> 4);
+    tab[i] = make_uint4((uint32_t)ad, (uint32_t)bd, e.acc * 128u, e.accumulate);
   }
   return n < kMaxMmas ? n : kMaxMmas;
 }
