@@ -809,7 +809,82 @@ __global__ void __launch_bounds__(256) classify_kernel(const LargeArgs a, int mo
 // exact splits x - o of the rows staged in shared memory a k-tile at a time.
 // Each output keeps dot2_pair's order over k, so the values equal
 // precise_rotation's.
+// The compensated products of J rows (J = the item's job count, fixed at
+// compile time so a partial chunk costs in proportion to its rows) for the
+// k-tile in pr, into the running sums S, C of this thread's output.
+template <int J>
+__device__ __forceinline__ void rot_tile(const float2 (*pr)[kRotJobs], const float* qcol, int k0,
+                                         int kt, int DP, float* S, float* C) {
+  constexpr int kAhead = 16;  // Q loads issued ahead of the dependent updates
+  int kk = 0;
+  for (; kk + kAhead <= kt; kk += kAhead) {
+    float qv[kAhead];
+#pragma unroll
+    for (int u = 0; u < kAhead; ++u) qv[u] = __ldg(qcol + (size_t)(k0 + kk + u) * DP);
+#pragma unroll
+    for (int u = 0; u < kAhead; ++u) {
+      const float q = qv[u];
+#pragma unroll
+      for (int j = 0; j < J; ++j) {
+        const float2 hl = pr[kk + u][j];
+        const float pp = __fmul_rn(q, hl.x);
+        const float e = __fmaf_rn(q, hl.x, -pp);
+        float t, te;
+        two_sum(S[j], pp, t, te);
+        S[j] = t;
+        C[j] = __fmaf_rn(q, hl.y, __fadd_rn(C[j], __fadd_rn(te, e)));
+      }
+    }
+  }
+  for (; kk < kt; ++kk) {
+    const float q = __ldg(qcol + (size_t)(k0 + kk) * DP);
+#pragma unroll
+    for (int j = 0; j < J; ++j) {
+      const float2 hl = pr[kk][j];
+      const float pp = __fmul_rn(q, hl.x);
+      const float e = __fmaf_rn(q, hl.x, -pp);
+      float t, te;
+      two_sum(S[j], pp, t, te);
+      S[j] = t;
+      C[j] = __fmaf_rn(q, hl.y, __fadd_rn(C[j], __fadd_rn(te, e)));
+    }
+  }
+}
+
+// One rotation work item with J jobs: stage each k-tile of the rows' exact
+// splits, accumulate, write the FP64-class outputs.
+template <int J>
+__device__ __forceinline__ void rot_item(const LargeArgs& a, const TaskDev& td, int blk, int j0,
+                                         float2 (*pr)[kRotJobs], const float* const* jrow) {
+  const int D = td.D, DP = td.DP;
+  const float* o = a.shift + td.o_off;
+  const int n = blk * kRotCols + threadIdx.x;
+  const bool live = n < D;
+  const float* qcol = a.qt + td.q_off + (live ? n : 0);
+  float S[J], C[J];
+#pragma unroll
+  for (int j = 0; j < J; ++j) S[j] = C[j] = 0.f;
+  for (int k0 = 0; k0 < D; k0 += kRotTile) {
+    const int kt = min(kRotTile, D - k0);
+    __syncthreads();  // jrow written; the previous tile consumed
+    for (int it = threadIdx.x; it < J * kt; it += blockDim.x) {
+      const int j = it / kt, kk = it - j * kt;
+      float sh, sl;
+      two_sum(jrow[j][k0 + kk], -o[k0 + kk], sh, sl);
+      pr[kk][j] = make_float2(sh, sl);
+    }
+    __syncthreads();
+    if (live) rot_tile<J>(pr, qcol, k0, kt, DP, S, C);
+  }
+  if (live) {
+    double* z = a.zr + 2 * td.pop_off + (size_t)j0 * DP + n;
+#pragma unroll
+    for (int j = 0; j < J; ++j) z[(size_t)j * DP] = (double)S[j] + (double)C[j];
+  }
+}
+
 __global__ void __launch_bounds__(kRotCols) rot_kernel(const LargeArgs a) {
+  static_assert(kRotJobs == 8, "the job-count dispatch below covers 1..8");
   __shared__ __align__(16) float2 pr[kRotTile][kRotJobs];
   __shared__ const float* jrow[kRotJobs];
   const int items = a.nwork[1];
@@ -817,7 +892,7 @@ __global__ void __launch_bounds__(kRotCols) rot_kernel(const LargeArgs a) {
     const int code = a.rwork[w];
     const int task = code >> 16, blk = (code >> 12) & 15, chunk = code & 0xFFF;
     const TaskDev td = a.tasks[task];
-    const int D = td.D, DP = td.DP;
+    const int DP = td.DP;
     const int j0 = chunk * kRotJobs, nj = min(kRotJobs, a.njob[task] - j0);
     if (threadIdx.x < kRotJobs) {
       const int t = threadIdx.x;
@@ -828,68 +903,15 @@ __global__ void __launch_bounds__(kRotCols) rot_kernel(const LargeArgs a) {
       }
       jrow[t] = r;
     }
-    const float* o = a.shift + td.o_off;
-    const int n = blk * kRotCols + threadIdx.x;
-    const bool live = n < D;
-    const float* qcol = a.qt + td.q_off + (live ? n : 0);
-    float S[kRotJobs], C[kRotJobs];
-#pragma unroll
-    for (int j = 0; j < kRotJobs; ++j) S[j] = C[j] = 0.f;
-    for (int k0 = 0; k0 < D; k0 += kRotTile) {
-      const int kt = min(kRotTile, D - k0);
-      __syncthreads();  // jrow written; the previous tile consumed
-      for (int it = threadIdx.x; it < kRotJobs * kt; it += blockDim.x) {
-        const int j = it / kt, kk = it - j * kt;
-        float sh = 0.f, sl = 0.f;
-        if (j < nj) two_sum(jrow[j][k0 + kk], -o[k0 + kk], sh, sl);
-        pr[kk][j] = make_float2(sh, sl);
-      }
-      __syncthreads();
-      if (!live) continue;
-      constexpr int kAhead = 16;  // Q loads issued ahead of the dependent updates
-      int kk = 0;
-      for (; kk + kAhead <= kt; kk += kAhead) {
-        float qv[kAhead];
-#pragma unroll
-        for (int u = 0; u < kAhead; ++u) qv[u] = __ldg(qcol + (size_t)(k0 + kk + u) * DP);
-#pragma unroll
-        for (int u = 0; u < kAhead; ++u) {
-          const float q = qv[u];
-#pragma unroll
-          for (int j = 0; j < kRotJobs; ++j) {
-            if (j < nj) {
-              const float2 hl = pr[kk + u][j];
-              const float pp = __fmul_rn(q, hl.x);
-              const float e = __fmaf_rn(q, hl.x, -pp);
-              float t, te;
-              two_sum(S[j], pp, t, te);
-              S[j] = t;
-              C[j] = __fmaf_rn(q, hl.y, __fadd_rn(C[j], __fadd_rn(te, e)));
-            }
-          }
-        }
-      }
-      for (; kk < kt; ++kk) {
-        const float q = __ldg(qcol + (size_t)(k0 + kk) * DP);
-#pragma unroll
-        for (int j = 0; j < kRotJobs; ++j) {
-          if (j < nj) {
-            const float2 hl = pr[kk][j];
-            const float pp = __fmul_rn(q, hl.x);
-            const float e = __fmaf_rn(q, hl.x, -pp);
-            float t, te;
-            two_sum(S[j], pp, t, te);
-            S[j] = t;
-            C[j] = __fmaf_rn(q, hl.y, __fadd_rn(C[j], __fadd_rn(te, e)));
-          }
-        }
-      }
-    }
-    if (live) {
-      double* z = a.zr + 2 * td.pop_off + (size_t)j0 * DP + n;
-#pragma unroll
-      for (int j = 0; j < kRotJobs; ++j)
-        if (j < nj) z[(size_t)j * DP] = (double)S[j] + (double)C[j];
+    switch (nj) {  // uniform over the CTA
+      case 1: rot_item<1>(a, td, blk, j0, pr, jrow); break;
+      case 2: rot_item<2>(a, td, blk, j0, pr, jrow); break;
+      case 3: rot_item<3>(a, td, blk, j0, pr, jrow); break;
+      case 4: rot_item<4>(a, td, blk, j0, pr, jrow); break;
+      case 5: rot_item<5>(a, td, blk, j0, pr, jrow); break;
+      case 6: rot_item<6>(a, td, blk, j0, pr, jrow); break;
+      case 7: rot_item<7>(a, td, blk, j0, pr, jrow); break;
+      default: rot_item<8>(a, td, blk, j0, pr, jrow); break;
     }
     __syncthreads();  // jrow of the next item
   }
