@@ -54,6 +54,10 @@ template <typename T>
 struct DevBuf {
   T* p = nullptr;
   size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }  // every buffer of a handle goes with it
   cudaError_t ensure(size_t count) {
     if (count <= n && p) return cudaSuccess;
     if (p) cudaFree(p);
@@ -132,6 +136,7 @@ struct emt_handle {
   DevBuf<float> d_U, d_ftr, d_ttr, d_S, d_Z, d_qbig;
   DevBuf<int64_t> d_srow, d_qrow;
   DevBuf<int32_t> d_rank, d_flag, d_ties, d_ntie, d_work, d_nwork, d_tjob, d_jobs, d_njob, d_rwork;
+  DevBuf<float> d_wprec;  // large islands: which cached FP64-class values are float-float
   DevBuf<double> d_zr;  // re-check rotations of the large-island pipeline
   CUtensorMap smap, qmap;
 
@@ -377,6 +382,7 @@ int large_upload(emt_handle* h, int64_t pop, int32_t fit) {
       (e = h->d_flag.ensure((size_t)fit)) || (e = h->d_ties.ensure((size_t)fit)) ||
       (e = h->d_ntie.ensure(n)) || (e = h->d_work.ensure((size_t)fit)) || (e = h->d_nwork.ensure(2)) ||
       (e = h->d_tjob.ensure((size_t)fit)) || (e = h->d_jobs.ensure(2 * (size_t)fit)) ||
+      (e = h->d_wprec.ensure((size_t)fit)) ||
       (e = h->d_njob.ensure(n)) || (e = h->d_rwork.ensure((size_t)ritems)) ||
       (e = h->d_zr.ensure(2 * (size_t)pop)) ||
       (e = h->d_srow.ensure(n)) || (e = h->d_qrow.ensure(n)) ||
@@ -387,7 +393,8 @@ int large_upload(emt_handle* h, int64_t pop, int32_t fit) {
       (e = cudaMemcpy(h->d_qrow.p, qrow.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice)) ||
       (e = cudaMemset(h->d_S.p, 0, sizeof(float) * h->d_S.n)) ||
       (e = cudaMemset(h->d_Z.p, 0, sizeof(float) * h->d_Z.n)) ||
-      (e = cudaMemset(h->d_U.p, 0, sizeof(float) * (size_t)pop)))
+      (e = cudaMemset(h->d_U.p, 0, sizeof(float) * (size_t)pop)) ||
+      (e = cudaMemset(h->d_wprec.p, 0xFF, sizeof(float) * (size_t)fit)))
     return h->cuda_fail(e, "upload");
   if (!h->large_tc) return EMT_OK;
   const size_t plane = (size_t)n * h->lNq * h->lKp, per = (size_t)h->lNq * h->lKp;
@@ -759,6 +766,7 @@ emt::LargeArgs large_args(emt_handle* h) {
   a.ties = h->d_ties.p;
   a.ntie = h->d_ntie.p;
   a.tjob = h->d_tjob.p;
+  a.wprec = h->d_wprec.p;
   a.jobs = h->d_jobs.p;
   a.njob = h->d_njob.p;
   a.zr = h->d_zr.p;
@@ -1759,6 +1767,8 @@ int emt_restore(emt_handle_t* h, const void* buf, size_t bytes) {
   }
   // the cached compensated rotations belong to the replaced islands
   cudaError_t ez = cudaMemset(h->d_zcb.p, 0xFF, sizeof(float) * h->d_zcb.n);
+  if (ez == cudaSuccess && h->d_wprec.p)  // restored values are not known to be float-float
+    ez = cudaMemset(h->d_wprec.p, 0xFF, sizeof(float) * h->d_wprec.n);
   if (ez != cudaSuccess) return h->cuda_fail(ez, "restore");
   h->gdone = (uint32_t)hdr[2];
   h->initialized = true;

@@ -545,6 +545,10 @@ template <typename T>
 struct Buf {
   T* p = nullptr;
   size_t n = 0;
+  Buf() = default;
+  Buf(const Buf&) = delete;
+  Buf& operator=(const Buf&) = delete;
+  ~Buf() { release(); }
   cudaError_t ensure(size_t count) {
     if (count <= n && p) return cudaSuccess;
     if (p) cudaFree(p);

@@ -141,6 +141,8 @@ struct LargeArgs {
   int32_t* ties;         // per task (fit offsets): its near-tie rows, in order found
   int32_t* ntie;         // per task: their number
   int32_t* tjob;         // per near tie (fit offsets): trial job | (member job + 1) << 16
+  float* wprec;          // per member (fit offsets): 0 when fit64 holds a float-float
+                         // Weierstrass value, anything else when not
   int32_t* jobs;         // per task (2 x fit offsets): rows to rotate, row | 1 << 16 for a member
   int32_t* njob;         // per task: their number
   double* zr;            // FP64-class rotations of the jobs, 2 x pop offsets, stride DP
@@ -189,10 +191,12 @@ EMT_HD int64_t rot_items_max(int D, int NP) {
 }
 }  // namespace large
 
-// Dynamic shared memory of the large-island selection kernel: per-warp
-// re-check scratch (2 DP doubles) and the flag/list/target/misc arrays.
+// Dynamic shared memory of the large-island ranking / export / migration
+// kernel: the flag/list/target/misc arrays (no re-checks run there; the
+// stride DP is kept for the launch's interface).
 EMT_HD size_t large_select_smem(int DP) {
-  return sizeof(double) * kWarps * 2 * (size_t)DP + sizeof(int) * (4 * kMaxPopLarge + 16);
+  (void)DP;
+  return sizeof(int) * (4 * kMaxPopLarge + 16);
 }
 
 // Arguments of the standalone evaluation kernel (emt_evaluate).

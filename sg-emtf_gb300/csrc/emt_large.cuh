@@ -591,8 +591,9 @@ __global__ void __launch_bounds__(256) eval_kernel(const LargeArgs a, int which,
 }
 
 // ---------------------------------------------------------------------------
-// selection, ranking and elite exchange: one CTA (256 threads) per task,
-// the fused kernel's select_and_replace over global-memory rows
+// ranking, elite export and the migrants' preparation: one CTA (256 threads)
+// per task over global-memory rows (the selections themselves run through
+// the split pipeline below)
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) select_kernel(const LargeArgs a, int mode) {
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -605,8 +606,8 @@ __global__ void __launch_bounds__(256) select_kernel(const LargeArgs a, int mode
   }
   const int NP = td.NP, DP = td.DP;
   Smem s{};
-  s.z64 = reinterpret_cast<double*>(smraw);
-  int* ip = reinterpret_cast<int*>(s.z64 + (size_t)kWarps * 2 * DP);
+  s.z64 = nullptr;
+  int* ip = reinterpret_cast<int*>(smraw);
   s.flag = ip;
   s.list = ip + kMaxPopLarge;
   s.idx = ip + 2 * kMaxPopLarge;  // targets (transfer)
@@ -621,19 +622,8 @@ __global__ void __launch_bounds__(256) select_kernel(const LargeArgs a, int mode
   s.o = const_cast<float*>(a.shift + td.o_off);
   s.QT = const_cast<float*>(a.qt + td.q_off);
   s.zc = s.zcb = nullptr;
-  EpochArgs ea{};
-  ea.flags = a.flags;
-  const FnConst fc = fn_const(td, a.recheck_rel);
-  unsigned long long* st_re = a.stats ? a.stats + 0 : nullptr;
-  unsigned long long* st_fl = a.stats ? a.stats + 1 : nullptr;
   int* byrank = a.rank + td.fit_off;
-  if (mode == SEL_GENERATION) {
-    select_and_replace(s, ea, fc, NP, nullptr, false, DP, st_re, st_fl);
-    if (threadIdx.x == 0) {
-      a.gen[task] += 1u;
-      if (a.stats) atomicAdd(a.stats + 3, (unsigned long long)NP);
-    }
-  } else if (mode == SEL_RANK || mode == SEL_EXPORT) {
+  if (mode == SEL_RANK || mode == SEL_EXPORT) {
     rank_members(s, NP, s.idx);
     if (mode == SEL_RANK) {
       for (int i = threadIdx.x; i < NP; i += kThreads) byrank[i] = s.idx[i];
@@ -675,16 +665,9 @@ __global__ void __launch_bounds__(256) select_kernel(const LargeArgs a, int mode
       s.ftr[c] = s.fit[src];
       s.ttr[c] = s.tol[src];
     }
-  } else {  // SEL_IMPORT: candidates in trial rows [0, k) against ranks NP - k + c
-    int k = 0;
-    if (transfer_partner(a, task, a.gen[task], k) < 0) return;
-    for (int c = threadIdx.x; c < k; c += kThreads) s.idx[c] = byrank[NP - k + c];
-    __syncthreads();
-    // each thread returns the replacements among its own rows
-    const int acc = select_and_replace(s, ea, fc, k, s.idx, true, DP, st_re, st_fl);
-    if (acc && a.stats) atomicAdd(a.stats + 2, (unsigned long long)acc);
-    if (threadIdx.x == 0 && a.stats) atomicAdd(a.stats + 3, (unsigned long long)k);
   }
+  // SEL_GENERATION and SEL_IMPORT run through the split selection below
+  // (emt_large_selection), never here
 }
 
 // ---------------------------------------------------------------------------
@@ -967,27 +950,46 @@ __global__ void __launch_bounds__(256) decide_kernel(const LargeArgs a, int mode
         decided = true;
       }
     }
+    // Weierstrass: whether fit64[m] is a float-float value afterwards (1) or
+    // not (0); -1 for the other functions
+    int wprec = -1;
     if (!decided) {
       const bool weier = fc.fid == F_WEIERSTRASS;
       ft = weier ? eval_weier_precise_t(fc, zt, tm) : eval_tier3_t(fc, zt, tm);
       if (zp) fpv = weier ? eval_weier_precise_t(fc, zp, tm) : eval_tier3_t(fc, zp, tm);
-      if (weier && fabs(ft - fpv) <= 2.0 * weier_precise_bound(fc.D)) {
-        // closer than the FP32 terms' error: every term in float-float,
-        // the member's rotation computed here when its value was cached
-        double* zm = zmem;
-        if (zp) {
-          zm = const_cast<double*>(zp);
-        } else {
-          precise_rotation_team(a.pop + td.pop_off + (size_t)m * td.DP, a.shift + td.o_off,
-                                a.qt + td.q_off, td.DP, td.D, zmem, tm);
+      if (weier) {
+        // the member's cached value is already float-float (exact to ~1e-12)
+        const bool pprec = !zp && !isnan(fp) && a.wprec[td.fit_off + m] == 0.f;
+        const double bound = weier_precise_bound(fc.D);
+        wprec = 0;
+        if (fabs(ft - fpv) <= (pprec ? bound : 2.0 * bound)) {
+          // closer than the FP32 terms' error: every term in float-float, the
+          // member's too unless already so, its rotation computed here when
+          // only its value was cached
+          if (!pprec) {
+            double* zm = zmem;
+            if (zp) {
+              zm = const_cast<double*>(zp);
+            } else {
+              precise_rotation_team(a.pop + td.pop_off + (size_t)m * td.DP, a.shift + td.o_off,
+                                    a.qt + td.q_off, td.DP, td.D, zmem, tm);
+            }
+            fpv = eval_weier_ff_t(fc, zm, tm);
+          }
+          ft = eval_weier_ff_t(fc, zt, tm);
+          wprec = 1;
+          if (threadIdx.x == 0 && a.stats) atomicAdd(a.stats + kStatWeierFp64, 1ull);
         }
-        ft = eval_weier_ff_t(fc, zt, tm);
-        fpv = eval_weier_ff_t(fc, zm, tm);
-        if (threadIdx.x == 0 && a.stats) atomicAdd(a.stats + kStatWeierFp64, 1ull);
+        d64 = strict ? (ft < fpv) : (ft <= fpv);
+        if (!wprec && !d64 && pprec) wprec = 1;  // the member keeps its float-float value
+      } else {
+        d64 = strict ? (ft < fpv) : (ft <= fpv);
       }
-      d64 = strict ? (ft < fpv) : (ft <= fpv);
     }
-    if (threadIdx.x == 0) decide_write(a, td, strict, c, m, d64, ft, fpv);
+    if (threadIdx.x == 0) {
+      decide_write(a, td, strict, c, m, d64, ft, fpv);
+      if (wprec >= 0) a.wprec[td.fit_off + m] = wprec ? 0.f : __int_as_float(0x7FC00000);
+    }
   }
 }
 

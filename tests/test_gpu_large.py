@@ -162,3 +162,26 @@ def test_large_best_snapshot_and_limits(sgemtf, orc):
     with pytest.raises(sgemtf.EngineError):
         eng.run_noalloc(1)
     eng.close()
+
+
+def test_large_handles_return_their_memory(sgemtf, orc):
+    """Destroying a large-island handle frees every device buffer it took
+    (trials, rotation operands and results, Q planes, re-check rotations)."""
+    import torch
+    specs = [(0, 300, 256, 1), (6, 200, 256, 1), (3, 50, 512, 1)]
+
+    def cycle():
+        eng, _ = make_engine(sgemtf, orc, specs, seed=3, precision=1, transfer_interval=2)
+        eng.reset()
+        eng.run(3)
+        eng.close()
+
+    cycle()  # the first handle also brings up the context's own allocations
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        cycle()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 >= free0 - (8 << 20), (free0, free1)
+
