@@ -96,7 +96,7 @@ struct Smem {
   // tensor-core form
   unsigned char *A, *B;
   uint32_t a_saddr, b_saddr, mma_bar, tma_bar, tmem;
-  uint32_t acc_cols;  // TMEM columns per accumulator (accumulator k starts at k * acc_cols)
+  // two accumulators of 128 TMEM columns: accumulator k at column 128 k
   int nmma;           // MMAs per rotation
   int bplanes;        // B tiles per K block
   bool paired;        // Q in 64-row tiles, N = 128 MMAs over two of them
@@ -892,7 +892,6 @@ __device__ __forceinline__ void epoch_body(const EpochArgs& a, const void* tmap,
     s.mma_bar = cta.mma_bar;
     s.tma_bar = cta.tma_bar;
     s.tmem = cta.tmem;
-    s.acc_cols = 128;
     s.dead = &cta.hdr->dead;
     s.wait_ns = a.wait_ns ? a.wait_ns : tc::kWaitLimitNs;
     s.lose_completion = (a.flags & FLAG_TEST_LOST_COMPLETION) != 0;
