@@ -148,7 +148,8 @@ struct LargeArgs {
   double* zr;            // FP64-class rotations of the jobs, 2 x pop offsets, stride DP
   int32_t* work;         // decision work items: task << 16 | tie
   int32_t* rwork;        // rotation work items: task << 16 | column block << 12 | job chunk
-  int32_t* nwork;        // [0] decision items, [1] rotation items
+  int32_t* nwork;        // [0] decision items, [1] rotation items, [2] [3] the next
+                         // rotation / decision item to hand out
   int32_t rot_grid, decide_grid;  // persistent grids of the two re-check kernels
   int32_t algorithm;
   float F, CR, eta_c, p_c, eta_m, p_m;

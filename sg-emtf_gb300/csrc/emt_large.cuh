@@ -866,12 +866,23 @@ __device__ __forceinline__ void rot_item(const LargeArgs& a, const TaskDev& td, 
   }
 }
 
+// Next work item of a persistent grid: one atomic on a device-wide counter
+// per item, broadcast to the CTA through shared memory, so CTAs that draw
+// cheap items take more of them.
+__device__ __forceinline__ int next_item(int* counter, int* slot) {
+  __syncthreads();  // every thread has read the previous item's index
+  if (threadIdx.x == 0) *slot = atomicAdd(counter, 1);
+  __syncthreads();
+  return *slot;
+}
+
 __global__ void __launch_bounds__(kRotCols) rot_kernel(const LargeArgs a) {
   static_assert(kRotJobs == 8, "the job-count dispatch below covers 1..8");
   __shared__ __align__(16) float2 pr[kRotTile][kRotJobs];
   __shared__ const float* jrow[kRotJobs];
+  __shared__ int slot;
   const int items = a.nwork[1];
-  for (int w = blockIdx.x; w < items; w += gridDim.x) {
+  for (int w = next_item(a.nwork + 2, &slot); w < items; w = next_item(a.nwork + 2, &slot)) {
     const int code = a.rwork[w];
     const int task = code >> 16, blk = (code >> 12) & 15, chunk = code & 0xFFF;
     const TaskDev td = a.tasks[task];
@@ -925,8 +936,9 @@ __global__ void __launch_bounds__(256) decide_kernel(const LargeArgs a, int mode
   __shared__ double zmem[kMaxDimLarge];  // a member's rotation, when a tie needs it here
   const CtaTeam tm{scratch};
   const bool strict = mode == SEL_IMPORT || mode == SEL_MIGRATE;  // candidates must be better
+  __shared__ int slot;
   const int items = a.nwork[0];
-  for (int w = blockIdx.x; w < items; w += gridDim.x) {
+  for (int w = next_item(a.nwork + 3, &slot); w < items; w = next_item(a.nwork + 3, &slot)) {
     const int task = a.work[w] >> 16, i = a.work[w] & 0xFFFF;
     const TaskDev td = a.tasks[task];
     int k = 0;
@@ -1123,7 +1135,7 @@ int emt_large_select(const emt::LargeArgs& a, int mode, void* stream) {
 }
 
 int emt_large_selection(const emt::LargeArgs& a, int mode, void* stream) {
-  cudaError_t e = cudaMemsetAsync(a.nwork, 0, 2 * sizeof(int32_t), (cudaStream_t)stream);
+  cudaError_t e = cudaMemsetAsync(a.nwork, 0, 4 * sizeof(int32_t), (cudaStream_t)stream);
   if (e != cudaSuccess) return (int)e;
   emt::large::classify_kernel<<<a.n_tasks, 256, 0, (cudaStream_t)stream>>>(a, mode);
   emt::large::rot_kernel<<<a.rot_grid, emt::large::kRotCols, 0, (cudaStream_t)stream>>>(a);
