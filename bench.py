@@ -1118,7 +1118,10 @@ def main():
                                  rotation_matrix=Qs[t], shift=shifts[t])
                  for t, f in enumerate(fids)]
         dp = (DIM + 3) // 4 * 4
-        h2d = n * (DIM * dp * 4 + dp * 4 + 96 + 4)
+        # the library's copies: each rotation row-major (rows padded to dp;
+        # transposed and split on the device), the shift, the task table
+        # entry (88 B) and its two schedule-order slots
+        h2d = n * (DIM * dp * 4 + dp * 4 + 88 + 8)
         d2h = n * 4 + 4
         times = []
         for it in range(max(1, args.steps)):

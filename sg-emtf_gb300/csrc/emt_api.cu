@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <new>
 #include <numeric>
@@ -242,31 +243,6 @@ int max_smem_optin(int device) {
   return v;
 }
 
-// TF32 hi part of x, round to nearest with ties away from zero on the
-// magnitude (what cvt.rna.tf32.f32 computes); lo = x - hi is exact in FP32.
-float tf32_hi(float x) {
-  uint32_t b;
-  std::memcpy(&b, &x, 4);
-  b = (b + 0x1000u) & 0xFFFFE000u;
-  float r;
-  std::memcpy(&r, &b, 4);
-  return r;
-}
-
-// BF16 round to nearest even (what cvt.rn.bf16.f32 computes), and back.
-uint16_t bf16_rn(float x) {
-  uint32_t b;
-  std::memcpy(&b, &x, 4);
-  b += 0x7FFFu + ((b >> 16) & 1u);
-  return (uint16_t)(b >> 16);
-}
-float bf16_value(uint16_t h) {
-  const uint32_t b = (uint32_t)h << 16;
-  float r;
-  std::memcpy(&r, &b, 4);
-  return r;
-}
-
 bool device_has_tcgen05(int device) {
   int major = 0;
   if (cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device) != cudaSuccess)
@@ -354,7 +330,7 @@ int encode_planes(emt_handle* h, CUtensorMap* map, float* base, int K, int64_t r
 // rotation operands S (rows of a task padded to 128, Kp columns; FP32, or
 // TF32 hi and lo planes) and results Z (Nq columns), and for the tensor-core
 // form Q's TF32 hi/lo planes, Nq rows per task, with their TMA maps.
-int large_upload(emt_handle* h, int64_t pop, int32_t fit) {
+int large_upload(emt_handle* h, int64_t pop, int32_t fit, emt::QPlanes* qp) {
   const int n = (int)h->tasks.size();
   int dmax = 1, dpmax = 4;
   for (const auto& t : h->tasks) dmax = std::max(dmax, t.D);
@@ -399,22 +375,13 @@ int large_upload(emt_handle* h, int64_t pop, int32_t fit) {
   if (!h->large_tc) return EMT_OK;
   const size_t plane = (size_t)n * h->lNq * h->lKp, per = (size_t)h->lNq * h->lKp;
   if ((e = h->d_qbig.ensure(2 * plane))) return h->cuda_fail(e, "cudaMalloc");
-  std::vector<float> hi(per), lo(per);
-  for (int t = 0; t < n; ++t) {
-    const HostTask& ht = h->tasks[t];
-    std::fill(hi.begin(), hi.end(), 0.f);
-    std::fill(lo.begin(), lo.end(), 0.f);
-    for (int r = 0; r < ht.D; ++r)
-      for (int c = 0; c < ht.D; ++c) {
-        const float v = ht.Q[(size_t)r * ht.D + c];
-        const float vh = tf32_hi(v);
-        hi[(size_t)r * h->lKp + c] = vh;
-        lo[(size_t)r * h->lKp + c] = tf32_hi(v - vh);  // rounded, as the S planes are
-      }
-    if ((e = cudaMemcpy(h->d_qbig.p + (size_t)t * per, hi.data(), sizeof(float) * per, cudaMemcpyHostToDevice)) ||
-        (e = cudaMemcpy(h->d_qbig.p + plane + (size_t)t * per, lo.data(), sizeof(float) * per, cudaMemcpyHostToDevice)))
-      return h->cuda_fail(e, "upload");
-  }
+  if ((e = cudaMemset(h->d_qbig.p, 0, sizeof(float) * 2 * plane))) return h->cuda_fail(e, "upload");
+  // TF32 hi and lo of Q, the lo part rounded as the S planes' is
+  qp->base = h->d_qbig.p;
+  qp->task_stride = (int64_t)per;
+  qp->plane_stride = (int64_t)plane;
+  qp->row_stride = h->lKp;
+  qp->kind = emt::QPLANES_TF32;
   int rc = encode_planes(h, &h->smap, h->d_S.p, h->lKp, rows, emt::kLargeBM);
   if (!rc) rc = encode_planes(h, &h->qmap, h->d_qbig.p, h->lKp, (int64_t)n * h->lNq, emt::kLargeBN);
   return rc;
@@ -541,12 +508,18 @@ int upload(emt_handle* h) {
   }
   h->tuned = 0;
 
-  std::vector<float> hq((size_t)q, 0.f), ho((size_t)o, 0.f);
+  // rotations go up row-major (rows padded to DP with zeros) and are
+  // transposed and split on the device (emt_prepare_rotations)
+  std::unique_ptr<float[]> hq(new float[(size_t)q]);
+  std::vector<float> ho((size_t)o, 0.f);
   for (int t = 0; t < n; ++t) {
     const HostTask& ht = h->tasks[t];
     const TaskDev& d = h->table[t];
-    for (int k = 0; k < ht.D; ++k)
-      for (int c = 0; c < ht.D; ++c) hq[(size_t)d.q_off + (size_t)k * d.DP + c] = ht.Q[(size_t)c * ht.D + k];
+    for (int r = 0; r < ht.D; ++r) {
+      float* row = hq.get() + d.q_off + (size_t)r * d.DP;
+      std::memcpy(row, ht.Q.data() + (size_t)r * ht.D, sizeof(float) * ht.D);
+      std::fill(row + ht.D, row + d.DP, 0.f);
+    }
     for (int j = 0; j < ht.D; ++j) ho[(size_t)d.o_off + j] = ht.o[j];
   }
   cudaError_t e;
@@ -573,7 +546,7 @@ int upload(emt_handle* h) {
       if ((e = h->d_elites[b].ensure((size_t)el)) != cudaSuccess) return h->cuda_fail(e, "cudaMalloc");
   if ((e = cudaMemcpy(h->d_tasks.p, h->table.data(), sizeof(TaskDev) * n, cudaMemcpyHostToDevice)) ||
       (e = cudaMemcpy(h->d_order.p, h->order.data(), sizeof(int32_t) * 2 * n, cudaMemcpyHostToDevice)) ||
-      (e = cudaMemcpy(h->d_qt.p, hq.data(), sizeof(float) * hq.size(), cudaMemcpyHostToDevice)) ||
+      (e = cudaMemcpy(h->d_qt.p, hq.get(), sizeof(float) * (size_t)q, cudaMemcpyHostToDevice)) ||
       (e = cudaMemcpy(h->d_shift.p, ho.data(), sizeof(float) * ho.size(), cudaMemcpyHostToDevice)) ||
       (e = cudaMemset(h->d_gen.p, 0, sizeof(uint32_t) * n)) ||
       (e = cudaMemset(h->d_pop.p, 0, sizeof(float) * (size_t)pop)) ||
@@ -581,45 +554,34 @@ int upload(emt_handle* h) {
       (e = cudaMemset(h->d_zcb.p, 0xFF, sizeof(float) * 2 * (size_t)fit)) ||
       (e = cudaMemset(h->d_err.p, 0, sizeof(int32_t))))
     return h->cuda_fail(e, "upload");
+  emt::QPlanes planes;
   if (h->use_tc) {
     // Q's split parts, part-major per task: TF32 hi and lo (both rounded to
     // nearest, as the A tiles are), or the exact three BF16 parts
     const size_t plane = (size_t)h->tc_np * h->tc_kp;
     const size_t per = (h->tc_bf16 ? 3 : 2) * plane;
-    const size_t esz = h->tc_bf16 ? sizeof(uint16_t) : sizeof(float);
-    std::vector<unsigned char> hqc(per * n * esz, 0);
-    for (int t = 0; t < n; ++t) {
-      const HostTask& ht = h->tasks[t];
-      for (int r = 0; r < ht.D; ++r)
-        for (int c = 0; c < ht.D; ++c) {
-          const float v = ht.Q[(size_t)r * ht.D + c];
-          const size_t at = per * t + (size_t)r * h->tc_kp + c;
-          if (h->tc_bf16) {
-            uint16_t* q = reinterpret_cast<uint16_t*>(hqc.data());
-            const uint16_t p0 = bf16_rn(v);
-            const float r1 = v - bf16_value(p0);
-            const uint16_t p1 = bf16_rn(r1);
-            q[at] = p0;
-            q[at + plane] = p1;
-            q[at + 2 * plane] = bf16_rn(r1 - bf16_value(p1));
-          } else {
-            float* q = reinterpret_cast<float*>(hqc.data());
-            const float vh = tf32_hi(v);
-            q[at] = vh;
-            q[at + plane] = tf32_hi(v - vh);
-          }
-        }
-    }
-    if ((e = h->d_qtc.ensure((hqc.size() + 3) / 4)) != cudaSuccess) return h->cuda_fail(e, "cudaMalloc");
-    if ((e = cudaMemcpy(h->d_qtc.p, hqc.data(), hqc.size(), cudaMemcpyHostToDevice)))
-      return h->cuda_fail(e, "upload");
+    const size_t bytes = per * n * (h->tc_bf16 ? sizeof(uint16_t) : sizeof(float));
+    if ((e = h->d_qtc.ensure((bytes + 3) / 4)) != cudaSuccess) return h->cuda_fail(e, "cudaMalloc");
+    if ((e = cudaMemset(h->d_qtc.p, 0, bytes)) != cudaSuccess) return h->cuda_fail(e, "upload");
+    planes.base = h->d_qtc.p;
+    planes.task_stride = (int64_t)per;
+    planes.plane_stride = (int64_t)plane;
+    planes.row_stride = h->tc_kp;
+    planes.kind = h->tc_bf16 ? emt::QPLANES_BF16 : emt::QPLANES_TF32;
     int rc = encode_qtc_map(h);
     if (rc) return rc;
   }
   if (h->large) {
-    int rc = large_upload(h, pop, fit);
+    int rc = large_upload(h, pop, fit, &planes);
     if (rc) return rc;
   }
+  int dmax = 1;
+  for (const auto& t : h->tasks) dmax = std::max(dmax, t.D);
+  int pe = emt_prepare_rotations(h->d_tasks.p, n, dmax, h->d_qt.p, planes, nullptr);
+  // the uploads and memsets above run on the legacy default stream: finish
+  // them before the caller's stream (possibly a non-blocking one) runs
+  if (!pe) pe = (int)cudaStreamSynchronize(nullptr);
+  if (pe) return h->cuda_fail((cudaError_t)pe, "rotation preparation");
   h->uploaded = true;
   h->initialized = false;
   return EMT_OK;

@@ -446,6 +446,20 @@ struct BestArgs {
   float* best_err;
 };
 
+// The tensor-core forms' split copies of each task's Q, written on the
+// device by emt_prepare_rotations: part p of Q[r][c] of task t at
+// base + t * task_stride + p * plane_stride + r * row_stride + c (elements),
+// TF32 hi and lo (float; each rounded to nearest, ties away, as
+// cvt.rna.tf32.f32 does; lo = tf32(Q - hi)) or the three exact BF16 parts
+// (round to nearest even, each part of the remainder of the previous ones).
+enum QPlaneKind : int32_t { QPLANES_NONE = 0, QPLANES_TF32 = 1, QPLANES_BF16 = 2 };
+struct QPlanes {
+  void* base = nullptr;
+  int64_t task_stride = 0;
+  int64_t plane_stride = 0;
+  int32_t row_stride = 0;
+  int32_t kind = QPLANES_NONE;
+};
 
 }  // namespace emt
 
@@ -471,3 +485,9 @@ void emt_large_recheck_grids(int sms, int32_t* rot, int32_t* decide);
 // them, apply
 int emt_large_selection(const emt::LargeArgs& a, int mode, void* stream);
 int emt_launch_best(const emt::BestArgs& a, void* stream);
+// Rotation matrices arrive in qt row-major (Q[r][c] at q_off + r * DP + c,
+// zero columns from D to DP); transposes them in place to the kernels'
+// layout (qt[q_off + k * DP + n] = Q[n][k]) and writes the split planes
+// (whose buffer the caller has zeroed).  max_dim: the largest D.
+int emt_prepare_rotations(const emt::TaskDev* tasks, int n_tasks, int max_dim, float* qt,
+                          const emt::QPlanes& planes, void* stream);

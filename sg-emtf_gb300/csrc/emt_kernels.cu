@@ -1300,7 +1300,80 @@ __global__ void __launch_bounds__(32) best_kernel(const BestArgs a) {
   }
 }
 
+// TF32 part of x: round to nearest, ties away from zero, on the bit pattern
+// (finite x); x - tf32_rna(x) is exact in FP32.
+__device__ __forceinline__ float tf32_rna(float x) {
+  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+}
+// BF16 part of x: round to nearest even on the bit pattern (finite x).
+__device__ __forceinline__ uint32_t bf16_rne(float x) {
+  const uint32_t b = __float_as_uint(x);
+  return (b + 0x7FFFu + ((b >> 16) & 1u)) >> 16;
+}
+__device__ __forceinline__ float bf16_val(uint32_t h) { return __uint_as_float(h << 16); }
+
+__device__ __forceinline__ void put_planes(const QPlanes& pl, int t, int r, int c, float v) {
+  const size_t at = (size_t)t * pl.task_stride + (size_t)r * pl.row_stride + c;
+  if (pl.kind == QPLANES_BF16) {
+    uint16_t* q = static_cast<uint16_t*>(pl.base);
+    const uint32_t p0 = bf16_rne(v);
+    const float r1 = __fsub_rn(v, bf16_val(p0));  // exact
+    const uint32_t p1 = bf16_rne(r1);
+    q[at] = (uint16_t)p0;
+    q[at + pl.plane_stride] = (uint16_t)p1;
+    q[at + 2 * pl.plane_stride] = (uint16_t)bf16_rne(__fsub_rn(r1, bf16_val(p1)));
+  } else if (pl.kind == QPLANES_TF32) {
+    float* q = static_cast<float*>(pl.base);
+    const float vh = tf32_rna(v);
+    q[at] = vh;
+    q[at + pl.plane_stride] = tf32_rna(__fsub_rn(v, vh));
+  }
+}
+
+// One CTA per task and pair of 32 x 32 tiles (i, j), (j, i) with i <= j: both
+// tiles are read into shared memory before either is written, so the in-place
+// transpose has one writer per element; the split planes are written from the
+// same tiles, along rows of Q.
+__global__ void __launch_bounds__(256) prepare_rotations_kernel(const TaskDev* tasks, float* qt,
+                                                                const QPlanes pl) {
+  const int t = blockIdx.x, bi = blockIdx.y, bj = blockIdx.z;
+  if (bi > bj) return;
+  const TaskDev td = tasks[t];
+  const int D = td.D, DP = td.DP;
+  if (bj * 32 >= D) return;
+  __shared__ float ta[32][33], tb[32][33];  // Q[32 bi + y][32 bj + x], Q[32 bj + y][32 bi + x]
+  float* q = qt + td.q_off;
+  const int x = threadIdx.x & 31, y0 = threadIdx.x >> 5;
+  for (int y = y0; y < 32; y += 8) {
+    const int ra = 32 * bi + y, ca = 32 * bj + x, rb = 32 * bj + y, cb = 32 * bi + x;
+    ta[y][x] = (ra < D && ca < D) ? q[(size_t)ra * DP + ca] : 0.f;
+    tb[y][x] = (rb < D && cb < D) ? q[(size_t)rb * DP + cb] : 0.f;
+  }
+  __syncthreads();
+  for (int y = y0; y < 32; y += 8) {
+    const int ra = 32 * bi + y, ca = 32 * bj + x;
+    if (ra < D && ca < D) {
+      if (pl.kind != QPLANES_NONE) put_planes(pl, t, ra, ca, ta[y][x]);
+      q[(size_t)ra * DP + ca] = tb[x][y];  // Q^T[ra][ca] = Q[ca][ra]
+    }
+    const int rb = 32 * bj + y, cb = 32 * bi + x;
+    if (bi != bj && rb < D && cb < D) {
+      if (pl.kind != QPLANES_NONE) put_planes(pl, t, rb, cb, tb[y][x]);
+      q[(size_t)rb * DP + cb] = ta[x][y];
+    }
+  }
+}
+
 }  // namespace emt
+
+int emt_prepare_rotations(const emt::TaskDev* tasks, int n_tasks, int max_dim, float* qt,
+                          const emt::QPlanes& planes, void* stream) {
+  if (n_tasks <= 0 || max_dim <= 0) return 0;
+  const unsigned tiles = (unsigned)(max_dim + 31) / 32;
+  emt::prepare_rotations_kernel<<<dim3((unsigned)n_tasks, tiles, tiles), 256, 0,
+                                  (cudaStream_t)stream>>>(tasks, qt, planes);
+  return (int)cudaGetLastError();
+}
 
 int emt_launch_best(const emt::BestArgs& a, void* stream) {
   if (a.n_tasks <= 0) return 0;
