@@ -1046,7 +1046,8 @@ int join_tasks(emt_handle* h, std::vector<HostTask>& add) {
     h->uploaded = false;
     h->initialized = false;
     if (!emt_reset(h, h->stream) && !emt_restore(h, before.data(), before.size()) &&
-        cudaMemcpy(h->d_stats.p, st, sizeof(st), cudaMemcpyHostToDevice) == cudaSuccess)
+        cudaMemcpy(h->d_stats.p, st, sizeof(st), cudaMemcpyHostToDevice) == cudaSuccess &&
+        cudaStreamSynchronize(nullptr) == cudaSuccess)
       h->gen_joined = joined;
     h->err = why;
     return rc;
@@ -1073,7 +1074,8 @@ int join_tasks(emt_handle* h, std::vector<HostTask>& add) {
   }
   if ((rc = emt_restore(h, merged.data(), merged.size()))) return rc;
   st[3] += np_new;  // the new islands' initial evaluation
-  if ((e = cudaMemcpy(h->d_stats.p, st, sizeof(st), cudaMemcpyHostToDevice)) != cudaSuccess)
+  if ((e = cudaMemcpy(h->d_stats.p, st, sizeof(st), cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(nullptr)) != cudaSuccess)
     return h->cuda_fail(e, "restore stats");
   h->gen_joined = joined + (uint64_t)gdone * (h->tasks.size() - n_old);
   return EMT_OK;
@@ -1423,6 +1425,7 @@ int emt_sync(emt_handle_t* h) {
     if (e != cudaSuccess) return h->cuda_fail(e, "error word");
     if (code) {
       cudaMemset(h->d_err.p, 0, sizeof(int32_t));
+      cudaStreamSynchronize(nullptr);  // cleared before the next launch on any stream
       return h->fail(EMT_ERR_DEVICE_CHECK, "device check " + std::to_string(code) +
                                                (code == emt::CHECK_BAD_DESCRIPTOR ? " (bad task descriptor)"
                                                 : code == emt::CHECK_SMEM_TOO_SMALL ? " (shared memory too small)"
@@ -1513,12 +1516,14 @@ int emt_set_population(emt_handle_t* h, int32_t task, const float* x) {
   const TaskDev& d = h->table[task];
   for (size_t k = 0; k < (size_t)d.NP * d.D; ++k)
     if (!(x[k] >= d.lo && x[k] <= d.hi)) return h->fail(EMT_ERR_INVALID_ARG, "member outside the box");
-  cudaError_t e = cudaMemcpy2D(h->d_pop.p + d.pop_off, sizeof(float) * d.DP, x, sizeof(float) * d.D,
-                               sizeof(float) * d.D, d.NP, cudaMemcpyHostToDevice);
+  // on the handle's stream, ahead of the evaluation launched there
+  cudaError_t e = cudaMemcpy2DAsync(h->d_pop.p + d.pop_off, sizeof(float) * d.DP, x,
+                                    sizeof(float) * d.D, sizeof(float) * d.D, d.NP,
+                                    cudaMemcpyHostToDevice, h->stream);
   if (e != cudaSuccess) return h->cuda_fail(e, "copy population");
   int le;
   if (h->large) {  // re-evaluates every island (unchanged ones get the same values)
-    e = cudaMemset(h->d_fit64.p + d.fit_off, 0xFF, sizeof(double) * d.NP);
+    e = cudaMemsetAsync(h->d_fit64.p + d.fit_off, 0xFF, sizeof(double) * d.NP, h->stream);
     if (e != cudaSuccess) return h->cuda_fail(e, "reset cache");
     le = large_eval_members(h, h->stream);
   } else {
@@ -1573,7 +1578,7 @@ int emt_evaluate(emt_handle_t* h, int32_t task, int32_t n, const float* x, float
     cudaFree(df);
     return h->cuda_fail(e, "cudaMalloc");
   }
-  e = cudaMemcpy(dx, x, sizeof(float) * (size_t)n * t.D, cudaMemcpyHostToDevice);
+  e = cudaMemcpyAsync(dx, x, sizeof(float) * (size_t)n * t.D, cudaMemcpyHostToDevice, h->stream);
   int out = EMT_OK;
   if (e == cudaSuccess) {
     emt::EvalArgs a{h->d_tasks.p, task, n, dx, df, dz, h->d_qt.p, h->d_shift.p, h->d_err.p,
@@ -1731,6 +1736,9 @@ int emt_restore(emt_handle_t* h, const void* buf, size_t bytes) {
   cudaError_t ez = cudaMemset(h->d_zcb.p, 0xFF, sizeof(float) * h->d_zcb.n);
   if (ez == cudaSuccess && h->d_wprec.p)  // restored values are not known to be float-float
     ez = cudaMemset(h->d_wprec.p, 0xFF, sizeof(float) * h->d_wprec.n);
+  // the copies and memsets above run on the legacy default stream, which a
+  // non-blocking caller stream does not wait for
+  if (ez == cudaSuccess) ez = cudaStreamSynchronize(nullptr);
   if (ez != cudaSuccess) return h->cuda_fail(ez, "restore");
   h->gdone = (uint32_t)hdr[2];
   h->initialized = true;

@@ -662,6 +662,9 @@ int cvrp_upload(emt_cvrp_handle* h) {
       (e = cudaMemset(h->d_stats.p, 0, sizeof(unsigned long long) * 3)) ||
       (e = cudaMemset(h->d_err.p, 0, sizeof(int32_t))))
     return h->cuda_fail(e, "upload");
+  // the copies and memsets above run on the legacy default stream, which a
+  // non-blocking caller stream does not wait for
+  if ((e = cudaStreamSynchronize(nullptr)) != cudaSuccess) return h->cuda_fail(e, "upload");
   h->uploaded = true;
   h->initialized = false;
   return EMT_OK;
@@ -865,6 +868,7 @@ int emt_cvrp_sync(emt_cvrp_handle_t* h) {
     if (e != cudaSuccess) return h->cuda_fail(e, "error word");
     if (code) {
       cudaMemset(h->d_err.p, 0, sizeof(int32_t));
+      cudaStreamSynchronize(nullptr);  // cleared before the next launch on any stream
       return h->fail(EMT_ERR_DEVICE_CHECK, "device check " + std::to_string(code));
     }
   }
@@ -946,7 +950,7 @@ int emt_cvrp_evaluate(emt_cvrp_handle_t* h, int32_t inst, int32_t count, const u
   int32_t* dc = nullptr;
   cudaError_t e = cudaMalloc((void**)&dp, (size_t)count * n);
   if (e == cudaSuccess) e = cudaMalloc((void**)&dc, sizeof(int32_t) * count);
-  if (e == cudaSuccess) e = cudaMemcpy(dp, perms, (size_t)count * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dp, perms, (size_t)count * n, cudaMemcpyHostToDevice, h->stream);
   auto kern = h->shape.qb == 1 ? emt::cvrp::cvrp_eval_kernel<1>
              : h->shape.qb == 2 ? emt::cvrp::cvrp_eval_kernel<2> : emt::cvrp::cvrp_eval_kernel<4>;
   if (e == cudaSuccess)
