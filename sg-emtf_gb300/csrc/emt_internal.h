@@ -174,9 +174,10 @@ enum BuildMode : int { BUILD_X = 0, BUILD_TRIALS = 1, BUILD_CANDIDATES = 2 };
 enum SelectMode : int {
   SEL_GENERATION = 0, SEL_IMPORT = 1, SEL_EXPORT = 2, SEL_RANK = 3, SEL_MIGRATE = 4
 };
-// Near-tie rotation work items (rot_kernel): kRotCols outputs of up to
-// kRotJobs rows of one task, one output per thread (registers: 2 per job and
-// thread).  A build may set other shapes through EMT_ROT_COLS / EMT_ROT_JOBS.
+// Near-tie rotation work items (rot_kernel): 2 kRotCols outputs of up to
+// kRotJobs rows of one task on kRotCols threads, two outputs per thread
+// (registers: 4 per job and thread).  A build may set other shapes through
+// EMT_ROT_COLS / EMT_ROT_JOBS.
 #ifndef EMT_ROT_COLS
 #define EMT_ROT_COLS 128
 #endif
@@ -188,7 +189,7 @@ constexpr int kRotJobs = EMT_ROT_JOBS;
 // Rotation items a task can list in one selection step: column blocks x job
 // chunks, with up to two jobs (trial and member) per selected row
 EMT_HD int64_t rot_items_max(int D, int NP) {
-  return (int64_t)((D + kRotCols - 1) / kRotCols) * ((2 * NP + kRotJobs - 1) / kRotJobs);
+  return (int64_t)((D + 2 * kRotCols - 1) / (2 * kRotCols)) * ((2 * NP + kRotJobs - 1) / kRotJobs);
 }
 }  // namespace large
 

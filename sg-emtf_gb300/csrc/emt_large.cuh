@@ -711,7 +711,7 @@ constexpr int kRotTile = 128;
 // row | member << 16, tie jobs trial | (member + 1) << 16, decisions
 // task << 16 | tie (tasks < 2^15, checked on the host).  Rotation items per
 // task: at most rot_items_max(D, NP), which the host allocates per task.
-static_assert((kMaxDimLarge + kRotCols - 1) / kRotCols <= 16, "column block in 4 bits");
+static_assert((kMaxDimLarge + 2 * kRotCols - 1) / (2 * kRotCols) <= 16, "column block in 4 bits");
 static_assert((2 * kMaxPopLarge + kRotJobs - 1) / kRotJobs < 4096, "job chunk in 12 bits");
 static_assert(2 * kMaxPopLarge + 1 < 0xFFFF, "job and tie indices in 16 bits");
 static_assert(kRotCols >= kRotJobs && kRotCols % 32 == 0, "row pointers set by the first threads");
@@ -777,7 +777,7 @@ __global__ void __launch_bounds__(256) classify_kernel(const LargeArgs a, int mo
   if (threadIdx.x == 0) {
     a.ntie[task] = ties;
     a.njob[task] = nj;
-    const int blocks = (D + kRotCols - 1) / kRotCols, chunks = (nj + kRotJobs - 1) / kRotJobs;
+    const int blocks = (D + 2 * kRotCols - 1) / (2 * kRotCols), chunks = (nj + kRotJobs - 1) / kRotJobs;
     if (chunks) {
       const int w0 = atomicAdd(a.nwork + 1, blocks * chunks);
       for (int b = 0; b < blocks; ++b)
@@ -786,50 +786,57 @@ __global__ void __launch_bounds__(256) classify_kernel(const LargeArgs a, int mo
   }
 }
 
-// Rotation work item: outputs [kRotCols b, kRotCols (b + 1)) of up to kRotJobs rows of
-// one task (small items keep the grid busy when few islands have near ties).  A persistent grid takes items from the queue; each thread owns
-// one output and streams its column of Q once for all the item's rows, the
-// exact splits x - o of the rows staged in shared memory a k-tile at a time.
-// Each output keeps dot2_pair's order over k, so the values equal
-// precise_rotation's.
+// Rotation work item: outputs [2 kRotCols b, 2 kRotCols (b + 1)) of up to
+// kRotJobs rows of one task (small items keep the grid busy when few islands
+// have near ties).  A persistent grid takes items from the queue; each thread
+// owns outputs n and n + kRotCols and streams their columns of Q once for all
+// the item's rows, the exact splits x - o of the rows staged in shared memory
+// a k-tile at a time (each staged pair serves both outputs: 1.5% faster at
+// D = 1000 than one output per thread).  Each output keeps dot2_pair's order
+// over k, so the values equal precise_rotation's.
+// Compensated product q * (h + l) into the running sums S, C of one output.
+__device__ __forceinline__ void comp_step(float q, float2 hl, float& S, float& C) {
+  const float pp = __fmul_rn(q, hl.x);
+  const float e = __fmaf_rn(q, hl.x, -pp);
+  float t, te;
+  two_sum(S, pp, t, te);
+  S = t;
+  C = __fmaf_rn(q, hl.y, __fadd_rn(C, __fadd_rn(te, e)));
+}
 // The compensated products of J rows (J = the item's job count, fixed at
 // compile time so a partial chunk costs in proportion to its rows) for the
-// k-tile in pr, into the running sums S, C of this thread's output.
+// k-tile in pr, into S[0..J), C[0..J) (output n, column qa of Q) and
+// S[J..2J), C[J..2J) (output n + kRotCols, column qb).
 template <int J>
-__device__ __forceinline__ void rot_tile(const float2 (*pr)[kRotJobs], const float* qcol, int k0,
-                                         int kt, int DP, float* S, float* C) {
-  constexpr int kAhead = 16;  // Q loads issued ahead of the dependent updates
+__device__ __forceinline__ void rot_tile(const float2 (*pr)[kRotJobs], const float* qa,
+                                         const float* qb, int k0, int kt, int DP, float* S,
+                                         float* C) {
+  constexpr int kAhead = 8;  // Q loads issued ahead of the dependent updates
   int kk = 0;
   for (; kk + kAhead <= kt; kk += kAhead) {
-    float qv[kAhead];
-#pragma unroll
-    for (int u = 0; u < kAhead; ++u) qv[u] = __ldg(qcol + (size_t)(k0 + kk + u) * DP);
+    float va[kAhead], vb[kAhead];
 #pragma unroll
     for (int u = 0; u < kAhead; ++u) {
-      const float q = qv[u];
+      va[u] = __ldg(qa + (size_t)(k0 + kk + u) * DP);
+      vb[u] = __ldg(qb + (size_t)(k0 + kk + u) * DP);
+    }
+#pragma unroll
+    for (int u = 0; u < kAhead; ++u) {
 #pragma unroll
       for (int j = 0; j < J; ++j) {
         const float2 hl = pr[kk + u][j];
-        const float pp = __fmul_rn(q, hl.x);
-        const float e = __fmaf_rn(q, hl.x, -pp);
-        float t, te;
-        two_sum(S[j], pp, t, te);
-        S[j] = t;
-        C[j] = __fmaf_rn(q, hl.y, __fadd_rn(C[j], __fadd_rn(te, e)));
+        comp_step(va[u], hl, S[j], C[j]);
+        comp_step(vb[u], hl, S[J + j], C[J + j]);
       }
     }
   }
   for (; kk < kt; ++kk) {
-    const float q = __ldg(qcol + (size_t)(k0 + kk) * DP);
+    const float a = __ldg(qa + (size_t)(k0 + kk) * DP), b = __ldg(qb + (size_t)(k0 + kk) * DP);
 #pragma unroll
     for (int j = 0; j < J; ++j) {
       const float2 hl = pr[kk][j];
-      const float pp = __fmul_rn(q, hl.x);
-      const float e = __fmaf_rn(q, hl.x, -pp);
-      float t, te;
-      two_sum(S[j], pp, t, te);
-      S[j] = t;
-      C[j] = __fmaf_rn(q, hl.y, __fadd_rn(C[j], __fadd_rn(te, e)));
+      comp_step(a, hl, S[j], C[j]);
+      comp_step(b, hl, S[J + j], C[J + j]);
     }
   }
 }
@@ -841,15 +848,16 @@ __device__ __forceinline__ void rot_item(const LargeArgs& a, const TaskDev& td, 
                                          float2 (*pr)[kRotJobs], const float* const* jrow) {
   const int D = td.D, DP = td.DP;
   const float* o = a.shift + td.o_off;
-  const int n = blk * kRotCols + threadIdx.x;
-  const bool live = n < D;
-  const float* qcol = a.qt + td.q_off + (live ? n : 0);
-  float S[J], C[J];
+  const int n = blk * 2 * kRotCols + threadIdx.x, m = n + kRotCols;
+  const bool live = n < D, live2 = m < D;
+  const float* qa = a.qt + td.q_off + (live ? n : 0);
+  const float* qb = live2 ? a.qt + td.q_off + m : qa;
+  float S[2 * J], C[2 * J];
 #pragma unroll
-  for (int j = 0; j < J; ++j) S[j] = C[j] = 0.f;
+  for (int j = 0; j < 2 * J; ++j) S[j] = C[j] = 0.f;
   for (int k0 = 0; k0 < D; k0 += kRotTile) {
     const int kt = min(kRotTile, D - k0);
-    __syncthreads();  // jrow written; the previous tile consumed
+    __syncthreads();
     for (int it = threadIdx.x; it < J * kt; it += blockDim.x) {
       const int j = it / kt, kk = it - j * kt;
       float sh, sl;
@@ -857,12 +865,16 @@ __device__ __forceinline__ void rot_item(const LargeArgs& a, const TaskDev& td, 
       pr[kk][j] = make_float2(sh, sl);
     }
     __syncthreads();
-    if (live) rot_tile<J>(pr, qcol, k0, kt, DP, S, C);
+    if (live) rot_tile<J>(pr, qa, qb, k0, kt, DP, S, C);
   }
+  double* z = a.zr + 2 * td.pop_off + (size_t)j0 * DP;
   if (live) {
-    double* z = a.zr + 2 * td.pop_off + (size_t)j0 * DP + n;
 #pragma unroll
-    for (int j = 0; j < J; ++j) z[(size_t)j * DP] = (double)S[j] + (double)C[j];
+    for (int j = 0; j < J; ++j) z[(size_t)j * DP + n] = (double)S[j] + (double)C[j];
+  }
+  if (live2) {
+#pragma unroll
+    for (int j = 0; j < J; ++j) z[(size_t)j * DP + m] = (double)S[J + j] + (double)C[J + j];
   }
 }
 
