@@ -429,15 +429,43 @@ __device__ __forceinline__ void dot2_pair(const float* __restrict__ x, const flo
 // The calling team fills zbuf[0..D) with the FP64-class rotation of row x,
 // one output per member of the team at a time (the team synchronises before
 // returning).
+// Outputs n + i st (i < 4) of the same compensated rotation, their four Dot2
+// chains interleaved for instruction-level parallelism; each keeps
+// dot2_pair's operations and order over k, so the values are the same.
+// Outputs at or beyond D repeat output n and are not stored.
+__device__ __forceinline__ void dot2_quad(const float* __restrict__ x, const float* __restrict__ o,
+                                          const float* __restrict__ qt, int DP, int D, int n,
+                                          int st, double* zbuf) {
+  int m[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) m[i] = n + i * st < D ? n + i * st : n;
+  float S[4] = {0.f, 0.f, 0.f, 0.f}, C[4] = {0.f, 0.f, 0.f, 0.f};
+  for (int k = 0; k < D; ++k) {
+    float sh, sl;
+    two_sum(x[k], -o[k], sh, sl);
+    const float* qk = qt + (size_t)k * DP;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float q = qk[m[i]];
+      const float p = __fmul_rn(q, sh);
+      const float e = __fmaf_rn(q, sh, -p);
+      float t, te;
+      two_sum(S[i], p, t, te);
+      S[i] = t;
+      C[i] = __fmaf_rn(q, sl, __fadd_rn(C[i], __fadd_rn(te, e)));
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+    if (n + i * st < D) zbuf[n + i * st] = (double)S[i] + (double)C[i];
+}
+
 template <class Team>
 __device__ void precise_rotation_team(const float* __restrict__ x, const float* __restrict__ o,
                                       const float* __restrict__ qt, int DP, int D, double* zbuf,
                                       const Team& tm) {
-  for (int n = tm.rank(); n < D; n += tm.size()) {
-    double a, b;
-    dot2_pair(x, o, qt, DP, D, n, false, a, b);
-    zbuf[n] = a;
-  }
+  const int st = tm.size();
+  for (int n = tm.rank(); n < D; n += 4 * st) dot2_quad(x, o, qt, DP, D, n, st, zbuf);
   tm.sum(0.0);  // a barrier of the team
 }
 
@@ -688,6 +716,63 @@ __device__ __noinline__ double eval_weier_precise(const FnConst& fc, const doubl
   return eval_weier_precise_t(fc, zbuf, WarpTeam{});
 }
 
+// weier_gene_precise of two genes, the two reductions and compensated sums
+// interleaved when both arguments take the 64-bit path (the usual case);
+// every operation of each gene is weier_gene_precise's.
+__device__ __forceinline__ void weier_gene_precise2(double z0, double z1, float& g0, float& g1) {
+  const unsigned long long b0 = (unsigned long long)__double_as_longlong(z0) & 0x7FFFFFFFFFFFFFFFull;
+  const unsigned long long b1 = (unsigned long long)__double_as_longlong(z1) & 0x7FFFFFFFFFFFFFFFull;
+  const int E0 = (int)(b0 >> 52), E1 = (int)(b1 >> 52);
+  const int sh0 = 1074 - E0, sh1 = 1074 - E1;
+  if (b0 == 0ull || E0 == 0 || sh0 <= 0 || sh0 >= 64 || b1 == 0ull || E1 == 0 || sh1 <= 0 ||
+      sh1 >= 64) {
+    g0 = weier_gene_precise(z0);
+    g1 = weier_gene_precise(z1);
+    return;
+  }
+  const unsigned long long mask0 = (2ull << sh0) - 1ull, mask1 = (2ull << sh1) - 1ull;
+  unsigned long long r0 = ((b0 & ((1ull << 52) - 1ull)) | (1ull << 52)) & mask0;
+  unsigned long long r1 = ((b1 & ((1ull << 52) - 1ull)) | (1ull << 52)) & mask1;
+  const int drop0 = sh0 > 24 ? sh0 - 24 : 0, drop1 = sh1 > 24 ? sh1 - 24 : 0;
+  const float scale0 = __uint_as_float((uint32_t)(127 - (sh0 - drop0)) << 23);
+  const float scale1 = __uint_as_float((uint32_t)(127 - (sh1 - drop1)) << 23);
+  float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f, ak = 1.f;
+  for (int k = 0; k <= 20; ++k) {
+    const float u0 = cospif(__uint2float_rn((uint32_t)(r0 >> drop0)) * scale0);
+    const float u1 = cospif(__uint2float_rn((uint32_t)(r1 >> drop1)) * scale1);
+    const float v0 = __fsub_rn(__fmul_rn(-ak, u0), c0);
+    const float v1 = __fsub_rn(__fmul_rn(-ak, u1), c1);
+    const float t0 = __fadd_rn(s0, v0), t1 = __fadd_rn(s1, v1);
+    c0 = __fsub_rn(__fsub_rn(t0, s0), v0);
+    c1 = __fsub_rn(__fsub_rn(t1, s1), v1);
+    s0 = t0;
+    s1 = t1;
+    ak *= 0.5f;
+    r0 = (r0 * 3ull) & mask0;
+    r1 = (r1 * 3ull) & mask1;
+  }
+  g0 = s0;
+  g1 = s1;
+}
+
+// eval_weier_precise_t with two genes per step of each team member, summed
+// in the same order (the same value).
+template <class Team>
+__device__ double eval_weier_precise_pair_t(const FnConst& fc, const double* zbuf, const Team& tm) {
+  const int st = tm.size();
+  double acc = 0.0;
+  int n = tm.rank();
+  for (; n + st < fc.D; n += 2 * st) {
+    float g0, g1;
+    weier_gene_precise2(zbuf[n], zbuf[n + st], g0, g1);
+    acc += (double)g0;
+    acc += (double)g1;
+  }
+  if (n < fc.D) acc += (double)weier_gene_precise(zbuf[n]);
+  acc = tm.sum(acc);
+  return acc + fc.woff64;
+}
+
 // Largest error of an eval_weier_precise value, per gene: each term's
 // argument y_k = 2 3^k |z| mod 2 reaches cospif as a 24-bit float after the
 // low bits are cut (< 2^-24) and the 25-bit rest rounded (<= 2^-24), so
@@ -800,6 +885,57 @@ __device__ __forceinline__ double weier_gene_ff(double z) {
     }
   }
   return (double)s.h + (double)s.l;
+}
+
+// weier_gene_ff of two genes, interleaved when both take the general path;
+// every operation of each gene is weier_gene_ff's.
+__device__ __forceinline__ void weier_gene_ff2(double z0, double z1, double& g0, double& g1) {
+  const unsigned long long b0 = (unsigned long long)__double_as_longlong(z0) & 0x7FFFFFFFFFFFFFFFull;
+  const unsigned long long b1 = (unsigned long long)__double_as_longlong(z1) & 0x7FFFFFFFFFFFFFFFull;
+  const int E0 = (int)(b0 >> 52), E1 = (int)(b1 >> 52);
+  const int sh0 = 1074 - E0, sh1 = 1074 - E1;
+  if (b0 == 0ull || E0 == 0 || sh0 <= 0 || sh0 > 127 || b1 == 0ull || E1 == 0 || sh1 <= 0 ||
+      sh1 > 127) {
+    g0 = weier_gene_ff(z0);
+    g1 = weier_gene_ff(z1);
+    return;
+  }
+  const unsigned __int128 mask0 = sh0 >= 127 ? ~(unsigned __int128)0
+                                             : (((unsigned __int128)2 << sh0) - 1);
+  const unsigned __int128 mask1 = sh1 >= 127 ? ~(unsigned __int128)0
+                                             : (((unsigned __int128)2 << sh1) - 1);
+  unsigned __int128 r0 = (unsigned __int128)((b0 & ((1ull << 52) - 1ull)) | (1ull << 52)) & mask0;
+  unsigned __int128 r1 = (unsigned __int128)((b1 & ((1ull << 52) - 1ull)) | (1ull << 52)) & mask1;
+  FF s0{0.f, 0.f}, s1{0.f, 0.f};
+  float ak = 1.f;
+  for (int k = 0; k <= 20; ++k, ak *= 0.5f) {
+    const FF c0 = cospi_ff(r0, sh0);
+    const FF c1 = cospi_ff(r1, sh1);
+    s0 = ff_add(s0, FF{-ak * c0.h, -ak * c0.l});
+    s1 = ff_add(s1, FF{-ak * c1.h, -ak * c1.l});
+    r0 = (r0 * 3u) & mask0;
+    r1 = (r1 * 3u) & mask1;
+  }
+  g0 = (double)s0.h + (double)s0.l;
+  g1 = (double)s1.h + (double)s1.l;
+}
+
+// eval_weier_ff_t with two genes per step of each team member, summed in the
+// same order (the same value).
+template <class Team>
+__device__ double eval_weier_ff_pair_t(const FnConst& fc, const double* zbuf, const Team& tm) {
+  const int st = tm.size();
+  double acc = 0.0;
+  int n = tm.rank();
+  for (; n + st < fc.D; n += 2 * st) {
+    double g0, g1;
+    weier_gene_ff2(zbuf[n], zbuf[n + st], g0, g1);
+    acc += g0;
+    acc += g1;
+  }
+  if (n < fc.D) acc += weier_gene_ff(zbuf[n]);
+  acc = tm.sum(acc);
+  return acc + fc.woff64;
 }
 
 template <class Team>

@@ -979,8 +979,8 @@ __global__ void __launch_bounds__(256) decide_kernel(const LargeArgs a, int mode
     int wprec = -1;
     if (!decided) {
       const bool weier = fc.fid == F_WEIERSTRASS;
-      ft = weier ? eval_weier_precise_t(fc, zt, tm) : eval_tier3_t(fc, zt, tm);
-      if (zp) fpv = weier ? eval_weier_precise_t(fc, zp, tm) : eval_tier3_t(fc, zp, tm);
+      ft = weier ? eval_weier_precise_pair_t(fc, zt, tm) : eval_tier3_t(fc, zt, tm);
+      if (zp) fpv = weier ? eval_weier_precise_pair_t(fc, zp, tm) : eval_tier3_t(fc, zp, tm);
       if (weier) {
         // the member's cached value is already float-float (exact to ~1e-12)
         const bool pprec = !zp && !isnan(fp) && a.wprec[td.fit_off + m] == 0.f;
@@ -998,9 +998,9 @@ __global__ void __launch_bounds__(256) decide_kernel(const LargeArgs a, int mode
               precise_rotation_team(a.pop + td.pop_off + (size_t)m * td.DP, a.shift + td.o_off,
                                     a.qt + td.q_off, td.DP, td.D, zmem, tm);
             }
-            fpv = eval_weier_ff_t(fc, zm, tm);
+            fpv = eval_weier_ff_pair_t(fc, zm, tm);
           }
-          ft = eval_weier_ff_t(fc, zt, tm);
+          ft = eval_weier_ff_pair_t(fc, zt, tm);
           wprec = 1;
           if (threadIdx.x == 0 && a.stats) atomicAdd(a.stats + kStatWeierFp64, 1ull);
         }
