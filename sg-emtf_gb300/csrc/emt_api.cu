@@ -356,7 +356,7 @@ int large_upload(emt_handle* h, int64_t pop, int32_t fit, emt::QPlanes* qp) {
   if ((e = h->d_U.ensure((size_t)pop)) || (e = h->d_ftr.ensure((size_t)fit)) ||
       (e = h->d_ttr.ensure((size_t)fit)) || (e = h->d_rank.ensure((size_t)fit)) ||
       (e = h->d_flag.ensure((size_t)fit)) || (e = h->d_ties.ensure((size_t)fit)) ||
-      (e = h->d_ntie.ensure(n)) || (e = h->d_work.ensure((size_t)fit)) || (e = h->d_nwork.ensure(4)) ||
+      (e = h->d_ntie.ensure(n)) || (e = h->d_work.ensure((size_t)fit)) || (e = h->d_nwork.ensure(5)) ||
       (e = h->d_tjob.ensure((size_t)fit)) || (e = h->d_jobs.ensure(2 * (size_t)fit)) ||
       (e = h->d_wprec.ensure((size_t)fit)) ||
       (e = h->d_njob.ensure(n)) || (e = h->d_rwork.ensure((size_t)ritems)) ||
@@ -735,6 +735,7 @@ emt::LargeArgs large_args(emt_handle* h) {
   a.work = h->d_work.p;
   a.rwork = h->d_rwork.p;
   a.nwork = h->d_nwork.p;
+  a.work_cap = (int32_t)h->d_work.n;
   a.rot_grid = h->lrot_grid;
   a.decide_grid = h->ldecide_grid;
   a.algorithm = h->cfg.algorithm;

@@ -146,10 +146,13 @@ struct LargeArgs {
   int32_t* jobs;         // per task (2 x fit offsets): rows to rotate, row | 1 << 16 for a member
   int32_t* njob;         // per task: their number
   double* zr;            // FP64-class rotations of the jobs, 2 x pop offsets, stride DP
-  int32_t* work;         // decision work items: task << 16 | tie
+  int32_t* work;         // decision work items: task << 16 | tie; Weierstrass ties
+                         // from the front, the others from the back (work_cap slots)
   int32_t* rwork;        // rotation work items: task << 16 | column block << 12 | job chunk
-  int32_t* nwork;        // [0] decision items, [1] rotation items, [2] [3] the next
-                         // rotation / decision item to hand out
+  int32_t* nwork;        // [0] Weierstrass decision items, [1] rotation items, [2] [3]
+                         // the next rotation / decision item to hand out, [4] the
+                         // other decision items
+  int32_t work_cap;
   int32_t rot_grid, decide_grid;  // persistent grids of the two re-check kernels
   int32_t algorithm;
   float F, CR, eta_c, p_c, eta_m, p_m;
