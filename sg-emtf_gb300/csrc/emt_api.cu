@@ -185,6 +185,45 @@ float weierstrass_reference_offset() {
 // Orthogonal factor of the FP64 Householder QR of a seeded N(0,1) D x D
 // matrix (Box-Muller on Philox words, purpose P_QR_NORMAL), column signs
 // fixed so that R has a positive diagonal.
+// For each of the vectors w_j = M + j * stride, j in [j0, j1): s = sum over
+// i in [k, D) of v_i w_j[i] (in order of i), s = 2 s / vn, w_j[i] -= s v_i.
+// Four vectors at a time; each vector's operations are exactly the
+// one-vector loop's.
+void reflect4(double* M, size_t stride, int j0, int j1, int D, const double* v, double vn,
+              int k) {
+  int j = j0;
+  for (; j + 4 <= j1; j += 4) {
+    double* w0 = M + (size_t)j * stride;
+    double* w1 = w0 + stride;
+    double* w2 = w1 + stride;
+    double* w3 = w2 + stride;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    for (int i = k; i < D; ++i) {
+      s0 += v[i] * w0[i];
+      s1 += v[i] * w1[i];
+      s2 += v[i] * w2[i];
+      s3 += v[i] * w3[i];
+    }
+    s0 = 2.0 * s0 / vn;
+    s1 = 2.0 * s1 / vn;
+    s2 = 2.0 * s2 / vn;
+    s3 = 2.0 * s3 / vn;
+    for (int i = k; i < D; ++i) {
+      w0[i] -= s0 * v[i];
+      w1[i] -= s1 * v[i];
+      w2[i] -= s2 * v[i];
+      w3[i] -= s3 * v[i];
+    }
+  }
+  for (; j < j1; ++j) {
+    double* w = M + (size_t)j * stride;
+    double s = 0.0;
+    for (int i = k; i < D; ++i) s += v[i] * w[i];
+    s = 2.0 * s / vn;
+    for (int i = k; i < D; ++i) w[i] -= s * v[i];
+  }
+}
+
 void seeded_rotation(uint64_t seed, uint32_t task, int D, std::vector<double>& Q) {
   // A is held column-major (At[c][i] = A[i][c]) so the Householder column
   // updates run over contiguous memory; every sum keeps its order.
@@ -217,19 +256,12 @@ void seeded_rotation(uint64_t seed, uint32_t task, int D, std::vector<double>& Q
     double vn = 0.0;
     for (int i = k; i < D; ++i) vn += v[i] * v[i];
     if (vn == 0.0) continue;
-    for (int c = k; c < D; ++c) {
-      double* ac = At.data() + (size_t)c * D;
-      double s = 0.0;
-      for (int i = k; i < D; ++i) s += v[i] * ac[i];
-      s = 2.0 * s / vn;
-      for (int i = k; i < D; ++i) ac[i] -= s * v[i];
-    }
-    for (int r = 0; r < D; ++r) {
-      double s = 0.0;
-      for (int i = k; i < D; ++i) s += Q[(size_t)r * D + i] * v[i];
-      s = 2.0 * s / vn;
-      for (int i = k; i < D; ++i) Q[(size_t)r * D + i] -= s * v[i];
-    }
+    // A <- H A column by column and Q <- Q H row by row, four columns (rows)
+    // at a time: their dot products are independent chains, interleaved so
+    // the adds overlap; each keeps its own order over i, so every value is
+    // the one-at-a-time loop's
+    reflect4(At.data(), (size_t)D, k, D, D, v.data(), vn, k);
+    reflect4(Q.data(), (size_t)D, 0, D, D, v.data(), vn, k);
   }
   for (int c = 0; c < D; ++c)
     if (At[(size_t)c * D + c] < 0)
