@@ -224,10 +224,62 @@ void reflect4(double* M, size_t stride, int j0, int j1, int D, const double* v, 
   }
 }
 
+// Orthogonal factor Q (row-major, D x D) of the Householder QR of A, held
+// column-major in At (At[c][i] = A[i][c]; overwritten); Q's columns are
+// negated where A's diagonal ends negative.
+void householder_q(std::vector<double>& At, int D, std::vector<double>& Q) {
+  // Householder QR: step k reflects with v_k = a_k - alpha e_k (a_k: column
+  // k of A from row k on, after steps 0..k-1; alpha = -sign(a_kk) |a_k|);
+  // every column c >= k of A and every row of Q gets
+  // w -= (2 (v_k . w) / |v_k|^2) v_k.  Each column and each row thus sees the
+  // reflectors in the order k = 0, 1, ..., and nothing else: the steps are
+  // applied left-looking, a block of kBlk columns (rows) at a time, so each
+  // v_k is read once per block instead of streaming all of A and Q per step.
+  // Four vectors of a block at a time (reflect4): their dot products are
+  // independent chains.  Every operation and every sum's order over i are
+  // the step-by-step loop's, so Q is the same bit for bit.
+  constexpr int kBlk = 16;
+  std::vector<double> V((size_t)D * D, 0.0), vn(D, 0.0);
+  std::vector<char> valid(D, 0);
+  double* A = At.data();
+  for (int c0 = 0; c0 < D; c0 += kBlk) {
+    const int c1 = std::min(D, c0 + kBlk);
+    for (int k = 0; k < c0 && k < D - 1; ++k)
+      if (valid[k]) reflect4(A, (size_t)D, c0, c1, D, V.data() + (size_t)k * D, vn[k], k);
+    for (int k = c0; k < c1 && k < D - 1; ++k) {
+      double nrm = 0.0;
+      const double* ak = A + (size_t)k * D;
+      for (int i = k; i < D; ++i) nrm += ak[i] * ak[i];
+      nrm = std::sqrt(nrm);
+      if (nrm == 0.0) continue;
+      const double alpha = ak[k] > 0 ? -nrm : nrm;
+      double* v = V.data() + (size_t)k * D;
+      for (int i = k; i < D; ++i) v[i] = ak[i];
+      v[k] -= alpha;
+      double n2 = 0.0;
+      for (int i = k; i < D; ++i) n2 += v[i] * v[i];
+      if (n2 == 0.0) continue;
+      vn[k] = n2;
+      valid[k] = 1;
+      reflect4(A, (size_t)D, k, c1, D, v, n2, k);  // this column and the block's later ones
+    }
+  }
+  Q.assign((size_t)D * D, 0.0);
+  for (int i = 0; i < D; ++i) Q[(size_t)i * D + i] = 1.0;
+  for (int r0 = 0; r0 < D; r0 += kBlk) {
+    const int r1 = std::min(D, r0 + kBlk);
+    for (int k = 0; k < D - 1; ++k)
+      if (valid[k]) reflect4(Q.data(), (size_t)D, r0, r1, D, V.data() + (size_t)k * D, vn[k], k);
+  }
+  for (int c = 0; c < D; ++c)
+    if (At[(size_t)c * D + c] < 0)
+      for (int r = 0; r < D; ++r) Q[(size_t)r * D + c] = -Q[(size_t)r * D + c];
+}
+
 void seeded_rotation(uint64_t seed, uint32_t task, int D, std::vector<double>& Q) {
   // A is held column-major (At[c][i] = A[i][c]) so the Householder column
   // updates run over contiguous memory; every sum keeps its order.
-  std::vector<double> At((size_t)D * D), v(D);
+  std::vector<double> At((size_t)D * D);
   for (int r = 0; r < D; ++r)
     for (int c = 0; c < D; c += 4) {
       emt::U4 w = emt::draw(seed, task, 0, (uint32_t)r, emt::P_QR_NORMAL, (uint32_t)(c >> 2));
@@ -241,31 +293,7 @@ void seeded_rotation(uint64_t seed, uint32_t task, int D, std::vector<double>& Q
         if (c + 2 * h + 1 < D) At[(size_t)(c + 2 * h + 1) * D + r] = rad * std::sin(th);
       }
     }
-  Q.assign((size_t)D * D, 0.0);
-  for (int i = 0; i < D; ++i) Q[(size_t)i * D + i] = 1.0;
-  for (int k = 0; k < D - 1; ++k) {
-    double nrm = 0.0;
-    const double* ak = At.data() + (size_t)k * D;
-    for (int i = k; i < D; ++i) nrm += ak[i] * ak[i];
-    nrm = std::sqrt(nrm);
-    if (nrm == 0.0) continue;
-    double alpha = ak[k] > 0 ? -nrm : nrm;
-    std::fill(v.begin(), v.end(), 0.0);
-    for (int i = k; i < D; ++i) v[i] = ak[i];
-    v[k] -= alpha;
-    double vn = 0.0;
-    for (int i = k; i < D; ++i) vn += v[i] * v[i];
-    if (vn == 0.0) continue;
-    // A <- H A column by column and Q <- Q H row by row, four columns (rows)
-    // at a time: their dot products are independent chains, interleaved so
-    // the adds overlap; each keeps its own order over i, so every value is
-    // the one-at-a-time loop's
-    reflect4(At.data(), (size_t)D, k, D, D, v.data(), vn, k);
-    reflect4(Q.data(), (size_t)D, 0, D, D, v.data(), vn, k);
-  }
-  for (int c = 0; c < D; ++c)
-    if (At[(size_t)c * D + c] < 0)
-      for (int r = 0; r < D; ++r) Q[(size_t)r * D + c] = -Q[(size_t)r * D + c];
+  householder_q(At, D, Q);
 }
 
 int max_smem_optin(int device) {
