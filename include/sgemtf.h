@@ -249,6 +249,14 @@ EMT_API int32_t emt_function_from_reference(int32_t reference_type);
 /* The function's box [lo, hi]; reference_boxes != 0 gives SG-EMTF.cu:197-214. */
 EMT_API int emt_function_box(int32_t function, int32_t reference_boxes, float* lo, float* hi);
 
+/* The rotation EMT_ROTATION_SEEDED_QR gives task number `task` (its index in
+ * the handle) of a handle configured with `seed`: the orthogonal factor of
+ * the FP64 Householder QR of a seeded N(0,1) dim x dim matrix, row-major in
+ * q (dim * dim doubles), before the handle rounds it to FP32.  Host code
+ * only; no device is needed.  No reference counterpart: the reference's
+ * rotation is a diagonal scale (SG-EMTF.cu:181-195). */
+EMT_API int emt_seeded_rotation(uint64_t seed, int32_t task, int32_t dim, double* q);
+
 /* Replaces the reference's initialization() (SG-EMTF.cu:293-380): validates
  * the configuration and binds the device.  No task exists yet. */
 EMT_API int emt_create(const emt_config* cfg, emt_handle_t** out);

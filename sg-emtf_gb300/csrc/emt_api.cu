@@ -1011,6 +1011,18 @@ void emt_config_default(emt_config* cfg) {
 
 int32_t emt_function_from_reference(int32_t t) { return (t >= 0 && t < 7) ? kRefToFid[t] : -1; }
 
+int emt_seeded_rotation(uint64_t seed, int32_t task, int32_t dim, double* q) {
+  if (!q || task < 0 || dim < 1 || dim > EMT_MAX_DIM) return EMT_ERR_INVALID_ARG;
+  std::vector<double> Q;
+  try {
+    seeded_rotation(seed, (uint32_t)task, dim, Q);
+  } catch (const std::bad_alloc&) {
+    return EMT_ERR_OUT_OF_MEMORY;
+  }
+  std::memcpy(q, Q.data(), sizeof(double) * Q.size());
+  return EMT_OK;
+}
+
 int emt_function_box(int32_t fid, int32_t reference_boxes, float* lo, float* hi) {
   if (fid < 0 || fid >= EMT_NUM_FUNCTIONS || !lo || !hi) return EMT_ERR_INVALID_ARG;
   if (reference_boxes) {

@@ -42,7 +42,8 @@ MAX_DIM_LARGE, MAX_POP_LARGE = 1024, 512
 NOALLOC_EXCHANGE_FLOATS = 1 << 19
 
 EXPORTED = [
-    "emt_config_default", "emt_function_from_reference", "emt_function_box", "emt_create",
+    "emt_config_default", "emt_function_from_reference", "emt_function_box",
+    "emt_seeded_rotation", "emt_create",
     "emt_add_tasks", "emt_reset", "emt_run", "emt_run_noalloc", "emt_tune", "emt_time_rotation",
     "emt_get_phase_cycles",
     "emt_sync", "emt_get_best", "emt_get_best_all",
@@ -187,6 +188,7 @@ def lib():
         L.emt_function_from_reference.argtypes = [i32]
         L.emt_function_from_reference.restype = i32
         L.emt_function_box.argtypes = [i32, i32, f32p, f32p]
+        L.emt_seeded_rotation.argtypes = [ctypes.c_uint64, i32, i32, ctypes.POINTER(ctypes.c_double)]
         L.emt_create.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(vp)]
         L.emt_add_tasks.argtypes = [vp, i32, ctypes.POINTER(TaskDescC)]
         L.emt_reset.argtypes = [vp, vp]
@@ -254,6 +256,17 @@ def lib():
 
 def status_string(s):
     return lib().emt_status_string(s).decode()
+
+
+def seeded_rotation(seed, task, dim):
+    """emt_seeded_rotation: the FP64 rotation EMT_ROTATION_SEEDED_QR gives task
+    `task` of a handle with this seed (host only)."""
+    q = np.zeros((dim, dim), np.float64)
+    rc = lib().emt_seeded_rotation(int(seed), int(task), int(dim),
+                                   q.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    if rc:
+        raise EngineError(rc, "seeded_rotation")
+    return q
 
 
 def function_box(fid, reference_boxes=False):
