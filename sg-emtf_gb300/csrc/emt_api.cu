@@ -1154,7 +1154,7 @@ int join_tasks(emt_handle* h, std::vector<HostTask>& add) {
   return EMT_OK;
 }
 
-int emt_add_tasks(emt_handle_t* h, int32_t n, const emt_task_desc* td) {
+static int add_tasks_impl(emt_handle_t* h, int32_t n, const emt_task_desc* td) {
   if (!h) return EMT_ERR_INVALID_ARG;
   const NvtxRange range("emt_add_tasks");
   if (n < 0 || (n > 0 && !td)) return h->fail(EMT_ERR_INVALID_ARG, "bad task array");
@@ -1283,7 +1283,17 @@ int emt_add_tasks(emt_handle_t* h, int32_t n, const emt_task_desc* td) {
   return EMT_OK;
 }
 
-int emt_reset(emt_handle_t* h, void* stream) {
+// Host allocations that grow with the handle (task matrices, staging
+// buffers) fail as EMT_ERR_OUT_OF_MEMORY instead of unwinding through the C ABI.
+int emt_add_tasks(emt_handle_t* h, int32_t n, const emt_task_desc* td) {
+  try {
+    return add_tasks_impl(h, n, td);
+  } catch (const std::bad_alloc&) {
+    return h ? h->fail(EMT_ERR_OUT_OF_MEMORY, "host memory") : EMT_ERR_OUT_OF_MEMORY;
+  }
+}
+
+static int reset_impl(emt_handle_t* h, void* stream) {
   if (!h) return EMT_ERR_INVALID_ARG;
   const NvtxRange range("emt_reset");
   int rc = upload(h);
@@ -1303,6 +1313,14 @@ int emt_reset(emt_handle_t* h, void* stream) {
   h->gen_joined = 0;
   h->elite_parity = 0;
   return EMT_OK;
+}
+
+int emt_reset(emt_handle_t* h, void* stream) {
+  try {
+    return reset_impl(h, stream);
+  } catch (const std::bad_alloc&) {
+    return h ? h->fail(EMT_ERR_OUT_OF_MEMORY, "host memory") : EMT_ERR_OUT_OF_MEMORY;
+  }
 }
 
 int emt_run(emt_handle_t* h, int32_t generations, void* stream) {
