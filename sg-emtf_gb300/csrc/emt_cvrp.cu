@@ -749,7 +749,7 @@ int emt_cvrp_create(const emt_cvrp_config* cfg, emt_cvrp_handle_t** out) {
   return EMT_OK;
 }
 
-int emt_cvrp_add_instances(emt_cvrp_handle_t* h, int32_t n, const emt_cvrp_instance* in) {
+static int add_instances_impl(emt_cvrp_handle_t* h, int32_t n, const emt_cvrp_instance* in) {
   if (!h) return EMT_ERR_INVALID_ARG;
   if (n < 0 || (n > 0 && !in)) return h->fail(EMT_ERR_INVALID_ARG, "bad instance array");
   int smax = 0;
@@ -809,7 +809,17 @@ int emt_cvrp_add_instances(emt_cvrp_handle_t* h, int32_t n, const emt_cvrp_insta
   return EMT_OK;
 }
 
-int emt_cvrp_reset(emt_cvrp_handle_t* h, void* stream) {
+// Host allocations that grow with the handle fail as EMT_ERR_OUT_OF_MEMORY
+// instead of unwinding through the C ABI.
+int emt_cvrp_add_instances(emt_cvrp_handle_t* h, int32_t n, const emt_cvrp_instance* in) {
+  try {
+    return add_instances_impl(h, n, in);
+  } catch (const std::bad_alloc&) {
+    return h ? h->fail(EMT_ERR_OUT_OF_MEMORY, "host memory") : EMT_ERR_OUT_OF_MEMORY;
+  }
+}
+
+static int cvrp_reset_impl(emt_cvrp_handle_t* h, void* stream) {
   if (!h) return EMT_ERR_INVALID_ARG;
   int rc = cvrp_upload(h);
   if (rc) return rc;
@@ -820,6 +830,14 @@ int emt_cvrp_reset(emt_cvrp_handle_t* h, void* stream) {
   h->gdone = 0;
   h->parity = 0;
   return EMT_OK;
+}
+
+int emt_cvrp_reset(emt_cvrp_handle_t* h, void* stream) {
+  try {
+    return cvrp_reset_impl(h, stream);
+  } catch (const std::bad_alloc&) {
+    return h ? h->fail(EMT_ERR_OUT_OF_MEMORY, "host memory") : EMT_ERR_OUT_OF_MEMORY;
+  }
 }
 
 int emt_cvrp_run(emt_cvrp_handle_t* h, int32_t generations, void* stream) {

@@ -172,23 +172,28 @@ EMT_API int emt_service_submit(emt_service_t* s, int32_t n, const emt_task_desc*
   if (!s) return EMT_ERR_INVALID_ARG;
   if (n < 1 || !tasks || !std::isfinite(arrival_ms))
     return s->fail(EMT_ERR_INVALID_ARG, "a batch needs tasks and a finite arrival time");
-  Batch b;
-  b.arrival = arrival_ms;
-  b.desc.assign(tasks, tasks + n);
-  b.rot.resize(n);
-  b.diag.resize(n);
-  b.shift.resize(n);
-  for (int t = 0; t < n; ++t) {
-    const emt_task_desc& d = tasks[t];
-    if (d.dim < 1 || d.dim > EMT_MAX_FUSED_DIM)
+  for (int t = 0; t < n; ++t)
+    if (tasks[t].dim < 1 || tasks[t].dim > EMT_MAX_FUSED_DIM)
       return s->fail(EMT_ERR_INVALID_ARG, "task " + std::to_string(t) +
                                               ": the service serves islands of D <= 128");
-    const size_t D = (size_t)d.dim;
-    if (d.rotation_matrix) b.rot[t].assign(d.rotation_matrix, d.rotation_matrix + D * D);
-    if (d.diag) b.diag[t].assign(d.diag, d.diag + D);
-    if (d.shift) b.shift[t].assign(d.shift, d.shift + D);
+  try {  // the batch keeps copies of the caller's arrays
+    Batch b;
+    b.arrival = arrival_ms;
+    b.desc.assign(tasks, tasks + n);
+    b.rot.resize(n);
+    b.diag.resize(n);
+    b.shift.resize(n);
+    for (int t = 0; t < n; ++t) {
+      const emt_task_desc& d = tasks[t];
+      const size_t D = (size_t)d.dim;
+      if (d.rotation_matrix) b.rot[t].assign(d.rotation_matrix, d.rotation_matrix + D * D);
+      if (d.diag) b.diag[t].assign(d.diag, d.diag + D);
+      if (d.shift) b.shift[t].assign(d.shift, d.shift + D);
+    }
+    s->batches.push_back(std::move(b));
+  } catch (const std::bad_alloc&) {
+    return s->fail(EMT_ERR_OUT_OF_MEMORY, "host memory for the batch");
   }
-  s->batches.push_back(std::move(b));
   if (batch) *batch = (int32_t)s->batches.size() - 1;
   return EMT_OK;
 }
