@@ -1025,6 +1025,10 @@ __global__ void __launch_bounds__(256) decide_kernel(const LargeArgs a, int mode
   }
 }
 
+// A task's accepted rows are copied by kApplySlices CTAs (its float4s
+// interleaved over them); the first also moves the fitness values and counts.
+constexpr int kApplySlices = 4;
+
 __global__ void __launch_bounds__(256) apply_kernel(const LargeArgs a, int mode) {
   const int task = blockIdx.x;
   const TaskDev td = a.tasks[task];
@@ -1032,10 +1036,8 @@ __global__ void __launch_bounds__(256) apply_kernel(const LargeArgs a, int mode)
   int k = 0;
   const int nrows = sel_rows(a, task, mode, k);
   const int DP = td.DP, nq = DP >> 2;
-  __shared__ int acc;
-  if (threadIdx.x == 0) acc = 0;
-  __syncthreads();
-  for (int it = threadIdx.x; it < nrows * nq; it += blockDim.x) {
+  for (int it = blockIdx.y * blockDim.x + threadIdx.x; it < nrows * nq;
+       it += kApplySlices * blockDim.x) {
     const int c = it / nq, q = it - c * nq;
     if (a.flag[td.fit_off + c] & 1) {
       const int m = sel_target(a, td, mode, k, c);
@@ -1043,6 +1045,10 @@ __global__ void __launch_bounds__(256) apply_kernel(const LargeArgs a, int mode)
           reinterpret_cast<const float4*>(a.U + td.pop_off + (size_t)c * DP)[q];
     }
   }
+  if (blockIdx.y != 0) return;
+  __shared__ int acc;
+  if (threadIdx.x == 0) acc = 0;
+  __syncthreads();
   for (int c = threadIdx.x; c < nrows; c += blockDim.x) {
     const int f = a.flag[td.fit_off + c];
     if (f & 1) {
@@ -1160,7 +1166,8 @@ int emt_large_selection(const emt::LargeArgs& a, int mode, void* stream) {
   emt::large::classify_kernel<<<a.n_tasks, 256, 0, (cudaStream_t)stream>>>(a, mode);
   emt::large::rot_kernel<<<a.rot_grid, emt::large::kRotCols, 0, (cudaStream_t)stream>>>(a);
   emt::large::decide_kernel<<<a.decide_grid, 256, 0, (cudaStream_t)stream>>>(a, mode);
-  emt::large::apply_kernel<<<a.n_tasks, 256, 0, (cudaStream_t)stream>>>(a, mode);
+  emt::large::apply_kernel<<<dim3(a.n_tasks, emt::large::kApplySlices), 256, 0, (cudaStream_t)stream>>>(
+      a, mode);
   return (int)cudaGetLastError();
 }
 
